@@ -1,0 +1,162 @@
+/*
+ * fm3dt_gpu.h -- C ABI of the GB300 forward teleseismic traveltime solver.
+ *
+ * Drop-in replacement for the forward-solve path of the Parallel Fast
+ * Marching Method program fm3dt_parallel (fm3dt_parallel.f90, "F" below).
+ * The reference is one monolithic Fortran/MPI program with no library
+ * interface; each entry point here replaces one stage of its per-source loop
+ * (F:6371-6599) and takes plain host pointers, so a Fortran host binds it with
+ * ISO_C_BINDING and a C/C++ or Python host with a prototype or ctypes.
+ *
+ * Conventions
+ *  - The caller owns every host buffer; the library owns device memory.
+ *  - Every function returns FM3DT_OK (0) or a negative FM3DT_E* code and never
+ *    exits the process; fm3dt_last_error() gives a message for the last
+ *    failure of that context (or of a failed create when ctx is NULL).
+ *  - One context per host thread; each context has its own CUDA stream.
+ *    Distinct contexts may be used concurrently from different threads.
+ *  - Layouts follow the reference: traveltime fields and boundary frames are
+ *    phi-fastest (F:6191 ttn(iz,ix,ir)), velocity nodes r-fastest (F:6118-6125).
+ *  - Grid index ir = 1 is the top layer and ir = nnr the bottom layer, where
+ *    the teleseismic wavefront is injected (F:6908-6913).
+ */
+#ifndef FM3DT_GPU_H
+#define FM3DT_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    FM3DT_OK = 0,
+    FM3DT_EINVAL = -1,        /* bad argument or dimension */
+    FM3DT_ENOMEM = -2,        /* device allocation failed */
+    FM3DT_ECUDA = -3,         /* CUDA runtime error */
+    FM3DT_ENOCONV = -4,       /* solver round limit reached before convergence */
+    FM3DT_ERANGE = -5,        /* receiver or ray support outside the grids */
+    FM3DT_ESTATE = -6,        /* call out of order (e.g. solve before velocity) */
+    FM3DT_ENODEV = -7         /* no CUDA device */
+};
+
+enum {
+    FM3DT_FP64 = 0,           /* double-precision stencils (plain drop-in) */
+    FM3DT_FP32_OFFSET = 1     /* single-precision stencils on times stored as
+                                 offsets from each event's earliest boundary time */
+};
+
+/* Grid header exactly as the six .vtx header lines give it (F:6103-6108):
+ * heights in km, latitude/longitude and angular steps in degrees.  The
+ * library converts units like F:6110-6117.  fom is line 10 of
+ * fm3dt_parallel.in (0 first order, 1 mixed order; F:100-111). */
+typedef struct {
+    int nvr, nvx, nvz;
+    double gor, goxd, gozd;
+    double dvr, dvxd, dvzd;
+    int nnr, nnx, nnz;
+    double rgor, rgoxd, rgozd;
+    double dnr, dnxd, dnzd;
+    double earth;
+    int fom;
+    int precision;            /* FM3DT_FP64 or FM3DT_FP32_OFFSET */
+    int max_events;           /* events solved together per fm3dt_solve call */
+} fm3dt_grid_desc;
+
+/* Per-solve report. */
+typedef struct {
+    int rounds;               /* tile rounds until no tile was active */
+    int converged;            /* 1 when every event reached its fixed point */
+    int64_t tile_updates;     /* tile activations processed */
+    int64_t node_passes;      /* node updates (tile nodes x in-tile passes) */
+    int64_t tile_nodes;       /* grid nodes staged by all tile activations */
+    double ms;                /* device time of the whole solve */
+    double round_ms;          /* device time inside the tile-round kernels */
+    int round_launches;       /* tile-round kernel launches */
+} fm3dt_status;
+
+typedef struct fm3dt_ctx fm3dt_ctx;
+
+/* Replaces F:6050-6191 (topology, input conversion, allocation).  Allocates
+ * the device fields for desc->max_events events. */
+int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out);
+
+/* Replaces F:6172 gridder (F:6989-7038): cubic B-spline interpolation of the
+ * velocity nodes onto every propagation node, including the one-node ghost
+ * ring.  velv: (nvz+2)(nvx+2)(nvr+2) doubles in .vtx order (r fastest). */
+int fm3dt_set_velocity(fm3dt_ctx *ctx, const double *velv);
+
+/* Replaces start_fmm (F:6894-6961) and the BSP fast-marching loop
+ * (F:6371-6451) for nev <= max_events sources.  boundary: nev frames of
+ * nnz*nnx doubles, phi fastest -- the itimes.out records of these sources;
+ * values <= 0 mean "no time" (F:6935-6936), positive values are fixed. */
+int fm3dt_solve(fm3dt_ctx *ctx, int nev, const double *boundary, fm3dt_status *st);
+
+/* Same as fm3dt_solve with the boundary frames already in device memory
+ * (d_boundary is a device pointer, e.g. frames kept resident between
+ * tomography iterations). */
+int fm3dt_solve_device(fm3dt_ctx *ctx, int nev, const double *d_boundary, fm3dt_status *st);
+
+/* Same solve with the boundary frames generated on the device from a
+ * synthetic teleseismic plane wave per event: params is nev x 4 doubles
+ * (t0 s, p s/km, cos az, sin az); time at a bottom node = t0 + p * d, d the
+ * distance of the node from the section centre along the propagation azimuth
+ * in the tangent plane of the bottom surface. */
+int fm3dt_solve_planewave(fm3dt_ctx *ctx, int nev, const double *params, fm3dt_status *st);
+
+/* Replaces srtimes (F:7040-7248): trilinear receiver times of every solved
+ * event, accumulated in single precision like REAL(4) trr (F:47, 7098-7106).
+ * rcr: receiver height km; rcx: colatitude rad; rcz: longitude rad
+ * (converted like F:6313-6314).  out: nev x nrc floats, event-major (the
+ * rtravel.out order, F:7174-7176). */
+int fm3dt_receiver_times(fm3dt_ctx *ctx, int nrc, const double *rcr, const double *rcx,
+                         const double *rcz, float *out);
+
+/* Replaces parallel_rpaths and the Frechet writer merge (F:6456-6599,
+ * F:7250-7777): one ray per (event, receiver), traced from the receiver down
+ * the traveltime gradient with step dnr until it leaves the grid, and its
+ * Frechet row -integral(B/v^2 ds) accumulated in single precision.
+ * Rows are returned as CSR over nev*nrc rows (event-major): row_ptr has
+ * nev*nrc+1 entries; cols are the reference's 1-based velocity-node columns
+ * ((iz*(nvx+2)+ix)*(nvr+2)+ir+1), ascending; vals single precision.  Only
+ * entries with |value| >= 1e-6 are kept (F:7263).  cap is the capacity of
+ * cols/vals; if the rows need more, FM3DT_ERANGE is returned with
+ * row_ptr[nev*nrc] = the required count.  endpoints (nullable): nev*nrc*3
+ * doubles (height km, colat rad, lon rad).  Pass cols = vals = NULL and
+ * cap = 0 to trace rays only. */
+int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double *rcx,
+                       const double *rcz, int64_t *row_ptr, int32_t *cols, float *vals,
+                       int64_t cap, double *endpoints);
+
+/* Copies the solved traveltime field of one event to the host: nnr*nnx*nnz
+ * doubles, phi fastest (absolute seconds in both precisions; unreached nodes
+ * are 0.0 like the reference's ttn). */
+int fm3dt_get_times(fm3dt_ctx *ctx, int event, double *ttn);
+
+/* Copies the gridded velocity (the reference's veln, F:6993) to the host:
+ * (nnr+3)(nnx+3)(nnz+3) doubles, phi fastest, node indices -1..n+1. */
+int fm3dt_get_velocity(fm3dt_ctx *ctx, double *veln);
+
+/* Uploads a traveltime field for one event (nnr*nnx*nnz doubles, phi
+ * fastest), e.g. to trace rays through a field computed elsewhere. */
+int fm3dt_set_times(fm3dt_ctx *ctx, int event, int nev_total, const double *ttn);
+
+/* Solver tuning: tile shape index, in-tile pass cap and round cap
+ * (0 keeps the current value). */
+int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rounds);
+
+/* Number of available tile shapes and the shape (TR, TX, TZ) of one. */
+int fm3dt_tile_shapes(int *count);
+int fm3dt_tile_shape(int index, int *tr, int *tx, int *tz);
+
+/* Kernel launches made by this context since creation. */
+int64_t fm3dt_launch_count(const fm3dt_ctx *ctx);
+
+const char *fm3dt_last_error(const fm3dt_ctx *ctx);
+
+void fm3dt_ctx_destroy(fm3dt_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

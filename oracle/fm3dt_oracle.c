@@ -1,0 +1,971 @@
+/*
+ * fm3dt_oracle.c -- CPU oracle (test infrastructure only) for the forward
+ * teleseismic traveltime path of fm3dt_parallel.f90 ("F" below).
+ *
+ * Parity status: UNPINNED by reference outputs (no Fortran/MPI toolchain, no
+ * reference tests or golden vectors, itimes.out missing).  Pinned by analytic
+ * known-answer tests instead.  See fm3dt_oracle.h for units and layouts.
+ *
+ * Every routine restates the serial behaviour of the cited Fortran lines with
+ * the reference's operation order (left-to-right, no fused multiply-add), so
+ * that double-precision results follow the reference's rounding.  Build with
+ * -ffp-contract=off.  Subdomain offsets of the MPI code are taken as those of
+ * a single subdomain (roffset = xoffset = zoffset = 1), which removes the
+ * (offset-1)*spacing terms (they are exactly 0.0).
+ */
+#include "fm3dt_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* F:61 declares pi as REAL(KIND=i10) but initialises it from the default-kind
+ * (single precision) literal 3.1415926535898, so the value the reference uses
+ * is that literal rounded to float and widened. */
+double orc_pi(void) { return (double)3.1415926535898f; }
+
+void orc_grid_from_header(const int nv[3], const double vorig[3], const double vstep[3],
+                          const int nn[3], const double norig[3], const double nstep[3],
+                          double earth, orc_grid *g)
+{
+    const double pi = orc_pi();
+    g->nvr = nv[0]; g->nvx = nv[1]; g->nvz = nv[2];
+    g->gor = vorig[0];
+    g->dvr = vstep[0];
+    /* F:6110-6117 */
+    g->dvx = vstep[1] * pi / 180.0;
+    g->dvz = vstep[2] * pi / 180.0;
+    g->gox = (90.0 - vorig[1]) * pi / 180.0;
+    g->goz = vorig[2] * pi / 180.0;
+    g->nnr = nn[0]; g->nnx = nn[1]; g->nnz = nn[2];
+    g->rgor = norig[0];
+    g->dnr = nstep[0];
+    g->dnx = nstep[1] * pi / 180.0;
+    g->dnz = nstep[2] * pi / 180.0;
+    g->rgox = (90.0 - norig[1]) * pi / 180.0;
+    g->rgoz = norig[2] * pi / 180.0;
+    g->earth = earth;
+}
+
+void orc_latlon_to_rad(int n, const double *lat, const double *lon, double *colat, double *lonr)
+{
+    const double pi = orc_pi();
+    for (int i = 0; i < n; ++i) {
+        colat[i] = (90.0 - lat[i]) * pi / 180.0;   /* F:6313 */
+        lonr[i] = lon[i] * pi / 180.0;             /* F:6314 */
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* B-spline weights (F:7002-7005 and repeated at F:7010-7021, 7671-7682)     */
+/* ------------------------------------------------------------------------ */
+static void bspline4(double u, double w[4])
+{
+    const double u2 = u * u, u3 = u * u * u;
+    const double om = 1.0 - u;
+    w[0] = om * om * om / 6.0;
+    w[1] = (4.0 - 6.0 * u2 + 3.0 * u3) / 6.0;
+    w[2] = (1.0 + 3.0 * u + 3.0 * u2 - 3.0 * u3) / 6.0;
+    w[3] = u3 / 6.0;
+}
+
+#define VELV(g, k, j, i) ((size_t)(k) + (size_t)((g)->nvr + 2) * ((size_t)(j) + (size_t)((g)->nvx + 2) * (size_t)(i)))
+#define VELN(g, iz, ix, ir) ((size_t)((iz) + 1) + (size_t)((g)->nnz + 3) * ((size_t)((ix) + 1) + (size_t)((g)->nnx + 3) * (size_t)((ir) + 1)))
+
+static int clampi(int v, int lo, int hi, int *hit)
+{
+    if (v < lo) { *hit = 1; return lo; }
+    if (v > hi) { *hit = 1; return hi; }
+    return v;
+}
+
+int orc_gridder(const orc_grid *g, const double *velv, double *veln, int *nclamped)
+{
+    int nclamp = 0;
+    for (int i = -1; i <= g->nnz + 1; ++i) {
+        /* F:6996-6998 with zoffset = 1 */
+        const double zpos = g->rgoz + (double)(i - 1) * g->dnz - g->goz;
+        const int zi = (int)floor(zpos / g->dvz) + 1;
+        const double distz = zpos - (double)(zi - 1) * g->dvz;
+        double wi[4];
+        bspline4(distz / g->dvz, wi);
+        for (int j = -1; j <= g->nnx + 1; ++j) {
+            const double xpos = g->rgox + (double)(j - 1) * g->dnx - g->gox;
+            const int xi = (int)floor(xpos / g->dvx) + 1;
+            const double distx = xpos - (double)(xi - 1) * g->dvx;
+            double vi[4];
+            bspline4(distx / g->dvx, vi);
+            for (int k = -1; k <= g->nnr + 1; ++k) {
+                /* F:7015-7016: ri from depth below the velocity origin */
+                const int ri = (int)floor((g->gor - g->rgor + (double)(k - 1) * g->dnr) / g->dvr) + 1;
+                const double distr = -(g->rgor - (double)(k - 1) * g->dnr) + (g->gor - (double)(ri - 1) * g->dvr);
+                double ui[4];
+                bspline4(distr / g->dvr, ui);
+                double sumi = 0.0;
+                for (int i1 = 1; i1 <= 4; ++i1) {
+                    double sumj = 0.0;
+                    for (int j1 = 1; j1 <= 4; ++j1) {
+                        double sumk = 0.0;
+                        for (int k1 = 1; k1 <= 4; ++k1) {
+                            int hit = 0;
+                            const int a = clampi(ri - 2 + k1, 0, g->nvr + 1, &hit);
+                            const int b = clampi(xi - 2 + j1, 0, g->nvx + 1, &hit);
+                            const int c = clampi(zi - 2 + i1, 0, g->nvz + 1, &hit);
+                            nclamp += hit;
+                            sumk = sumk + ui[k1 - 1] * velv[VELV(g, a, b, c)];
+                        }
+                        sumj = sumj + vi[j1 - 1] * sumk;
+                    }
+                    sumi = sumi + wi[i1 - 1] * sumj;
+                }
+                veln[VELN(g, i, j, k)] = sumi;
+            }
+        }
+    }
+    if (nclamped) *nclamped = nclamp;
+    return nclamp ? -1 : 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Serial fast marching (F:78-155, 535-1098, 6894-6961)                      */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    const orc_grid *g;
+    const double *veln;
+    int nnr, nnx, nnz;
+    int NZ2, NX2;          /* padded strides: indices 0..n+1 like F:6191 */
+    double *ttn;           /* padded (nnz+2)(nnx+2)(nnr+2) */
+    int *nsts;             /* padded, same shape */
+    int *hr, *hx, *hz;     /* heap btg (F:68-75), 1-based */
+    int ntr;
+} fmm_state;
+
+#define TI(s, iz, ix, ir) ((size_t)(iz) + (size_t)(s)->NZ2 * ((size_t)(ix) + (size_t)(s)->NX2 * (size_t)(ir)))
+#define TT(s, iz, ix, ir) ((s)->ttn[TI(s, iz, ix, ir)])
+#define NS(s, iz, ix, ir) ((s)->nsts[TI(s, iz, ix, ir)])
+
+static double sq(double x) { return x * x; }
+
+/* node radius and r*sin(colatitude) at the centre node (F:542-543, 642-643) */
+static void centre_geom(const fmm_state *s, int ix, int ir, double *ri, double *risti)
+{
+    const orc_grid *g = s->g;
+    *ri = g->rgor - (double)(ir - 1) * g->dnr + g->earth;
+    *risti = *ri * sin(g->rgox + (double)(ix - 1) * g->dnx);
+}
+
+/* fouds1_all: first-order update over the eight octants (F:535-633). */
+static void fouds1(fmm_state *s, int iz, int ix, int ir)
+{
+    const orc_grid *g = s->g;
+    const double dnr = g->dnr, dnx = g->dnx, dnz = g->dnz;
+    double ri, risti;
+    centre_geom(s, ix, ir, &ri, &risti);
+    const double slown = 1.0 / s->veln[VELN(g, iz, ix, ir)];
+    int tsw1 = 0;
+    double travm = 0.0;
+    for (int i = ir - 1; i <= ir + 1; i += 2)
+        for (int j = ix - 1; j <= ix + 1; j += 2)
+            for (int k = iz - 1; k <= iz + 1; k += 2) {
+                if (i < 1 || i > s->nnr || j < 1 || j > s->nnx || k < 1 || k > s->nnz) continue;
+                int swsol = 0;
+                double a = 0, b = 0, c = 0, tref = 0;
+                if (NS(s, iz, ix, i) == 0) {
+                    swsol = 1;
+                    if (NS(s, iz, j, ir) == 0 && NS(s, k, ix, ir) == 0) {
+                        const double u = dnr, v = ri * dnx, w = risti * dnz;
+                        const double em = TT(s, iz, j, ir) - TT(s, iz, ix, i);
+                        const double en = TT(s, k, ix, ir) - TT(s, iz, ix, i);
+                        const double rd1 = sq(v) * sq(w), rd2 = sq(u) * sq(w), rd3 = sq(u) * sq(v);
+                        a = rd1 + rd2 + rd3;
+                        b = -2.0 * (em * rd2 + en * rd3);
+                        c = sq(em) * rd2 + sq(en) * rd3 - sq(slown) * sq(u) * rd1;
+                        tref = TT(s, iz, ix, i);
+                    } else if (NS(s, iz, j, ir) == 0) {
+                        const double u = dnr, v = ri * dnx;
+                        const double em = TT(s, iz, j, ir) - TT(s, iz, ix, i);
+                        a = sq(u) + sq(v);
+                        b = -2.0 * sq(u) * em;
+                        c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                        tref = TT(s, iz, ix, i);
+                    } else if (NS(s, k, ix, ir) == 0) {
+                        const double u = dnr, v = risti * dnz;
+                        const double em = TT(s, k, ix, ir) - TT(s, iz, ix, i);
+                        a = sq(u) + sq(v);
+                        b = -2.0 * sq(u) * em;
+                        c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                        tref = TT(s, iz, ix, i);
+                    } else {
+                        a = 1.0; b = 0.0;
+                        c = -sq(slown) * sq(dnr);
+                        tref = TT(s, iz, ix, i);
+                    }
+                } else if (NS(s, iz, j, ir) == 0) {
+                    swsol = 1;
+                    if (NS(s, k, ix, ir) == 0) {
+                        const double u = ri * dnx, v = risti * dnz;
+                        const double em = TT(s, k, ix, ir) - TT(s, iz, j, ir);
+                        a = sq(u) + sq(v);
+                        b = -2.0 * sq(u) * em;
+                        c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                        tref = TT(s, iz, j, ir);
+                    } else {
+                        a = 1.0; b = 0.0;
+                        c = -sq(slown) * sq(ri) * sq(dnx);
+                        tref = TT(s, iz, j, ir);
+                    }
+                } else if (NS(s, k, ix, ir) == 0) {
+                    swsol = 1;
+                    a = 1.0; b = 0.0;
+                    c = -sq(slown * risti * dnz);
+                    tref = TT(s, k, ix, ir);
+                }
+                if (swsol) {
+                    double rd1 = sq(b) - 4.0 * a * c;
+                    if (rd1 < 0.0) rd1 = 0.0;
+                    const double tdsh = (-b + sqrt(rd1)) / (2.0 * a);
+                    const double trav = tref + tdsh;
+                    if (tsw1) travm = fmin(trav, travm);
+                    else { travm = trav; tsw1 = 1; }
+                }
+            }
+    if (TT(s, iz, ix, ir) == 0.0 || TT(s, iz, ix, ir) > travm) TT(s, iz, ix, ir) = travm;
+}
+
+/* Upwind switch of one axis direction for fouds2_all (F:645-707): 0 when the
+ * second-order one-sided difference applies, -1 otherwise. */
+static int sw2(const fmm_state *s, int nb_alive, int nb2_in, int nb2_alive, double tnb, double tnb2)
+{
+    int sw = -1;
+    if (nb2_in && nb2_alive) sw = 0;
+    if (nb_alive && sw == 0) {
+        sw = -1;
+        if (tnb > tnb2) sw = 0;
+    } else {
+        sw = -1;
+    }
+    (void)s;
+    return sw;
+}
+
+/* fouds2_all: mixed-order update over the eight octants (F:635-1004). */
+static void fouds2(fmm_state *s, int iz, int ix, int ir)
+{
+    const orc_grid *g = s->g;
+    const double dnr = g->dnr, dnx = g->dnx, dnz = g->dnz;
+    double ri, risti;
+    centre_geom(s, ix, ir, &ri, &risti);
+    const double slown = 1.0 / s->veln[VELN(g, iz, ix, ir)];
+    int tsw1 = 0;
+    double travm = 0.0;
+    for (int i = ir - 1; i <= ir + 1; i += 2) {
+        const int i2 = (i == ir - 1) ? i - 1 : i + 1;
+        const int i2in = (i == ir - 1) ? (i2 >= 1) : (i2 <= s->nnr);
+        const int swi = sw2(s, NS(s, iz, ix, i) == 0, i2in, i2in && NS(s, iz, ix, i2) == 0,
+                            TT(s, iz, ix, i), i2in ? TT(s, iz, ix, i2) : 0.0);
+        for (int j = ix - 1; j <= ix + 1; j += 2) {
+            const int j2 = (j == ix - 1) ? j - 1 : j + 1;
+            const int j2in = (j == ix - 1) ? (j2 >= 1) : (j2 <= s->nnx);
+            const int swj = sw2(s, NS(s, iz, j, ir) == 0, j2in, j2in && NS(s, iz, j2, ir) == 0,
+                                TT(s, iz, j, ir), j2in ? TT(s, iz, j2, ir) : 0.0);
+            for (int k = iz - 1; k <= iz + 1; k += 2) {
+                const int k2 = (k == iz - 1) ? k - 1 : k + 1;
+                const int k2in = (k == iz - 1) ? (k2 >= 1) : (k2 <= s->nnz);
+                const int swk = sw2(s, NS(s, k, ix, ir) == 0, k2in, k2in && NS(s, k2, ix, ir) == 0,
+                                    TT(s, k, ix, ir), k2in ? TT(s, k2, ix, ir) : 0.0);
+                if (i < 1 || i > s->nnr || j < 1 || j > s->nnx || k < 1 || k > s->nnz) continue;
+                int swsol = 0;
+                double a = 0, b = 0, c = 0, u, v, w, em, en, tref = 0, tdiv = 1.0;
+                const int ai = NS(s, iz, ix, i) == 0, aj = NS(s, iz, j, ir) == 0, ak = NS(s, k, ix, ir) == 0;
+                /* neighbour values; second neighbours are only read on the
+                 * branches whose switch proved them in range */
+#define TIv TT(s, iz, ix, i)
+#define TI2 TT(s, iz, ix, i2)
+#define TJv TT(s, iz, j, ir)
+#define TJ2 TT(s, iz, j2, ir)
+#define TKv TT(s, k, ix, ir)
+#define TK2 TT(s, k2, ix, ir)
+                if (swi == 0) {
+                    swsol = 1;
+                    if (swj == 0) {
+                        if (swk == 0) {
+                            u = 2.0 * dnr; v = 2.0 * ri * dnx; w = 2.0 * risti * dnz;
+                            em = 4.0 * TIv - TI2 - 4.0 * TJv; em = em + TJ2;
+                            en = 4.0 * TIv - TI2 - 4.0 * TKv; en = en + TK2;
+                            a = sq(v) * sq(w) + sq(u) * sq(w) + sq(u) * sq(v);
+                            b = 2.0 * sq(u) * (em * sq(w) + en * sq(v));
+                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(v) * sq(w) * sq(slown));
+                            tref = 4.0 * TIv - TI2; tdiv = 3.0;
+                        } else if (ak) {
+                            u = risti * dnz; v = 2.0 * ri * dnx; w = 2.0 * dnr;
+                            em = 3.0 * TKv - 4.0 * TJv + TJ2;
+                            en = 3.0 * TKv - 4.0 * TIv + TI2;
+                            a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
+                            b = 6.0 * sq(u) * (em * sq(w) + en * sq(v));
+                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
+                            tref = TKv; tdiv = 1.0;
+                        } else {
+                            u = 2.0 * dnr; v = 2.0 * ri * dnx;
+                            em = 4.0 * TIv - TI2 - 4.0 * TJv; em = em + TJ2;
+                            a = sq(v) + sq(u);
+                            b = 2.0 * em * sq(u);
+                            c = sq(u) * (sq(em) - sq(slown) * sq(v));
+                            tref = 4.0 * TIv - TI2; tdiv = 3.0;
+                        }
+                    } else if (aj) {
+                        if (swk == 0) {
+                            u = ri * dnx; v = 2.0 * dnr; w = 2.0 * risti * dnz;
+                            em = 3.0 * TJv - 4.0 * TIv + TI2;
+                            en = 3.0 * TJv - 4.0 * TKv + TK2;
+                            a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
+                            b = 6.0 * sq(u) * (em * sq(w) + en * sq(v));
+                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
+                            tref = TJv; tdiv = 1.0;
+                        } else if (ak) {
+                            u = ri * dnx; v = 2.0 * dnr; w = risti * dnz;
+                            em = 3.0 * TJv - 4.0 * TIv + TI2;
+                            en = TJv - TKv;
+                            a = sq(w) * sq(v) + 9.0 * sq(u) * sq(w) + sq(u) * sq(v);
+                            b = sq(u) * (6.0 * em * sq(w) + 2.0 * en * sq(v));
+                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
+                            tref = TJv; tdiv = 1.0;
+                        } else {
+                            u = ri * dnx; v = 2.0 * dnr;
+                            em = 3.0 * TJv - 4.0 * TIv + TI2;
+                            a = sq(v) + 9.0 * sq(u);
+                            b = 6.0 * em * sq(u);
+                            c = sq(u) * (sq(em) - sq(slown) * sq(v));
+                            tref = TJv; tdiv = 1.0;
+                        }
+                    } else {
+                        if (swk == 0) {
+                            u = 2.0 * dnr; v = 2.0 * risti * dnz;
+                            em = 4.0 * TIv - TI2 - 4.0 * TKv; em = em + TK2;
+                            a = sq(u) + sq(v);
+                            b = 2.0 * em * sq(u);
+                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                            tref = 4.0 * TIv - TI2; tdiv = 3.0;
+                        } else if (ak) {
+                            u = risti * dnz; v = 2.0 * dnr;
+                            em = 3.0 * TKv - 4.0 * TIv + TI2;
+                            a = sq(v) + 9.0 * sq(u);
+                            b = 6.0 * em * sq(u);
+                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                            tref = TKv; tdiv = 1.0;
+                        } else {
+                            u = 2.0 * dnr;
+                            a = 1.0; b = 0.0;
+                            c = -sq(u) * sq(slown);
+                            tref = 4.0 * TIv - TI2; tdiv = 3.0;
+                        }
+                    }
+                } else if (ai) {
+                    swsol = 1;
+                    if (swj == 0) {
+                        if (swk == 0) {
+                            u = dnr; v = 2.0 * ri * dnx; w = 2.0 * risti * dnz;
+                            em = 3.0 * TIv - 4.0 * TJv + TJ2;
+                            en = 3.0 * TIv - 4.0 * TKv + TK2;
+                            a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
+                            b = 6.0 * sq(u) * (em * sq(w) + en * sq(v));
+                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
+                            tref = TIv; tdiv = 1.0;
+                        } else if (ak) {
+                            u = dnr; v = 2.0 * ri * dnx; w = risti * dnz;
+                            em = 3.0 * TIv - 4.0 * TJv + TJ2;
+                            en = TIv - TKv;
+                            a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + sq(u) * sq(v);
+                            b = sq(u) * (6.0 * em * sq(w) + 2.0 * en * sq(v));
+                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(v) * sq(w) * sq(slown));
+                            tref = TIv; tdiv = 1.0;
+                        } else {
+                            u = dnr; v = 2.0 * ri * dnx;
+                            em = 3.0 * TIv - 4.0 * TJv + TJ2;
+                            a = sq(v) + 9.0 * sq(u);
+                            b = 6.0 * em * sq(u);
+                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                            tref = TIv; tdiv = 1.0;
+                        }
+                    } else if (aj) {
+                        if (swk == 0) {
+                            u = dnr; v = ri * dnx; w = 2.0 * risti * dnz;
+                            em = TIv - TJv;
+                            en = 3.0 * TIv - 4.0 * TKv + TK2;
+                            a = sq(v) * sq(w) + sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
+                            b = sq(u) * (2.0 * em * sq(w) + 6.0 * en * sq(v));
+                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(v) * sq(w) * sq(slown));
+                            tref = TIv; tdiv = 1.0;
+                        } else if (ak) {
+                            u = dnr; v = ri * dnx; w = risti * dnz;
+                            em = TJv - TIv;
+                            en = TKv - TIv;
+                            a = sq(v) * sq(w) + sq(u) * sq(w) + sq(u) * sq(v);
+                            b = -2.0 * sq(u) * (em * sq(w) + en * sq(v));
+                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
+                            tref = TIv; tdiv = 1.0;
+                        } else {
+                            u = dnr; v = ri * dnx;
+                            em = TJv - TIv;
+                            a = sq(u) + sq(v);
+                            b = -2.0 * sq(u) * em;
+                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                            tref = TIv; tdiv = 1.0;
+                        }
+                    } else {
+                        if (swk == 0) {
+                            u = dnr; v = 2.0 * risti * dnz;
+                            em = 3.0 * TIv - 4.0 * TKv + TK2;
+                            a = sq(v) + 9.0 * sq(u);
+                            b = 6.0 * em * sq(u);
+                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                            tref = TIv; tdiv = 1.0;
+                        } else if (ak) {
+                            u = dnr; v = risti * dnz;
+                            em = TKv - TIv;
+                            a = sq(u) + sq(v);
+                            b = -2.0 * sq(u) * em;
+                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                            tref = TIv; tdiv = 1.0;
+                        } else {
+                            a = 1.0; b = 0.0;
+                            c = -sq(slown) * sq(dnr);
+                            tref = TIv; tdiv = 1.0;
+                        }
+                    }
+                } else {
+                    if (swj == 0) {
+                        swsol = 1;
+                        if (swk == 0) {
+                            u = 2.0 * ri * dnx; v = 2.0 * risti * dnz;
+                            em = 4.0 * TJv - TJ2 - 4.0 * TKv; em = em + TK2;
+                            a = sq(v) + sq(u);
+                            b = 2.0 * em * sq(u);
+                            c = sq(u) * (sq(em) - sq(slown) * sq(v));
+                            tref = 4.0 * TJv - TJ2; tdiv = 3.0;
+                        } else if (ak) {
+                            u = risti * dnz; v = 2.0 * ri * dnx;
+                            em = 3.0 * TKv - 4.0 * TJv + TJ2;
+                            a = sq(v) + 9.0 * sq(u);
+                            b = 6.0 * em * sq(u);
+                            c = sq(u) * (sq(em) - sq(slown) * sq(v));
+                            tref = TKv; tdiv = 1.0;
+                        } else {
+                            u = 2.0 * ri * dnx;
+                            a = 1.0; b = 0.0;
+                            c = -sq(u) * sq(slown);
+                            tref = 4.0 * TJv - TJ2; tdiv = 3.0;
+                        }
+                    } else if (aj) {
+                        swsol = 1;
+                        if (swk == 0) {
+                            u = ri * dnx; v = 2.0 * risti * dnz;
+                            em = 3.0 * TJv - 4.0 * TKv + TK2;
+                            a = sq(v) + 9.0 * sq(u);
+                            b = 6.0 * em * sq(u);
+                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                            tref = TJv; tdiv = 1.0;
+                        } else if (ak) {
+                            u = ri * dnx; v = risti * dnz;
+                            em = TKv - TJv;
+                            a = sq(u) + sq(v);
+                            b = -2.0 * sq(u) * em;
+                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                            tref = TJv; tdiv = 1.0;
+                        } else {
+                            a = 1.0; b = 0.0;
+                            c = -sq(slown) * sq(ri) * sq(dnx);
+                            tref = TJv; tdiv = 1.0;
+                        }
+                    } else {
+                        if (swk == 0) {
+                            swsol = 1;
+                            u = 2.0 * risti * dnz;
+                            a = 1.0; b = 0.0;
+                            c = -sq(u) * sq(slown);
+                            tref = 4.0 * TKv - TK2; tdiv = 3.0;
+                        } else if (ak) {
+                            swsol = 1;
+                            a = 1.0; b = 0.0;
+                            c = -sq(slown) * sq(risti) * sq(dnz);
+                            tref = TKv; tdiv = 1.0;
+                        }
+                    }
+                }
+#undef TIv
+#undef TI2
+#undef TJv
+#undef TJ2
+#undef TKv
+#undef TK2
+                if (swsol) {
+                    double rd1 = sq(b) - 4.0 * a * c;
+                    if (rd1 < 0.0) rd1 = 0.0;
+                    const double tdsh = (-b + sqrt(rd1)) / (2.0 * a);
+                    const double trav = (tref + tdsh) / tdiv;
+                    if (tsw1) travm = fmin(trav, travm);
+                    else { travm = trav; tsw1 = 1; }
+                }
+            }
+        }
+    }
+    /* F:1001: travm is undefined in the reference when no octant solved;
+     * that cannot happen for a neighbour of a popped node. */
+    if (TT(s, iz, ix, ir) == 0.0 || TT(s, iz, ix, ir) > travm) TT(s, iz, ix, ir) = travm;
+}
+
+/* Heap operations (F:1006-1098). Ties keep the reference's order. */
+static void addtree(fmm_state *s, int iz, int ix, int ir)
+{
+    s->ntr++;
+    NS(s, iz, ix, ir) = s->ntr;
+    s->hr[s->ntr] = ir; s->hx[s->ntr] = ix; s->hz[s->ntr] = iz;
+    int tpc = s->ntr, tpp = tpc / 2;
+    while (tpp > 0) {
+        if (TT(s, iz, ix, ir) < TT(s, s->hz[tpp], s->hx[tpp], s->hr[tpp])) {
+            NS(s, iz, ix, ir) = tpp;
+            NS(s, s->hz[tpp], s->hx[tpp], s->hr[tpp]) = tpc;
+            int t;
+            t = s->hr[tpc]; s->hr[tpc] = s->hr[tpp]; s->hr[tpp] = t;
+            t = s->hx[tpc]; s->hx[tpc] = s->hx[tpp]; s->hx[tpp] = t;
+            t = s->hz[tpc]; s->hz[tpc] = s->hz[tpp]; s->hz[tpp] = t;
+            tpc = tpp; tpp = tpc / 2;
+        } else {
+            tpp = 0;
+        }
+    }
+}
+
+static double hval(const fmm_state *s, int p) { return TT(s, s->hz[p], s->hx[p], s->hr[p]); }
+
+static void hswap_status(fmm_state *s, int tpp, int tpc)
+{
+    NS(s, s->hz[tpp], s->hx[tpp], s->hr[tpp]) = tpc;
+    NS(s, s->hz[tpc], s->hx[tpc], s->hr[tpc]) = tpp;
+    int t;
+    t = s->hr[tpc]; s->hr[tpc] = s->hr[tpp]; s->hr[tpp] = t;
+    t = s->hx[tpc]; s->hx[tpc] = s->hx[tpp]; s->hx[tpp] = t;
+    t = s->hz[tpc]; s->hz[tpc] = s->hz[tpp]; s->hz[tpp] = t;
+}
+
+static void downtree(fmm_state *s)
+{
+    if (s->ntr == 1) { s->ntr = 0; return; }
+    const int n = s->ntr;
+    NS(s, s->hz[n], s->hx[n], s->hr[n]) = 1;
+    s->hr[1] = s->hr[n]; s->hx[1] = s->hx[n]; s->hz[1] = s->hz[n];
+    s->ntr--;
+    int tpp = 1, tpc = 2;
+    while (tpc < s->ntr) {
+        if (hval(s, tpc) > hval(s, tpc + 1)) tpc++;
+        if (hval(s, tpc) < hval(s, tpp)) {
+            hswap_status(s, tpp, tpc);
+            tpp = tpc; tpc = 2 * tpp;
+        } else {
+            tpc = s->ntr + 1;
+        }
+    }
+    if (tpc == s->ntr) {
+        if (hval(s, tpc) < hval(s, tpp)) hswap_status(s, tpp, tpc);
+    }
+}
+
+static void updtree(fmm_state *s, int iz, int ix, int ir)
+{
+    int tpc = NS(s, iz, ix, ir), tpp = tpc / 2;
+    while (tpp > 0) {
+        if (TT(s, iz, ix, ir) < hval(s, tpp)) {
+            NS(s, iz, ix, ir) = tpp;
+            NS(s, s->hz[tpp], s->hx[tpp], s->hr[tpp]) = tpc;
+            int t;
+            t = s->hr[tpc]; s->hr[tpc] = s->hr[tpp]; s->hr[tpp] = t;
+            t = s->hx[tpc]; s->hx[tpc] = s->hx[tpp]; s->hx[tpp] = t;
+            t = s->hz[tpc]; s->hz[tpc] = s->hz[tpp]; s->hz[tpp] = t;
+            tpc = tpp; tpp = tpc / 2;
+        } else {
+            tpp = 0;
+        }
+    }
+}
+
+static void visit(fmm_state *s, int fom, int iz, int ix, int ir)
+{
+    const int st = NS(s, iz, ix, ir);
+    if (st == -1) {
+        if (fom == 0) fouds1(s, iz, ix, ir); else fouds2(s, iz, ix, ir);
+        addtree(s, iz, ix, ir);
+    } else if (st > 0) {
+        if (fom == 0) fouds1(s, iz, ix, ir); else fouds2(s, iz, ix, ir);
+        updtree(s, iz, ix, ir);
+    }
+}
+
+int orc_fmm(const orc_grid *g, const double *veln, int fom, const double *bottom,
+            double *ttn, long long *npops)
+{
+    fmm_state s;
+    memset(&s, 0, sizeof s);
+    s.g = g; s.veln = veln;
+    s.nnr = g->nnr; s.nnx = g->nnx; s.nnz = g->nnz;
+    s.NZ2 = g->nnz + 2; s.NX2 = g->nnx + 2;
+    const size_t npad = (size_t)s.NZ2 * (size_t)s.NX2 * (size_t)(g->nnr + 2);
+    const size_t nint = (size_t)g->nnz * (size_t)g->nnx * (size_t)g->nnr;
+    s.ttn = (double *)calloc(npad, sizeof(double));
+    s.nsts = (int *)malloc(npad * sizeof(int));
+    s.hr = (int *)malloc((nint + 2) * sizeof(int));
+    s.hx = (int *)malloc((nint + 2) * sizeof(int));
+    s.hz = (int *)malloc((nint + 2) * sizeof(int));
+    if (!s.ttn || !s.nsts || !s.hr || !s.hx || !s.hz) {
+        free(s.ttn); free(s.nsts); free(s.hr); free(s.hx); free(s.hz);
+        return -3;
+    }
+    for (size_t q = 0; q < npad; ++q) s.nsts[q] = -1;   /* F:6373-6375 */
+
+    /* start_fmm (F:6908-6960): load the bottom frame, freeze positive
+     * values, seed the heap with the single global minimum. */
+    const int rn = g->nnr;
+    int sw = 0, itmin = 0, jtmin = 0;
+    double ttmin = -100.0;
+    for (int i = 1; i <= g->nnx; ++i)
+        for (int j = 1; j <= g->nnz; ++j) {
+            const double rd1 = bottom[(size_t)(j - 1) + (size_t)g->nnz * (size_t)(i - 1)];
+            TT(&s, j, i, rn) = rd1;
+            if (rd1 > 0.0) {
+                if (sw == 0) { ttmin = rd1; itmin = i; jtmin = j; sw = 1; }
+                else if (rd1 < ttmin) { ttmin = rd1; itmin = i; jtmin = j; }
+                NS(&s, j, i, rn) = 0;
+            } else {
+                TT(&s, j, i, rn) = 0.0;
+            }
+        }
+    long long pops = 0;
+    if (sw) {
+        addtree(&s, jtmin, itmin, rn);
+        /* local_fmm (F:88-154) */
+        while (s.ntr > 0) {
+            const int ir = s.hr[1], ix = s.hx[1], iz = s.hz[1];
+            NS(&s, iz, ix, ir) = 0;
+            downtree(&s);
+            ++pops;
+            for (int i = ir - 1; i <= ir + 1; i += 2)
+                if (i >= 1 && i <= s.nnr) visit(&s, fom, iz, ix, i);
+            for (int i = ix - 1; i <= ix + 1; i += 2)
+                if (i >= 1 && i <= s.nnx) visit(&s, fom, iz, i, ir);
+            for (int i = iz - 1; i <= iz + 1; i += 2)
+                if (i >= 1 && i <= s.nnz) visit(&s, fom, i, ix, ir);
+        }
+    }
+    for (int ir = 1; ir <= g->nnr; ++ir)
+        for (int ix = 1; ix <= g->nnx; ++ix)
+            for (int iz = 1; iz <= g->nnz; ++iz)
+                ttn[(size_t)(iz - 1) + (size_t)g->nnz * ((size_t)(ix - 1) + (size_t)g->nnx * (size_t)(ir - 1))] = TT(&s, iz, ix, ir);
+    if (npops) *npops = pops;
+    free(s.ttn); free(s.nsts); free(s.hr); free(s.hx); free(s.hz);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Receiver traveltimes (F:7066-7106)                                        */
+/* ------------------------------------------------------------------------ */
+#define TD(g, iz, ix, ir) ttn[(size_t)((iz) - 1) + (size_t)(g)->nnz * ((size_t)((ix) - 1) + (size_t)(g)->nnx * (size_t)((ir) - 1))]
+
+int orc_srtimes(const orc_grid *g, const double *ttn, int nrc, const double *rcr,
+                const double *rcx, const double *rcz, float *trr)
+{
+    for (int i = 0; i < nrc; ++i) {
+        int irr = (int)floor((g->rgor - rcr[i]) / g->dnr) + 1;
+        int irx = (int)floor((rcx[i] - g->rgox) / g->dnx) + 1;
+        int irz = (int)floor((rcz[i] - g->rgoz) / g->dnz) + 1;
+        if (irx == g->nnx) irx = irx - 1;   /* F:7069-7070 on the last subdomain */
+        if (irz == g->nnz) irz = irz - 1;
+        if (irr < 1 || irr >= g->nnr || irx < 1 || irx >= g->nnx || irz < 1 || irz >= g->nnz)
+            return -(1 + i);
+        const double drx = (rcx[i] - g->rgox) - (double)(irx - 1) * g->dnx;
+        const double drz = (rcz[i] - g->rgoz) - (double)(irz - 1) * g->dnz;
+        const double drr = (g->rgor - rcr[i]) - (double)(irr - 1) * g->dnr;
+        float acc = 0.0f;
+        for (int j = 1; j <= 2; ++j)
+            for (int k = 1; k <= 2; ++k)
+                for (int l = 1; l <= 2; ++l) {
+                    double produ = (1.0 - fabs(((double)(l - 1) * g->dnz - drz) / g->dnz)) *
+                                   (1.0 - fabs(((double)(k - 1) * g->dnx - drx) / g->dnx));
+                    produ = produ * (1.0 - fabs(((double)(j - 1) * g->dnr - drr) / g->dnr));
+                    acc = (float)((double)acc + TD(g, irz - 1 + l, irx - 1 + k, irr - 1 + j) * produ);
+                }
+        trr[i] = acc;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Rays and Frechet derivatives (F:7250-7777)                                */
+/* ------------------------------------------------------------------------ */
+
+/* trilinear velocity at a point whose propagation cell is (ipz,ipx,ipr) and
+ * offsets drr,drx,drz; loop nesting order of F:7632-7641 (r, x, z) or
+ * F:7689-7698 (same order). */
+static double trilin_vel(const orc_grid *g, const double *veln, int ipz, int ipx, int ipr,
+                         double drr, double drx, double drz)
+{
+    double vel = 0.0;
+    for (int k = 1; k <= 2; ++k)
+        for (int l = 1; l <= 2; ++l)
+            for (int m = 1; m <= 2; ++m) {
+                double produ = (1.0 - fabs(((double)(m - 1) * g->dnz - drz) / g->dnz));
+                produ = produ * (1.0 - fabs(((double)(l - 1) * g->dnx - drx) / g->dnx));
+                produ = produ * (1.0 - fabs(((double)(k - 1) * g->dnr - drr) / g->dnr));
+                if (ipz - 1 + m <= g->nnz + 1 && ipx - 1 + l <= g->nnx + 1 && ipr - 1 + k <= g->nnr + 1)
+                    vel = vel + veln[VELN(g, ipz - 1 + m, ipx - 1 + l, ipr - 1 + k)] * produ;
+            }
+    return vel;
+}
+
+#define FDM(ivz, ivx, ivr) ((size_t)(ivr) + (size_t)(g->nvr + 2) * ((size_t)(ivx) + (size_t)(g->nvx + 2) * (size_t)(ivz)))
+
+int orc_rays(const orc_grid *g, const double *ttn, const double *veln, int nrc,
+             const double *rcr, const double *rcx, const double *rcz,
+             float *fdm_all, double *endpoints, int *nsteps)
+{
+    const int maxrp = 100000;             /* F:7262 */
+    const double dpl = g->dnr;            /* F:7290 */
+    const size_t nmp = (size_t)(g->nvr + 2) * (size_t)(g->nvx + 2) * (size_t)(g->nvz + 2);
+    int rc = 0;
+    for (int iray = 0; iray < nrc; ++iray) {
+        float *fdm = fdm_all ? fdm_all + nmp * (size_t)iray : NULL;
+        if (fdm) memset(fdm, 0, nmp * sizeof(float));
+        double r0 = rcr[iray], x0 = rcx[iray], z0 = rcz[iray];
+        int ipr = (int)floor((g->rgor - r0) / g->dnr) + 1;
+        int ipx = (int)floor((x0 - g->rgox) / g->dnx) + 1;
+        int ipz = (int)floor((z0 - g->rgoz) / g->dnz) + 1;
+        /* F:7320-7333: first-round clamp on the last subdomain of each axis */
+        if (ipr == g->nnr) ipr--;
+        if (ipx == g->nnx) ipx--;
+        if (ipz == g->nnz) ipz--;
+        if (endpoints) { endpoints[3 * iray] = r0; endpoints[3 * iray + 1] = x0; endpoints[3 * iray + 2] = z0; }
+        if (nsteps) nsteps[iray] = 0;
+        if (ipr < 1 || ipr >= g->nnr || ipx < 1 || ipx >= g->nnx || ipz < 1 || ipz >= g->nnz)
+            continue;
+        double rgr = r0, rgx = x0, rgz = z0;
+        int steps = 0;
+        for (int jstep = 1; jstep <= maxrp; ++jstep) {
+            ++steps;
+            /* F:7348-7378: cell-averaged gradient */
+            double dtr = 0.0;
+            int temp = 0;
+            if (TD(g, ipz, ipx, ipr + 1) < TD(g, ipz, ipx, ipr)) { dtr = dtr + TD(g, ipz, ipx, ipr + 1) - TD(g, ipz, ipx, ipr); temp++; }
+            if (TD(g, ipz + 1, ipx, ipr + 1) < TD(g, ipz + 1, ipx, ipr)) { dtr = dtr + TD(g, ipz + 1, ipx, ipr + 1) - TD(g, ipz + 1, ipx, ipr); temp++; }
+            if (TD(g, ipz + 1, ipx + 1, ipr + 1) < TD(g, ipz + 1, ipx + 1, ipr)) { dtr = dtr + TD(g, ipz + 1, ipx + 1, ipr + 1) - TD(g, ipz + 1, ipx + 1, ipr); temp++; }
+            if (TD(g, ipz, ipx + 1, ipr + 1) < TD(g, ipz, ipx + 1, ipr)) { dtr = dtr + TD(g, ipz, ipx + 1, ipr + 1) - TD(g, ipz, ipx + 1, ipr); temp++; }
+            if (temp != 0) dtr = dtr / ((double)temp * g->dnr);
+            const double rcell = g->earth + g->rgor - (double)(ipr - 1) * g->dnr;
+            double dtx = TD(g, ipz, ipx + 1, ipr) - TD(g, ipz, ipx, ipr);
+            dtx = dtx + TD(g, ipz + 1, ipx + 1, ipr) - TD(g, ipz + 1, ipx, ipr);
+            dtx = dtx + TD(g, ipz + 1, ipx + 1, ipr + 1) - TD(g, ipz + 1, ipx, ipr + 1);
+            dtx = dtx + TD(g, ipz, ipx + 1, ipr + 1) - TD(g, ipz, ipx, ipr + 1);
+            dtx = dtx / (4.0 * rcell * g->dnx);
+            const double sx = sin(rgx);
+            double dtz = TD(g, ipz + 1, ipx, ipr) - TD(g, ipz, ipx, ipr);
+            dtz = dtz + TD(g, ipz + 1, ipx + 1, ipr + 1) - TD(g, ipz, ipx + 1, ipr + 1);
+            dtz = dtz + TD(g, ipz + 1, ipx + 1, ipr) - TD(g, ipz, ipx + 1, ipr);
+            dtz = dtz + TD(g, ipz + 1, ipx, ipr + 1) - TD(g, ipz, ipx, ipr + 1);
+            dtz = dtz / (4.0 * rcell * sx * g->dnz);
+            const double crad = g->earth + rgr;
+            double rd1 = sqrt(dtr * dtr + dtx * dtx + dtz * dtz);
+            double nr = rgr + dpl * dtr / rd1;
+            double nx = rgx - dpl * dtx / (crad * rd1);
+            double nz = rgz - dpl * dtz / (crad * sx * rd1);
+            const int ipro = ipr, ipxo = ipx, ipzo = ipz;
+            ipr = (int)floor((g->rgor - nr) / g->dnr) + 1;
+            ipx = (int)floor((nx - g->rgox) / g->dnx) + 1;
+            ipz = (int)floor((nz - g->rgoz) / g->dnz) + 1;
+            const int swr = (ipr < 1 || ipr >= g->nnr);
+            const int swx = (ipx < 1 || ipx >= g->nnx);
+            const int swz = (ipz < 1 || ipz >= g->nnz);
+            int stop = 0;
+            if (swr || swx || swz) {
+                /* F:7474-7541: clip to the first outer face crossed */
+                int sw = 0;
+                double atio = 0.0;
+                if (swr) {
+                    double ri;
+                    if (ipr < 1) { ri = g->rgor; ipr = 1; }
+                    else { ri = g->rgor - (double)(g->nnr - 1) * g->dnr; ipr = g->nnr - 1; }
+                    atio = (ri - rgr) / (nr - rgr);
+                    sw = 1;
+                }
+                if (swx) {
+                    double xi;
+                    if (ipx < 1) { xi = g->rgox; ipx = 1; }
+                    else { xi = g->rgox + (double)(g->nnx - 1) * g->dnx; ipx = g->nnx - 1; }
+                    const double r1 = (xi - rgx) / (nx - rgx);
+                    if (sw == 1) { if (r1 < atio) { atio = r1; sw = 2; } }
+                    else { atio = r1; sw = 2; }
+                }
+                if (swz) {
+                    double zi;
+                    if (ipz < 1) { zi = g->rgoz; ipz = 1; }
+                    else { zi = g->rgoz + (double)(g->nnz - 1) * g->dnz; ipz = g->nnz - 1; }
+                    const double r1 = (zi - rgz) / (nz - rgz);
+                    if (sw != 0) { if (r1 < atio) { atio = r1; sw = 3; } }
+                    else { atio = r1; sw = 3; }
+                }
+                if (sw == 1) { ipx = ipxo; ipz = ipzo; }
+                else if (sw == 2) { ipr = ipro; ipz = ipzo; }
+                else if (sw == 3) { ipr = ipro; ipx = ipxo; }
+                nz = rgz + atio * (nz - rgz);
+                nx = rgx + atio * (nx - rgx);
+                nr = rgr + atio * (nr - rgr);
+                stop = 1;
+            }
+            if (fdm) {
+                /* F:7543-7733: split at velocity-cell crossings, trapezoid
+                 * integration of -B/v^2 ds into the single-precision fdm */
+                const int ivr = (int)floor((g->gor - nr) / g->dvr) + 1;
+                const int ivx = (int)floor((nx - g->gox) / g->dvx) + 1;
+                const int ivz = (int)floor((nz - g->goz) / g->dvz) + 1;
+                const int ivro = (int)floor((g->gor - rgr) / g->dvr) + 1;
+                const int ivxo = (int)floor((rgx - g->gox) / g->dvx) + 1;
+                const int ivzo = (int)floor((rgz - g->goz) / g->dvz) + 1;
+                double vrat[4];
+                int chp[4];
+                int nhp = 0;
+                if (ivr != ivro) {
+                    const double ri = (ivr > ivro) ? g->gor - (double)(ivr - 1) * g->dvr : g->gor - (double)ivr * g->dvr;
+                    vrat[nhp] = (ri - rgr) / (nr - rgr);
+                    chp[nhp] = 1;
+                    nhp++;
+                }
+                if (ivx != ivxo) {
+                    const double xi = (ivx > ivxo) ? g->gox + (double)(ivx - 1) * g->dvx : g->gox + (double)ivx * g->dvx;
+                    const double r1 = (xi - rgx) / (nx - rgx);
+                    nhp++;
+                    if (nhp == 1) { vrat[0] = r1; chp[0] = 2; }
+                    else if (r1 >= vrat[nhp - 2]) { vrat[nhp - 1] = r1; chp[nhp - 1] = 2; }
+                    else { vrat[nhp - 1] = vrat[nhp - 2]; chp[nhp - 1] = chp[nhp - 2]; vrat[nhp - 2] = r1; chp[nhp - 2] = 2; }
+                }
+                if (ivz != ivzo) {
+                    const double zi = (ivz > ivzo) ? g->goz + (double)(ivz - 1) * g->dvz : g->goz + (double)ivz * g->dvz;
+                    const double r1 = (zi - rgz) / (nz - rgz);
+                    nhp++;
+                    /* 1-based positions as in F:7590-7624 */
+                    const int n = nhp;
+                    if (n == 1) { vrat[0] = r1; chp[0] = 3; }
+                    else if (n == 2) {
+                        if (r1 >= vrat[0]) { vrat[1] = r1; chp[1] = 3; }
+                        else { vrat[1] = vrat[0]; chp[1] = chp[0]; vrat[0] = r1; chp[0] = 3; }
+                    } else {
+                        if (r1 >= vrat[1]) { vrat[2] = r1; chp[2] = 3; }
+                        else if (r1 >= vrat[0]) { vrat[2] = vrat[1]; chp[2] = chp[1]; vrat[1] = r1; chp[1] = 3; }
+                        else { vrat[2] = vrat[1]; chp[2] = chp[1]; vrat[1] = vrat[0]; chp[1] = chp[0]; vrat[0] = r1; chp[0] = 3; }
+                    }
+                }
+                vrat[nhp] = 1.0;
+                chp[nhp] = 0;
+                nhp++;
+                /* velocity and B-spline weights at the segment start */
+                double drr = (g->rgor - rgr) - (double)(ipro - 1) * g->dnr;
+                double drx = (rgx - g->rgox) - (double)(ipxo - 1) * g->dnx;
+                double drz = (rgz - g->rgoz) - (double)(ipzo - 1) * g->dnz;
+                double vel = trilin_vel(g, veln, ipzo, ipxo, ipro, drr, drx, drz);
+                double ui[4], vi[4], wi[4], uio[4], vio[4], wio[4];
+                drr = (g->gor - rgr) - (double)(ivro - 1) * g->dvr;
+                drx = (rgx - g->gox) - (double)(ivxo - 1) * g->dvx;
+                drz = (rgz - g->goz) - (double)(ivzo - 1) * g->dvz;
+                bspline4(drr / g->dvr, ui);
+                bspline4(drx / g->dvx, vi);
+                bspline4(drz / g->dvz, wi);
+                int ivrt = ivro, ivxt = ivxo, ivzt = ivzo;
+                for (int k = 0; k < nhp; ++k) {
+                    const double velo = vel;
+                    memcpy(uio, ui, sizeof ui); memcpy(vio, vi, sizeof vi); memcpy(wio, wi, sizeof wi);
+                    if (k > 0) {
+                        if (chp[k - 1] == 1) ivrt = ivr;
+                        else if (chp[k - 1] == 2) ivxt = ivx;
+                        else if (chp[k - 1] == 3) ivzt = ivz;
+                    }
+                    const double rigz = rgz + vrat[k] * (nz - rgz);
+                    const double rigx = rgx + vrat[k] * (nx - rgx);
+                    const double rigr = rgr + vrat[k] * (nr - rgr);
+                    const int iprt = (int)floor((g->rgor - rigr) / g->dnr) + 1;
+                    const int ipxt = (int)floor((rigx - g->rgox) / g->dnx) + 1;
+                    const int ipzt = (int)floor((rigz - g->rgoz) / g->dnz) + 1;
+                    drr = (g->rgor - rigr) - (double)(iprt - 1) * g->dnr;
+                    drx = (rigx - g->rgox) - (double)(ipxt - 1) * g->dnx;
+                    drz = (rigz - g->rgoz) - (double)(ipzt - 1) * g->dnz;
+                    vel = trilin_vel(g, veln, ipzt, ipxt, iprt, drr, drx, drz);
+                    drr = (g->gor - rigr) - (double)(ivrt - 1) * g->dvr;
+                    drx = (rigx - g->gox) - (double)(ivxt - 1) * g->dvx;
+                    drz = (rigz - g->goz) - (double)(ivzt - 1) * g->dvz;
+                    bspline4(drr / g->dvr, ui);
+                    bspline4(drx / g->dvx, vi);
+                    bspline4(drz / g->dvz, wi);
+                    const double dinc = (k == 0) ? vrat[k] * dpl : (vrat[k] - vrat[k - 1]) * dpl;
+                    if (ivzt - 1 < 0 || ivzt + 2 > g->nvz + 1 || ivxt - 1 < 0 || ivxt + 2 > g->nvx + 1 ||
+                        ivrt - 1 < 0 || ivrt + 2 > g->nvr + 1) {
+                        rc = -2;
+                        continue;
+                    }
+                    for (int n = 1; n <= 4; ++n)
+                        for (int m = 1; m <= 4; ++m)
+                            for (int l = 1; l <= 4; ++l) {
+                                double a1 = ui[n - 1] * vi[m - 1] * wi[l - 1] / (vel * vel);
+                                double a2 = uio[n - 1] * vio[m - 1] * wio[l - 1] / (velo * velo);
+                                a1 = -(a1 + a2) * dinc / 2.0;
+                                const size_t q = FDM(ivzt - 2 + l, ivxt - 2 + m, ivrt - 2 + n);
+                                fdm[q] = (float)(a1 + (double)fdm[q]);
+                            }
+                }
+            }
+            rgr = nr; rgx = nx; rgz = nz;
+            if (stop) break;
+        }
+        if (endpoints) { endpoints[3 * iray] = rgr; endpoints[3 * iray + 1] = rgx; endpoints[3 * iray + 2] = rgz; }
+        if (nsteps) nsteps[iray] = steps;
+    }
+    return rc;
+}
+
+int orc_sparsify(int nmp, const float *row, int cap, int *cols, float *vals)
+{
+    const float ftol = 1.0e-6f;   /* F:7263, REAL(KIND=i5) */
+    int n = 0;
+    for (int q = 0; q < nmp; ++q) {
+        if (fabsf(row[q]) >= ftol) {
+            if (n < cap) { cols[n] = q + 1; vals[n] = row[q]; }
+            n++;
+        }
+    }
+    return n;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Synthetic plane-wave boundary frames (test inputs; not in the reference)  */
+/* ------------------------------------------------------------------------ */
+void orc_planewave_params(const orc_grid *g, double delta_deg, double baz_deg, orc_planewave *pw)
+{
+    const double d2r = M_PI / 180.0;
+    const double rb = g->earth + (g->rgor - (double)(g->nnr - 1) * g->dnr);
+    /* synthetic distance law, seconds with delta in degrees */
+    pw->t0 = 150.0 + 10.0 * delta_deg - 0.025 * delta_deg * delta_deg;
+    pw->p = (10.0 - 0.05 * delta_deg) / (rb * d2r);
+    const double az = (baz_deg + 180.0) * d2r;
+    pw->cos_az = cos(az);
+    pw->sin_az = sin(az);
+}
+
+void orc_planewave_frame(const orc_grid *g, const orc_planewave *pw, double *frame)
+{
+    const double rb = g->earth + (g->rgor - (double)(g->nnr - 1) * g->dnr);
+    const double thc = g->rgox + (double)(g->nnx - 1) * g->dnx * 0.5;
+    const double phc = g->rgoz + (double)(g->nnz - 1) * g->dnz * 0.5;
+    const double rbs = rb * sin(thc);
+    for (int ix = 1; ix <= g->nnx; ++ix) {
+        const double th = g->rgox + (double)(ix - 1) * g->dnx;
+        const double dn = rb * (thc - th);
+        for (int iz = 1; iz <= g->nnz; ++iz) {
+            const double ph = g->rgoz + (double)(iz - 1) * g->dnz;
+            const double de = rbs * (ph - phc);
+            const double d = dn * pw->cos_az + de * pw->sin_az;
+            frame[(size_t)(iz - 1) + (size_t)g->nnz * (size_t)(ix - 1)] = pw->t0 + pw->p * d;
+        }
+    }
+}

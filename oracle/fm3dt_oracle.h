@@ -1,0 +1,113 @@
+/*
+ * fm3dt_oracle.h -- CPU oracle for the forward teleseismic traveltime path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the serial
+ * (1x1x1-subdomain) path of fm3dt_parallel.f90 of the Parallel Fast Marching
+ * Method.  Only tests/, the smoke() entry and bench.py's CPU-baseline leg may
+ * load it, and only as the checker.  The GPU library never links it.
+ *
+ * Parity status: UNPINNED by reference outputs.  The reference is Fortran 90 +
+ * MPI; no Fortran compiler or MPI exists in this image, the reference ships no
+ * tests and no golden vectors, and its one end-to-end input (itimes.out) is
+ * missing from the repository.  The restatement is pinned instead by analytic
+ * known-answer cases (homogeneous plane wave, linear gradient, straight ray)
+ * in tests/test_oracle.py.
+ *
+ * Units follow the reference after its input conversion (F = fm3dt_parallel.f90):
+ *   heights in km (positive up, r = earth + height), colatitude and longitude
+ *   in radians, traveltimes in seconds.
+ * Layouts:
+ *   velv  (nvz+2)(nvx+2)(nvr+2) doubles, r fastest (the .vtx value order,
+ *         F:6118-6125), index k + (nvr+2)*(j + (nvx+2)*i).
+ *   veln  (nnr+3)(nnx+3)(nnz+3) doubles, phi fastest, node indices -1..n+1
+ *         (F:6993), index (iz+1) + (nnz+3)*((ix+1) + (nnx+3)*(ir+1)) with
+ *         1-based iz,ix,ir.
+ *   ttn   nnr*nnx*nnz doubles, phi fastest, index (iz-1)+nnz*((ix-1)+nnx*(ir-1)).
+ *         ir = 1 is the top layer, ir = nnr the bottom layer.
+ *   bottom  nnz*nnx doubles, phi fastest: the boundary-time frame of one
+ *         source (one itimes.out record, F:6908-6913).
+ */
+#ifndef FM3DT_ORACLE_H
+#define FM3DT_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int nvr, nvx, nvz;
+    double gor, gox, goz, dvr, dvx, dvz;
+    int nnr, nnx, nnz;
+    double rgor, rgox, rgoz, dnr, dnx, dnz;
+    double earth;
+} orc_grid;
+
+/* Synthetic teleseismic plane wave on the bottom face (test input generator). */
+typedef struct {
+    double t0;      /* arrival time under the section centre, s */
+    double p;       /* horizontal slowness along the bottom surface, s/km */
+    double cos_az;  /* cosine / sine of the propagation azimuth (from north) */
+    double sin_az;
+} orc_planewave;
+
+double orc_pi(void);
+
+/* .vtx header (degrees, latitude) -> solver units (F:6103-6117). */
+void orc_grid_from_header(const int nv[3], const double vorig[3], const double vstep[3],
+                          const int nn[3], const double norig[3], const double nstep[3],
+                          double earth, orc_grid *g);
+
+/* receivers.dat / sources.dat latitude, longitude (degrees) -> colatitude,
+ * longitude in radians (F:6283-6284, 6313-6314). */
+void orc_latlon_to_rad(int n, const double *lat, const double *lon,
+                       double *colat, double *lonr);
+
+/* Cubic B-spline gridder (F:6989-7038).  Returns 0, or -1 if a velocity
+ * index falls outside 0..nv+1 (the reference reads out of bounds there;
+ * the oracle clamps and reports it). */
+int orc_gridder(const orc_grid *g, const double *velv, double *veln, int *nclamped);
+
+/* Serial narrow-band fast marching of one source: start_fmm seeding
+ * (F:6894-6961) followed by local_fmm (F:78-155) with fouds1_all (fom=0,
+ * F:535-633) or fouds2_all (fom=1, F:635-1004) and the binary heap of
+ * F:1006-1098.  Unset nodes come back as 0.0 like the reference.  Returns
+ * the number of heap pops in *npops.  Returns 0 or a negative error. */
+int orc_fmm(const orc_grid *g, const double *veln, int fom, const double *bottom,
+            double *ttn, long long *npops);
+
+/* Receiver traveltimes (F:7040-7248): trilinear interpolation accumulated
+ * in single precision.  Returns 0, or -(1+k) if receiver k lies outside the
+ * propagation grid. */
+int orc_srtimes(const orc_grid *g, const double *ttn, int nrc, const double *rcr,
+                const double *rcx, const double *rcz, float *trr);
+
+/* Ray back-tracing and Frechet rows (F:7250-7777) with the reference's global
+ * boundary behaviour (rays stop, clipped, at the outer faces of the whole
+ * grid).  fdm is nrc*nmp floats, nmp=(nvr+2)(nvx+2)(nvz+2), column order r
+ * fastest (F:7753-7763); pass NULL to skip the Frechet accumulation (cfd=0).
+ * endpoints gets 3 doubles (height km, colat, lon) per ray; nsteps the step
+ * count per ray (0 when the start cell is outside the grid).  Returns 0 or a
+ * negative error (-2: B-spline support outside the velocity grid). */
+int orc_rays(const orc_grid *g, const double *ttn, const double *veln, int nrc,
+             const double *rcr, const double *rcx, const double *rcz,
+             float *fdm, double *endpoints, int *nsteps);
+
+/* Sparsify one dense Frechet row like F:7739-7765 (|f| >= 1e-6 in single
+ * precision).  Writes up to cap (col, val) pairs with 1-based columns and
+ * returns the count. */
+int orc_sparsify(int nmp, const float *row, int cap, int *cols, float *vals);
+
+/* Synthetic plane-wave boundary frame: t = t0 + p * d, d the distance of the
+ * bottom node from the section centre along the propagation azimuth in the
+ * local tangent plane of the bottom surface.  frame is nnz*nnx, phi fastest. */
+void orc_planewave_frame(const orc_grid *g, const orc_planewave *pw, double *frame);
+
+/* Event parameters of the synthetic plane wave from an epicentral distance
+ * and back-azimuth (degrees). */
+void orc_planewave_params(const orc_grid *g, double delta_deg, double baz_deg,
+                          orc_planewave *pw);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

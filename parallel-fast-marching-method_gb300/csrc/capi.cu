@@ -1,0 +1,640 @@
+// capi.cu -- the C ABI of libfm3dt_gpu (declared in include/fm3dt_gpu.h).
+//
+// Host-side orchestration of the per-source pipeline that fm3dt_parallel.f90
+// runs per source (F:6371-6599): boundary injection, the tile-round solve
+// loop, receiver times, rays and Frechet rows.  All device memory is owned by
+// the context; all work goes to the context's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+using namespace fm3dt;
+
+namespace {
+
+thread_local std::string g_create_err;
+
+int fail(fm3dt_ctx *ctx, int code, const std::string &msg)
+{
+    if (ctx) ctx->err = msg;
+    else g_create_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                 \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? FM3DT_ENOMEM : FM3DT_ECUDA,       \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                     \
+    } while (0)
+
+#define CKL()                                                                                    \
+    do {                                                                                         \
+        cudaError_t e_ = cudaGetLastError();                                                     \
+        if (e_ != cudaSuccess)                                                                   \
+            return fail(ctx, FM3DT_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+// fm3dt_parallel.f90:61 initialises the double-precision pi from a
+// default-kind (single precision) literal; the converted angles use that value.
+double ref_pi() { return (double)3.1415926535898f; }
+
+Geom convert(const fm3dt_grid_desc &d)
+{
+    const double pi = ref_pi();
+    Geom g;
+    g.nvr = d.nvr; g.nvx = d.nvx; g.nvz = d.nvz;
+    g.gor = d.gor;
+    g.dvr = d.dvr;
+    g.dvx = d.dvxd * pi / 180.0;          // F:6110-6117
+    g.dvz = d.dvzd * pi / 180.0;
+    g.gox = (90.0 - d.goxd) * pi / 180.0;
+    g.goz = d.gozd * pi / 180.0;
+    g.nnr = d.nnr; g.nnx = d.nnx; g.nnz = d.nnz;
+    g.rgor = d.rgor;
+    g.dnr = d.dnr;
+    g.dnx = d.dnxd * pi / 180.0;
+    g.dnz = d.dnzd * pi / 180.0;
+    g.rgox = (90.0 - d.rgoxd) * pi / 180.0;
+    g.rgoz = d.rgozd * pi / 180.0;
+    g.earth = d.earth;
+    return g;
+}
+
+int sm_count()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+size_t rsize(int prec) { return prec == FM3DT_FP64 ? sizeof(double) : sizeof(float); }
+
+int tiles_per_event(const Geom &g, int shape, int *ntr, int *ntx, int *ntz)
+{
+    const TileShape s = kShapes[shape];
+    *ntr = (g.nnr + s.tr - 1) / s.tr;
+    *ntx = (g.nnx + s.tx - 1) / s.tx;
+    *ntz = (g.nnz + s.tz - 1) / s.tz;
+    return *ntr * *ntx * *ntz;
+}
+
+template <typename R>
+void fill_geometry(const Geom &g, std::vector<R> &hx, std::vector<R> &hz)
+{
+    // spacings at each node as the stencil evaluates them (F:642-644, 712ff):
+    // dr, r*dtheta, r*sin(theta)*dphi with r = rgor - (ir-1)*dnr + earth
+    hx.resize(g.nnr);
+    hz.resize((size_t)g.nnr * g.nnx);
+    for (int ir = 0; ir < g.nnr; ++ir) {
+        const double ri = g.rgor - (double)ir * g.dnr + g.earth;
+        hx[ir] = (R)(ri * g.dnx);
+        for (int ix = 0; ix < g.nnx; ++ix) {
+            const double risti = ri * std::sin(g.rgox + (double)ix * g.dnx);
+            hz[(size_t)ir * g.nnx + ix] = (R)(risti * g.dnz);
+        }
+    }
+}
+
+template <typename R>
+int upload_geometry(fm3dt_ctx *ctx)
+{
+    std::vector<R> hx, hz;
+    fill_geometry<R>(ctx->g, hx, hz);
+    CK(cudaMemcpy(ctx->d_hx, hx.data(), hx.size() * sizeof(R), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_hz, hz.data(), hz.size() * sizeof(R), cudaMemcpyHostToDevice));
+    return FM3DT_OK;
+}
+
+int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st)
+{
+    cudaStream_t s = ctx->stream;
+    const Geom &g = ctx->g;
+    cudaEvent_t ev0, ev1;
+    CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev1));
+    CK(cudaEventRecord(ev0, s));
+
+    launch_fill_inf(ctx->d_T, (size_t)nev * ctx->N, ctx->prec, s);
+    launch_finalize_frames(g, nev, ctx->prec, ctx->d_frames, ctx->d_T, ctx->d_frozen, ctx->d_base, s);
+    ctx->launches += 2;
+    CKL();
+
+    const int shape = ctx->shape;
+    const TileShape ts = kShapes[shape];
+    int ntr, ntx, ntz;
+    const int tpe = tiles_per_event(g, shape, &ntr, &ntx, &ntz);
+    // tiles whose nodes or 2-deep halos include the bottom layer
+    const int tlo = std::max(0, (g.nnr - 3) / ts.tr);
+    const int first = tlo * ntx * ntz;
+    const int cnt = (ntr - tlo) * ntx * ntz;
+    CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
+    CK(cudaMemsetAsync(ctx->d_count[1], 0, sizeof(int), s));
+    CK(cudaMemsetAsync(ctx->d_stats, 0, 3 * sizeof(unsigned long long), s));
+    launch_initial_tiles(nev, tpe, first, cnt, ctx->d_list[0], ctx->d_count[0], ctx->d_flag, s);
+    ctx->launches += 1;
+    CKL();
+
+    const int bps = std::max(1, round_blocks_per_sm(shape, ctx->prec));
+    const int grid = bps * sm_count();
+    const int max_rounds = ctx->max_rounds > 0 ? ctx->max_rounds : 64 * (ntr + ntx + ntz) + 256;
+    const int chunk = 8;
+
+    RoundArgs<double> a64{};
+    RoundArgs<float> a32{};
+    auto fill_args = [&](auto &a, auto *T, auto *sl, auto *hx, auto *hz) {
+        a.T = T; a.s = sl; a.hx = hx; a.hz = hz;
+        a.frozen = ctx->d_frozen;
+        a.nnr = g.nnr; a.nnx = g.nnx; a.nnz = g.nnz;
+        a.ntr = ntr; a.ntx = ntx; a.ntz = ntz;
+        a.tiles_per_event = tpe;
+        a.flag = ctx->d_flag;
+        a.max_passes = ctx->max_passes;
+        a.order2 = ctx->desc.fom ? 1 : 0;
+        a.stats = ctx->d_stats;
+    };
+    if (ctx->prec == FM3DT_FP64) {
+        fill_args(a64, (double *)ctx->d_T, (const double *)ctx->d_s, (const double *)ctx->d_hx,
+                  (const double *)ctx->d_hz);
+        a64.hr = g.dnr;
+    } else {
+        fill_args(a32, (float *)ctx->d_T, (const float *)ctx->d_s, (const float *)ctx->d_hx,
+                  (const float *)ctx->d_hz);
+        a32.hr = (float)g.dnr;
+    }
+
+    int rounds = 0;
+    bool done = false;
+    double round_ms = 0.0;
+    while (!done && rounds < max_rounds) {
+        int k;
+        const int first_round = rounds;
+        while ((int)ctx->round_events.size() < 2 * chunk) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            ctx->round_events.push_back(e);
+        }
+        for (k = 0; k < chunk && rounds < max_rounds; ++k, ++rounds) {
+            const int cur = rounds & 1, nxt = cur ^ 1;
+            CK(cudaMemsetAsync(ctx->d_count[nxt], 0, sizeof(int), s));
+            CK(cudaEventRecord(ctx->round_events[2 * k], s));
+            if (ctx->prec == FM3DT_FP64) {
+                a64.cur_list = ctx->d_list[cur]; a64.cur_count = ctx->d_count[cur];
+                a64.next_list = ctx->d_list[nxt]; a64.next_count = ctx->d_count[nxt];
+                launch_round_f64(shape, grid, a64, s);
+            } else {
+                a32.cur_list = ctx->d_list[cur]; a32.cur_count = ctx->d_count[cur];
+                a32.next_list = ctx->d_list[nxt]; a32.next_count = ctx->d_count[nxt];
+                launch_round_f32(shape, grid, a32, s);
+            }
+            CK(cudaEventRecord(ctx->round_events[2 * k + 1], s));
+            ctx->launches += 1;
+        }
+        CKL();
+        const int last_next = (rounds - 1) & 1 ? 0 : 1;
+        CK(cudaMemcpyAsync(ctx->h_count, ctx->d_count[last_next], sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        for (int q = 0; q < rounds - first_round; ++q) {
+            float m = 0.0f;
+            cudaEventElapsedTime(&m, ctx->round_events[2 * q], ctx->round_events[2 * q + 1]);
+            round_ms += m;
+        }
+        if (*ctx->h_count == 0) done = true;
+    }
+    CK(cudaEventRecord(ev1, s));
+    CK(cudaMemcpyAsync(ctx->h_stats, ctx->d_stats, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    ctx->h_base.resize(nev);
+    CK(cudaMemcpyAsync(ctx->h_base.data(), ctx->d_base, nev * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    ctx->nev_solved = nev;
+    if (st) {
+        st->rounds = rounds;
+        st->converged = done ? 1 : 0;
+        st->tile_updates = (int64_t)ctx->h_stats[0];
+        st->node_passes = (int64_t)ctx->h_stats[1];
+        st->tile_nodes = (int64_t)ctx->h_stats[2];
+        st->ms = ms;
+        st->round_ms = round_ms;
+        st->round_launches = rounds;
+    }
+    if (!done) return fail(ctx, FM3DT_ENOCONV, "solver round limit reached before convergence");
+    return FM3DT_OK;
+}
+
+int check_ready(fm3dt_ctx *ctx, int nev)
+{
+    if (!ctx) return FM3DT_EINVAL;
+    if (!ctx->have_velocity) return fail(ctx, FM3DT_ESTATE, "fm3dt_set_velocity must come first");
+    if (nev < 1 || nev > ctx->maxev) return fail(ctx, FM3DT_EINVAL, "nev outside 1..max_events");
+    return FM3DT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
+{
+    fm3dt_ctx *ctx = nullptr;
+    if (!desc || !out) return fail(nullptr, FM3DT_EINVAL, "null argument");
+    *out = nullptr;
+    const fm3dt_grid_desc &d = *desc;
+    if (d.nnr < 3 || d.nnx < 3 || d.nnz < 3 || d.nvr < 1 || d.nvx < 1 || d.nvz < 1)
+        return fail(nullptr, FM3DT_EINVAL, "grid dimensions too small (need nn >= 3, nv >= 1)");
+    if (d.dnr <= 0 || d.dnxd <= 0 || d.dnzd <= 0 || d.dvr <= 0 || d.dvxd <= 0 || d.dvzd <= 0 || d.earth <= 0)
+        return fail(nullptr, FM3DT_EINVAL, "grid spacings and earth radius must be positive");
+    if (d.fom != 0 && d.fom != 1) return fail(nullptr, FM3DT_EINVAL, "fom must be 0 or 1");
+    if (d.precision != FM3DT_FP64 && d.precision != FM3DT_FP32_OFFSET)
+        return fail(nullptr, FM3DT_EINVAL, "unknown precision");
+    if (d.max_events < 1) return fail(nullptr, FM3DT_EINVAL, "max_events must be >= 1");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return fail(nullptr, FM3DT_ENODEV, "no CUDA device");
+    }
+    ctx = new fm3dt_ctx();
+    ctx->desc = d;
+    ctx->g = convert(d);
+    ctx->prec = d.precision;
+    ctx->maxev = d.max_events;
+    ctx->N = (size_t)d.nnr * d.nnx * d.nnz;
+    ctx->NB = (size_t)d.nnx * d.nnz;
+    ctx->hr = ctx->g.dnr;
+    const size_t rs = rsize(ctx->prec);
+    size_t maxtiles = 0;
+    for (int sh = 0; sh < kNumShapes; ++sh) {
+        int a, b, c;
+        maxtiles = std::max(maxtiles, (size_t)tiles_per_event(ctx->g, sh, &a, &b, &c));
+    }
+    ctx->flag_capacity = maxtiles * (size_t)ctx->maxev;
+    if (ctx->flag_capacity > (size_t)INT32_MAX) {
+        delete ctx;
+        return fail(nullptr, FM3DT_EINVAL, "too many tiles for 32-bit work items");
+    }
+    auto cleanup_fail = [&](int code, const std::string &m) {
+        g_create_err = m;
+        fm3dt_ctx_destroy(ctx);
+        return code;
+    };
+#define CKC(call)                                                                                     \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return cleanup_fail(e_ == cudaErrorMemoryAllocation ? FM3DT_ENOMEM : FM3DT_ECUDA,         \
+                                std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+    } while (0)
+    CKC(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    const size_t nvel = (size_t)(d.nvr + 2) * (d.nvx + 2) * (d.nvz + 2);
+    const size_t npad = (size_t)(d.nnr + 3) * (d.nnx + 3) * (d.nnz + 3);
+    CKC(cudaMalloc(&ctx->d_velv, nvel * sizeof(double)));
+    CKC(cudaMalloc(&ctx->d_veln, npad * sizeof(double)));
+    CKC(cudaMalloc(&ctx->d_s, ctx->N * rs));
+    CKC(cudaMalloc(&ctx->d_hx, (size_t)d.nnr * rs));
+    CKC(cudaMalloc(&ctx->d_hz, (size_t)d.nnr * d.nnx * rs));
+    CKC(cudaMalloc(&ctx->d_T, ctx->N * ctx->maxev * rs));
+    CKC(cudaMalloc(&ctx->d_frames, ctx->NB * ctx->maxev * sizeof(double)));
+    CKC(cudaMalloc(&ctx->d_base, ctx->maxev * sizeof(double)));
+    CKC(cudaMalloc(&ctx->d_frozen, ctx->NB * ctx->maxev));
+    CKC(cudaMalloc(&ctx->d_flag, ctx->flag_capacity * sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_list[0], ctx->flag_capacity * sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_list[1], ctx->flag_capacity * sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_count[0], sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_count[1], sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_stats, 3 * sizeof(unsigned long long)));
+    CKC(cudaMalloc(&ctx->d_params, 4 * ctx->maxev * sizeof(double)));
+    CKC(cudaMallocHost(&ctx->h_count, sizeof(int)));
+    CKC(cudaMallocHost(&ctx->h_stats, 3 * sizeof(unsigned long long)));
+    CKC(cudaMemset(ctx->d_base, 0, ctx->maxev * sizeof(double)));
+    int rc = ctx->prec == FM3DT_FP64 ? upload_geometry<double>(ctx) : upload_geometry<float>(ctx);
+    if (rc != FM3DT_OK) return cleanup_fail(rc, ctx->err);
+#undef CKC
+    *out = ctx;
+    return FM3DT_OK;
+}
+
+int fm3dt_set_velocity(fm3dt_ctx *ctx, const double *velv)
+{
+    if (!ctx || !velv) return FM3DT_EINVAL;
+    const Geom &g = ctx->g;
+    const size_t nvel = (size_t)(g.nvr + 2) * (g.nvx + 2) * (g.nvz + 2);
+    for (size_t q = 0; q < nvel; ++q)
+        if (!(velv[q] > 0.0) || !std::isfinite(velv[q]))
+            return fail(ctx, FM3DT_EINVAL, "velocity values must be positive and finite");
+    CK(cudaMemcpyAsync(ctx->d_velv, velv, nvel * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    launch_gridder(g, ctx->d_velv, ctx->d_veln, ctx->stream);
+    launch_slowness(g, ctx->d_veln, ctx->d_s, ctx->prec, ctx->stream);
+    ctx->launches += 2;
+    CKL();
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->have_velocity = 1;
+    return FM3DT_OK;
+}
+
+int fm3dt_solve(fm3dt_ctx *ctx, int nev, const double *boundary, fm3dt_status *st)
+{
+    int rc = check_ready(ctx, nev);
+    if (rc) return rc;
+    if (!boundary) return fail(ctx, FM3DT_EINVAL, "null boundary");
+    CK(cudaMemcpyAsync(ctx->d_frames, boundary, (size_t)nev * ctx->NB * sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    return solve_common(ctx, nev, st);
+}
+
+int fm3dt_solve_device(fm3dt_ctx *ctx, int nev, const double *d_boundary, fm3dt_status *st)
+{
+    int rc = check_ready(ctx, nev);
+    if (rc) return rc;
+    if (!d_boundary) return fail(ctx, FM3DT_EINVAL, "null boundary");
+    CK(cudaMemcpyAsync(ctx->d_frames, d_boundary, (size_t)nev * ctx->NB * sizeof(double), cudaMemcpyDeviceToDevice,
+                       ctx->stream));
+    return solve_common(ctx, nev, st);
+}
+
+int fm3dt_solve_planewave(fm3dt_ctx *ctx, int nev, const double *params, fm3dt_status *st)
+{
+    int rc = check_ready(ctx, nev);
+    if (rc) return rc;
+    if (!params) return fail(ctx, FM3DT_EINVAL, "null params");
+    const Geom &g = ctx->g;
+    PlaneWaveGeom pg;
+    pg.rb = g.earth + (g.rgor - (double)(g.nnr - 1) * g.dnr);
+    pg.thc = g.rgox + (double)(g.nnx - 1) * g.dnx * 0.5;
+    pg.phc = g.rgoz + (double)(g.nnz - 1) * g.dnz * 0.5;
+    pg.rbs = pg.rb * std::sin(pg.thc);
+    CK(cudaMemcpyAsync(ctx->d_params, params, (size_t)nev * 4 * sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    launch_planewave_frames(g, pg, nev, ctx->d_params, ctx->d_frames, ctx->stream);
+    ctx->launches += 1;
+    CKL();
+    return solve_common(ctx, nev, st);
+}
+
+int fm3dt_receiver_times(fm3dt_ctx *ctx, int nrc, const double *rcr, const double *rcx, const double *rcz,
+                         float *out)
+{
+    if (!ctx || nrc < 0 || (nrc > 0 && (!rcr || !rcx || !rcz || !out))) return FM3DT_EINVAL;
+    if (ctx->nev_solved < 1) return fail(ctx, FM3DT_ESTATE, "no solved events");
+    if (nrc == 0) return FM3DT_OK;
+    const Geom &g = ctx->g;
+    std::vector<RecCell> cells(nrc);
+    for (int i = 0; i < nrc; ++i) {
+        // F:7066-7097 with the last-subdomain clamp of F:7069-7070
+        RecCell c;
+        c.irr = (int)std::floor((g.rgor - rcr[i]) / g.dnr) + 1;
+        c.irx = (int)std::floor((rcx[i] - g.rgox) / g.dnx) + 1;
+        c.irz = (int)std::floor((rcz[i] - g.rgoz) / g.dnz) + 1;
+        c.pad = 0;
+        if (c.irx == g.nnx) c.irx--;
+        if (c.irz == g.nnz) c.irz--;
+        if (c.irr < 1 || c.irr >= g.nnr || c.irx < 1 || c.irx >= g.nnx || c.irz < 1 || c.irz >= g.nnz)
+            return fail(ctx, FM3DT_ERANGE, "receiver " + std::to_string(i + 1) + " lies outside the grid");
+        c.drx = (rcx[i] - g.rgox) - (double)(c.irx - 1) * g.dnx;
+        c.drz = (rcz[i] - g.rgoz) - (double)(c.irz - 1) * g.dnz;
+        c.drr = (g.rgor - rcr[i]) - (double)(c.irr - 1) * g.dnr;
+        cells[i] = c;
+    }
+    RecCell *d_cells = nullptr;
+    float *d_out = nullptr;
+    const int nev = ctx->nev_solved;
+    CK(cudaMallocAsync(&d_cells, nrc * sizeof(RecCell), ctx->stream));
+    CK(cudaMallocAsync(&d_out, (size_t)nev * nrc * sizeof(float), ctx->stream));
+    CK(cudaMemcpyAsync(d_cells, cells.data(), nrc * sizeof(RecCell), cudaMemcpyHostToDevice, ctx->stream));
+    launch_receivers(g, ctx->prec, ctx->d_T, ctx->d_base, nev, nrc, d_cells, d_out, ctx->stream);
+    ctx->launches += 1;
+    CKL();
+    CK(cudaMemcpyAsync(out, d_out, (size_t)nev * nrc * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(d_cells, ctx->stream));
+    CK(cudaFreeAsync(d_out, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FM3DT_OK;
+}
+
+int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double *rcx, const double *rcz,
+                       int64_t *row_ptr, int32_t *cols, float *vals, int64_t cap, double *endpoints)
+{
+    if (!ctx || nrc < 0 || (nrc > 0 && (!rcr || !rcx || !rcz))) return FM3DT_EINVAL;
+    if (ctx->nev_solved < 1) return fail(ctx, FM3DT_ESTATE, "no solved events");
+    if (!ctx->have_velocity) return fail(ctx, FM3DT_ESTATE, "no velocity model");
+    const bool want_rows = cols != nullptr && vals != nullptr;
+    if (want_rows && !row_ptr) return FM3DT_EINVAL;
+    if (nrc == 0) return FM3DT_OK;
+    const Geom &g = ctx->g;
+    const int nev = ctx->nev_solved;
+    const int nrows = nev * nrc;
+    const size_t nmp = (size_t)(g.nvr + 2) * (g.nvx + 2) * (g.nvz + 2);
+    cudaStream_t s = ctx->stream;
+    double *d_rec = nullptr, *d_end = nullptr;
+    int *d_steps = nullptr, *d_status = nullptr;
+    float *d_fdm = nullptr;
+    int64_t *d_counts = nullptr, *d_rowptr = nullptr;
+    int32_t *d_cols = nullptr;
+    float *d_vals = nullptr;
+    CK(cudaMallocAsync(&d_rec, 3 * (size_t)nrc * sizeof(double), s));
+    CK(cudaMallocAsync(&d_end, 3 * (size_t)nrows * sizeof(double), s));
+    CK(cudaMallocAsync(&d_steps, (size_t)nrows * sizeof(int), s));
+    CK(cudaMallocAsync(&d_status, (size_t)nrows * sizeof(int), s));
+    CK(cudaMemcpyAsync(d_rec, rcr, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_rec + nrc, rcx, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_rec + 2 * nrc, rcz, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (want_rows) {
+        CK(cudaMallocAsync(&d_fdm, (size_t)nrows * nmp * sizeof(float), s));
+        CK(cudaMemsetAsync(d_fdm, 0, (size_t)nrows * nmp * sizeof(float), s));
+    }
+    RayArgs ra;
+    ra.g = g;
+    ra.prec = ctx->prec;
+    ra.T = ctx->d_T;
+    ra.veln = ctx->d_veln;
+    ra.nev = nev;
+    ra.nrc = nrc;
+    ra.rcr = d_rec;
+    ra.rcx = d_rec + nrc;
+    ra.rcz = d_rec + 2 * nrc;
+    ra.fdm = d_fdm;
+    ra.endpoints = d_end;
+    ra.nsteps = d_steps;
+    ra.status = d_status;
+    launch_rays(ra, s);
+    ctx->launches += 1;
+    CKL();
+    std::vector<int> status(nrows);
+    CK(cudaMemcpyAsync(status.data(), d_status, nrows * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (endpoints)
+        CK(cudaMemcpyAsync(endpoints, d_end, 3 * (size_t)nrows * sizeof(double), cudaMemcpyDeviceToHost, s));
+    int rc = FM3DT_OK;
+    if (want_rows) {
+        CK(cudaMallocAsync(&d_counts, (size_t)nrows * sizeof(int64_t), s));
+        launch_row_counts(d_fdm, nrows, (int)nmp, d_counts, s);
+        ctx->launches += 1;
+        CKL();
+        std::vector<int64_t> counts(nrows);
+        CK(cudaMemcpyAsync(counts.data(), d_counts, nrows * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        row_ptr[0] = 0;
+        for (int q = 0; q < nrows; ++q) row_ptr[q + 1] = row_ptr[q] + counts[q];
+        const int64_t total = row_ptr[nrows];
+        if (total > cap) {
+            rc = fail(ctx, FM3DT_ERANGE, "Frechet rows need " + std::to_string(total) + " entries, capacity " +
+                                             std::to_string(cap));
+        } else if (total > 0) {
+            CK(cudaMallocAsync(&d_rowptr, (size_t)(nrows + 1) * sizeof(int64_t), s));
+            CK(cudaMallocAsync(&d_cols, (size_t)total * sizeof(int32_t), s));
+            CK(cudaMallocAsync(&d_vals, (size_t)total * sizeof(float), s));
+            CK(cudaMemcpyAsync(d_rowptr, row_ptr, (nrows + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+            launch_row_compact(d_fdm, nrows, (int)nmp, d_rowptr, d_cols, d_vals, s);
+            ctx->launches += 1;
+            CKL();
+            CK(cudaMemcpyAsync(cols, d_cols, (size_t)total * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(vals, d_vals, (size_t)total * sizeof(float), cudaMemcpyDeviceToHost, s));
+        }
+    } else if (row_ptr) {
+        for (int q = 0; q <= nrows; ++q) row_ptr[q] = 0;
+    }
+    CK(cudaStreamSynchronize(s));
+    cudaFreeAsync(d_rec, s);
+    cudaFreeAsync(d_end, s);
+    cudaFreeAsync(d_steps, s);
+    cudaFreeAsync(d_status, s);
+    if (d_fdm) cudaFreeAsync(d_fdm, s);
+    if (d_counts) cudaFreeAsync(d_counts, s);
+    if (d_rowptr) cudaFreeAsync(d_rowptr, s);
+    if (d_cols) cudaFreeAsync(d_cols, s);
+    if (d_vals) cudaFreeAsync(d_vals, s);
+    CK(cudaStreamSynchronize(s));
+    if (rc == FM3DT_OK)
+        for (int q = 0; q < nrows; ++q)
+            if (status[q])
+                return fail(ctx, FM3DT_ERANGE, "ray " + std::to_string(q) +
+                                                   ": B-spline support outside the velocity grid");
+    return rc;
+}
+
+int fm3dt_get_times(fm3dt_ctx *ctx, int event, double *ttn)
+{
+    if (!ctx || !ttn) return FM3DT_EINVAL;
+    if (event < 0 || event >= ctx->nev_solved) return fail(ctx, FM3DT_EINVAL, "event not solved");
+    double *d_out = nullptr;
+    CK(cudaMallocAsync(&d_out, ctx->N * sizeof(double), ctx->stream));
+    const double base = ctx->prec == FM3DT_FP64 ? 0.0 : ctx->h_base[event];
+    launch_to_absolute(ctx->g, ctx->prec, ctx->d_T, (size_t)event * ctx->N, base, d_out, ctx->stream);
+    ctx->launches += 1;
+    CKL();
+    CK(cudaMemcpyAsync(ttn, d_out, ctx->N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(d_out, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FM3DT_OK;
+}
+
+int fm3dt_get_velocity(fm3dt_ctx *ctx, double *veln)
+{
+    if (!ctx || !veln) return FM3DT_EINVAL;
+    if (!ctx->have_velocity) return fail(ctx, FM3DT_ESTATE, "no velocity model");
+    const Geom &g = ctx->g;
+    const size_t npad = (size_t)(g.nnr + 3) * (g.nnx + 3) * (g.nnz + 3);
+    CK(cudaMemcpyAsync(veln, ctx->d_veln, npad * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FM3DT_OK;
+}
+
+int fm3dt_set_times(fm3dt_ctx *ctx, int event, int nev_total, const double *ttn)
+{
+    if (!ctx || !ttn) return FM3DT_EINVAL;
+    if (nev_total < 1 || nev_total > ctx->maxev || event < 0 || event >= nev_total)
+        return fail(ctx, FM3DT_EINVAL, "event index outside 1..max_events");
+    double base = 0.0;
+    if (ctx->prec != FM3DT_FP64) {
+        double m = INFINITY;
+        for (size_t q = 0; q < ctx->N; ++q)
+            if (ttn[q] > 0.0 && ttn[q] < m) m = ttn[q];
+        base = std::isfinite(m) ? m : 0.0;
+    }
+    if ((int)ctx->h_base.size() < nev_total) ctx->h_base.resize(nev_total, 0.0);
+    ctx->h_base[event] = base;
+    double *d_in = nullptr;
+    CK(cudaMallocAsync(&d_in, ctx->N * sizeof(double), ctx->stream));
+    CK(cudaMemcpyAsync(d_in, ttn, ctx->N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    launch_from_absolute(ctx->g, ctx->prec, d_in, base, ctx->d_T, (size_t)event * ctx->N, ctx->stream);
+    ctx->launches += 1;
+    CKL();
+    CK(cudaMemcpyAsync(ctx->d_base + event, &ctx->h_base[event], sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaFreeAsync(d_in, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->nev_solved = nev_total;
+    return FM3DT_OK;
+}
+
+int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rounds)
+{
+    if (!ctx) return FM3DT_EINVAL;
+    if (tile_shape < 0 || tile_shape >= kNumShapes) return fail(ctx, FM3DT_EINVAL, "tile shape out of range");
+    ctx->shape = tile_shape;
+    if (max_passes > 0) ctx->max_passes = max_passes;
+    if (max_rounds > 0) ctx->max_rounds = max_rounds;
+    return FM3DT_OK;
+}
+
+int fm3dt_tile_shapes(int *count)
+{
+    if (!count) return FM3DT_EINVAL;
+    *count = kNumShapes;
+    return FM3DT_OK;
+}
+
+int fm3dt_tile_shape(int index, int *tr, int *tx, int *tz)
+{
+    if (index < 0 || index >= kNumShapes || !tr || !tx || !tz) return FM3DT_EINVAL;
+    *tr = kShapes[index].tr;
+    *tx = kShapes[index].tx;
+    *tz = kShapes[index].tz;
+    return FM3DT_OK;
+}
+
+int64_t fm3dt_launch_count(const fm3dt_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+const char *fm3dt_last_error(const fm3dt_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_err.c_str(); }
+
+void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
+{
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto &gr : ctx->graphs) cudaGraphExecDestroy(gr.exec);
+    for (auto e : ctx->round_events) cudaEventDestroy(e);
+    cudaFree(ctx->d_velv);
+    cudaFree(ctx->d_veln);
+    cudaFree(ctx->d_s);
+    cudaFree(ctx->d_hx);
+    cudaFree(ctx->d_hz);
+    cudaFree(ctx->d_T);
+    cudaFree(ctx->d_frames);
+    cudaFree(ctx->d_base);
+    cudaFree(ctx->d_frozen);
+    cudaFree(ctx->d_flag);
+    cudaFree(ctx->d_list[0]);
+    cudaFree(ctx->d_list[1]);
+    cudaFree(ctx->d_count[0]);
+    cudaFree(ctx->d_count[1]);
+    cudaFree(ctx->d_stats);
+    cudaFree(ctx->d_params);
+    if (ctx->h_count) cudaFreeHost(ctx->h_count);
+    if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+}  // extern "C"

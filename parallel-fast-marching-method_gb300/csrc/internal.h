@@ -1,0 +1,138 @@
+// internal.h -- device data layout and kernel launchers of libfm3dt_gpu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/fm3dt_gpu.h"
+
+namespace fm3dt {
+
+// Grid in solver units (converted like fm3dt_parallel.f90:6110-6117).
+struct Geom {
+    int nvr, nvx, nvz;
+    double gor, gox, goz, dvr, dvx, dvz;
+    int nnr, nnx, nnz;
+    double rgor, rgox, rgoz, dnr, dnx, dnz;
+    double earth;
+};
+
+// Tile shapes of the solver kernel (r, theta, phi extents; phi is the
+// contiguous axis).  One thread owns one (theta, phi) column of TR nodes.
+struct TileShape { int tr, tx, tz; };
+constexpr int kNumShapes = 6;
+constexpr TileShape kShapes[kNumShapes] = {{4, 8, 32}, {8, 8, 32}, {4, 4, 32}, {8, 4, 32}, {2, 8, 32}, {4, 16, 16}};
+
+// Arguments of one solver round.
+template <typename R>
+struct RoundArgs {
+    R *T;                       // [E][nnr][nnx][nnz]
+    const R *s;                 // [nnr][nnx][nnz] slowness
+    const R *hx;                // [nnr]      r * dtheta
+    const R *hz;                // [nnr*nnx]  r * sin(theta) * dphi
+    R hr;                       // dr
+    const uint8_t *frozen;      // [E][nnx*nnz] fixed bottom-layer nodes
+    int nnr, nnx, nnz;
+    int ntr, ntx, ntz;          // tiles per axis
+    int tiles_per_event;
+    int *flag;                  // [E*tiles] 1 while a tile is queued
+    const int *cur_list;
+    const int *cur_count;
+    int *next_list;
+    int *next_count;
+    int max_passes;
+    int order2;
+    unsigned long long *stats;  // [0] tiles processed, [1] node updates, [2] staged nodes
+};
+
+void launch_round_f64(int shape, int grid, const RoundArgs<double> &a, cudaStream_t st);
+void launch_round_f32(int shape, int grid, const RoundArgs<float> &a, cudaStream_t st);
+int round_blocks_per_sm(int shape, int prec);
+
+// model.cu
+void launch_gridder(const Geom &g, const double *velv, double *veln, cudaStream_t st);
+void launch_slowness(const Geom &g, const double *veln, void *s, int prec, cudaStream_t st);
+
+// boundary.cu
+struct PlaneWaveGeom { double rb, thc, phc, rbs; };
+void launch_planewave_frames(const Geom &g, const PlaneWaveGeom &pg, int nev, const double *params,
+                             double *frames, cudaStream_t st);
+void launch_finalize_frames(const Geom &g, int nev, int prec, const double *frames, void *T,
+                            uint8_t *frozen, double *base, cudaStream_t st);
+void launch_fill_inf(void *T, size_t n, int prec, cudaStream_t st);
+void launch_initial_tiles(int nev, int tiles_per_event, int first_tile, int count_per_event,
+                          int *list, int *count, int *flag, cudaStream_t st);
+void launch_to_absolute(const Geom &g, int prec, const void *T, size_t offset, double base, double *out,
+                        cudaStream_t st);
+void launch_from_absolute(const Geom &g, int prec, const double *in, double base, void *T, size_t offset,
+                          cudaStream_t st);
+
+// receivers.cu
+struct RecCell { int irr, irx, irz, pad; double drr, drx, drz; };
+void launch_receivers(const Geom &g, int prec, const void *T, const double *base, int nev, int nrc,
+                      const RecCell *cells, float *out, cudaStream_t st);
+
+// rays.cu
+struct RayArgs {
+    Geom g;
+    int prec;
+    const void *T;              // [E][N] traveltimes (R)
+    const double *veln;         // padded velocity (-1..n+1)
+    int nev, nrc;
+    const double *rcr, *rcx, *rcz;
+    float *fdm;                 // [E*nrc][nmp] dense rows, or nullptr
+    double *endpoints;          // [E*nrc][3]
+    int *nsteps;                // [E*nrc]
+    int *status;                // [E*nrc] 0 ok, 1 B-spline support outside grid
+};
+void launch_rays(const RayArgs &a, cudaStream_t st);
+void launch_row_counts(const float *fdm, int nrows, int nmp, int64_t *counts, cudaStream_t st);
+void launch_row_compact(const float *fdm, int nrows, int nmp, const int64_t *row_ptr, int32_t *cols,
+                        float *vals, cudaStream_t st);
+
+}  // namespace fm3dt
+
+struct fm3dt_ctx {
+    fm3dt_grid_desc desc;
+    fm3dt::Geom g;
+    int prec = 0;
+    int maxev = 0;
+    size_t N = 0;       // nodes per event
+    size_t NB = 0;      // bottom-frame nodes per event
+    cudaStream_t stream = nullptr;
+    // device buffers
+    double *d_velv = nullptr;
+    double *d_veln = nullptr;
+    void *d_s = nullptr;
+    void *d_hx = nullptr;
+    void *d_hz = nullptr;
+    void *d_T = nullptr;
+    double *d_frames = nullptr;
+    double *d_base = nullptr;
+    uint8_t *d_frozen = nullptr;
+    int *d_flag = nullptr;
+    int *d_list[2] = {nullptr, nullptr};
+    int *d_count[2] = {nullptr, nullptr};
+    unsigned long long *d_stats = nullptr;
+    double *d_params = nullptr;
+    int *h_count = nullptr;       // pinned
+    unsigned long long *h_stats = nullptr;  // pinned
+    std::vector<double> h_base;
+    double hr = 0.0;
+    int have_velocity = 0;
+    int nev_solved = 0;
+    // tuning
+    int shape = 0;
+    int max_passes = 64;
+    int max_rounds = 0;           // 0 = automatic
+    size_t flag_capacity = 0;     // tiles allocated for flags/lists
+    int64_t launches = 0;
+    std::string err;
+    // graphs of solver rounds, keyed by shape and event count
+    struct Graph { int shape, nev, rounds; cudaGraphExec_t exec; };
+    std::vector<Graph> graphs;
+    std::vector<cudaEvent_t> round_events;   // start/stop pairs of round kernels
+};

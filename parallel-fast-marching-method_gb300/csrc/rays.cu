@@ -1,0 +1,346 @@
+// rays.cu -- kernel (d): ray back-tracing down the traveltime gradient and
+// Frechet-row assembly (fm3dt_parallel.f90 parallel_rpaths, F:7250-7777, and
+// the writer's row merge, F:6503-6599).
+//
+// One thread traces one (event, receiver) ray over the whole grid, so the
+// reference's ray hand-off between subdomains (F:6464-6501) and the partial
+// rows it creates disappear; the global outer faces stop a ray exactly where
+// the reference's boundary subdomains stop it (clip to the first face
+// crossed, F:7474-7541).  The row accumulates in single precision in the same
+// order as the reference's REAL(4) fdm (F:7722-7732), including its quirks:
+// the segment clipped at the grid face is integrated with the full nominal
+// step length (dinc from vrat*dpl), and the start-point B-spline weights of a
+// sub-segment that follows a velocity-cell crossing keep the indices of the
+// new cell (F:7647-7652, 7717-7732).
+// Compiled without FMA contraction.
+#include "internal.h"
+
+namespace fm3dt {
+
+__device__ __forceinline__ void bspl(double u, double w[4])
+{
+    const double u2 = u * u, u3 = u * u * u;
+    const double om = 1.0 - u;
+    w[0] = om * om * om / 6.0;
+    w[1] = (4.0 - 6.0 * u2 + 3.0 * u3) / 6.0;
+    w[2] = (1.0 + 3.0 * u + 3.0 * u2 - 3.0 * u3) / 6.0;
+    w[3] = u3 / 6.0;
+}
+
+struct RayCtx {
+    const Geom *g;
+    const double *veln;
+};
+
+__device__ __forceinline__ double veln_at(const Geom &g, const double *veln, int iz, int ix, int ir)
+{
+    return veln[(size_t)(iz + 1) + (size_t)(g.nnz + 3) * ((size_t)(ix + 1) + (size_t)(g.nnx + 3) * (size_t)(ir + 1))];
+}
+
+// trilinear velocity at a point of propagation cell (ipz,ipx,ipr) (F:7629-7641)
+__device__ double trilin(const Geom &g, const double *veln, int ipz, int ipx, int ipr, double drr, double drx,
+                         double drz)
+{
+    double vel = 0.0;
+    for (int k = 1; k <= 2; ++k)
+        for (int l = 1; l <= 2; ++l)
+            for (int m = 1; m <= 2; ++m) {
+                double produ = (1.0 - fabs(((double)(m - 1) * g.dnz - drz) / g.dnz));
+                produ = produ * (1.0 - fabs(((double)(l - 1) * g.dnx - drx) / g.dnx));
+                produ = produ * (1.0 - fabs(((double)(k - 1) * g.dnr - drr) / g.dnr));
+                if (ipz - 1 + m <= g.nnz + 1 && ipx - 1 + l <= g.nnx + 1 && ipr - 1 + k <= g.nnr + 1)
+                    vel = vel + veln_at(g, veln, ipz - 1 + m, ipx - 1 + l, ipr - 1 + k) * produ;
+            }
+    return vel;
+}
+
+template <typename R>
+__global__ void rays_kernel(RayArgs a)
+{
+    const Geom g = a.g;
+    const int total = a.nev * a.nrc;
+    const size_t NB = (size_t)g.nnx * g.nnz;
+    const size_t N = NB * g.nnr;
+    const size_t nmp = (size_t)(g.nvr + 2) * (g.nvx + 2) * (g.nvz + 2);
+    const int maxrp = 100000;        // F:7262
+    const double dpl = g.dnr;        // F:7290
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+        const int e = q / a.nrc, i = q - e * a.nrc;
+        const R *Te = (const R *)a.T + (size_t)e * N;
+        float *fdm = a.fdm ? a.fdm + nmp * (size_t)q : nullptr;
+        auto TD = [&](int iz, int ix, int ir) -> double {
+            return (double)Te[((size_t)(ir - 1) * g.nnx + (ix - 1)) * g.nnz + (iz - 1)];
+        };
+        int st = 0;
+        double rgr = a.rcr[i], rgx = a.rcx[i], rgz = a.rcz[i];
+        int ipr = (int)floor((g.rgor - rgr) / g.dnr) + 1;
+        int ipx = (int)floor((rgx - g.rgox) / g.dnx) + 1;
+        int ipz = (int)floor((rgz - g.rgoz) / g.dnz) + 1;
+        if (ipr == g.nnr) ipr--;   // F:7320-7333
+        if (ipx == g.nnx) ipx--;
+        if (ipz == g.nnz) ipz--;
+        int steps = 0;
+        if (!(ipr < 1 || ipr >= g.nnr || ipx < 1 || ipx >= g.nnx || ipz < 1 || ipz >= g.nnz)) {
+            for (int jstep = 1; jstep <= maxrp; ++jstep) {
+                ++steps;
+                double dtr = 0.0;
+                int temp = 0;
+                if (TD(ipz, ipx, ipr + 1) < TD(ipz, ipx, ipr)) { dtr = dtr + TD(ipz, ipx, ipr + 1) - TD(ipz, ipx, ipr); temp++; }
+                if (TD(ipz + 1, ipx, ipr + 1) < TD(ipz + 1, ipx, ipr)) { dtr = dtr + TD(ipz + 1, ipx, ipr + 1) - TD(ipz + 1, ipx, ipr); temp++; }
+                if (TD(ipz + 1, ipx + 1, ipr + 1) < TD(ipz + 1, ipx + 1, ipr)) { dtr = dtr + TD(ipz + 1, ipx + 1, ipr + 1) - TD(ipz + 1, ipx + 1, ipr); temp++; }
+                if (TD(ipz, ipx + 1, ipr + 1) < TD(ipz, ipx + 1, ipr)) { dtr = dtr + TD(ipz, ipx + 1, ipr + 1) - TD(ipz, ipx + 1, ipr); temp++; }
+                if (temp != 0) dtr = dtr / ((double)temp * g.dnr);
+                const double rcell = g.earth + g.rgor - (double)(ipr - 1) * g.dnr;
+                double dtx = TD(ipz, ipx + 1, ipr) - TD(ipz, ipx, ipr);
+                dtx = dtx + TD(ipz + 1, ipx + 1, ipr) - TD(ipz + 1, ipx, ipr);
+                dtx = dtx + TD(ipz + 1, ipx + 1, ipr + 1) - TD(ipz + 1, ipx, ipr + 1);
+                dtx = dtx + TD(ipz, ipx + 1, ipr + 1) - TD(ipz, ipx, ipr + 1);
+                dtx = dtx / (4.0 * rcell * g.dnx);
+                const double sx = sin(rgx);
+                double dtz = TD(ipz + 1, ipx, ipr) - TD(ipz, ipx, ipr);
+                dtz = dtz + TD(ipz + 1, ipx + 1, ipr + 1) - TD(ipz, ipx + 1, ipr + 1);
+                dtz = dtz + TD(ipz + 1, ipx + 1, ipr) - TD(ipz, ipx + 1, ipr);
+                dtz = dtz + TD(ipz + 1, ipx, ipr + 1) - TD(ipz, ipx, ipr + 1);
+                dtz = dtz / (4.0 * rcell * sx * g.dnz);
+                const double crad = g.earth + rgr;
+                const double rd1 = sqrt(dtr * dtr + dtx * dtx + dtz * dtz);
+                double nr = rgr + dpl * dtr / rd1;
+                double nx = rgx - dpl * dtx / (crad * rd1);
+                double nz = rgz - dpl * dtz / (crad * sx * rd1);
+                const int ipro = ipr, ipxo = ipx, ipzo = ipz;
+                ipr = (int)floor((g.rgor - nr) / g.dnr) + 1;
+                ipx = (int)floor((nx - g.rgox) / g.dnx) + 1;
+                ipz = (int)floor((nz - g.rgoz) / g.dnz) + 1;
+                const bool swr = (ipr < 1 || ipr >= g.nnr);
+                const bool swx = (ipx < 1 || ipx >= g.nnx);
+                const bool swz = (ipz < 1 || ipz >= g.nnz);
+                bool stop = false;
+                if (swr || swx || swz) {
+                    int sw = 0;
+                    double atio = 0.0;
+                    if (swr) {
+                        double ri;
+                        if (ipr < 1) { ri = g.rgor; ipr = 1; }
+                        else { ri = g.rgor - (double)(g.nnr - 1) * g.dnr; ipr = g.nnr - 1; }
+                        atio = (ri - rgr) / (nr - rgr);
+                        sw = 1;
+                    }
+                    if (swx) {
+                        double xi;
+                        if (ipx < 1) { xi = g.rgox; ipx = 1; }
+                        else { xi = g.rgox + (double)(g.nnx - 1) * g.dnx; ipx = g.nnx - 1; }
+                        const double r1 = (xi - rgx) / (nx - rgx);
+                        if (sw == 1) { if (r1 < atio) { atio = r1; sw = 2; } }
+                        else { atio = r1; sw = 2; }
+                    }
+                    if (swz) {
+                        double zi;
+                        if (ipz < 1) { zi = g.rgoz; ipz = 1; }
+                        else { zi = g.rgoz + (double)(g.nnz - 1) * g.dnz; ipz = g.nnz - 1; }
+                        const double r1 = (zi - rgz) / (nz - rgz);
+                        if (sw != 0) { if (r1 < atio) { atio = r1; sw = 3; } }
+                        else { atio = r1; sw = 3; }
+                    }
+                    if (sw == 1) { ipx = ipxo; ipz = ipzo; }
+                    else if (sw == 2) { ipr = ipro; ipz = ipzo; }
+                    else if (sw == 3) { ipr = ipro; ipx = ipxo; }
+                    nz = rgz + atio * (nz - rgz);
+                    nx = rgx + atio * (nx - rgx);
+                    nr = rgr + atio * (nr - rgr);
+                    stop = true;
+                }
+                if (fdm) {
+                    const int ivr = (int)floor((g.gor - nr) / g.dvr) + 1;
+                    const int ivx = (int)floor((nx - g.gox) / g.dvx) + 1;
+                    const int ivz = (int)floor((nz - g.goz) / g.dvz) + 1;
+                    const int ivro = (int)floor((g.gor - rgr) / g.dvr) + 1;
+                    const int ivxo = (int)floor((rgx - g.gox) / g.dvx) + 1;
+                    const int ivzo = (int)floor((rgz - g.goz) / g.dvz) + 1;
+                    double vrat[4];
+                    int chp[4];
+                    int nhp = 0;
+                    if (ivr != ivro) {
+                        const double ri = (ivr > ivro) ? g.gor - (double)(ivr - 1) * g.dvr : g.gor - (double)ivr * g.dvr;
+                        vrat[0] = (ri - rgr) / (nr - rgr);
+                        chp[0] = 1;
+                        nhp = 1;
+                    }
+                    if (ivx != ivxo) {
+                        const double xi = (ivx > ivxo) ? g.gox + (double)(ivx - 1) * g.dvx : g.gox + (double)ivx * g.dvx;
+                        const double r1 = (xi - rgx) / (nx - rgx);
+                        nhp++;
+                        if (nhp == 1) { vrat[0] = r1; chp[0] = 2; }
+                        else if (r1 >= vrat[0]) { vrat[1] = r1; chp[1] = 2; }
+                        else { vrat[1] = vrat[0]; chp[1] = chp[0]; vrat[0] = r1; chp[0] = 2; }
+                    }
+                    if (ivz != ivzo) {
+                        const double zi = (ivz > ivzo) ? g.goz + (double)(ivz - 1) * g.dvz : g.goz + (double)ivz * g.dvz;
+                        const double r1 = (zi - rgz) / (nz - rgz);
+                        nhp++;
+                        if (nhp == 1) { vrat[0] = r1; chp[0] = 3; }
+                        else if (nhp == 2) {
+                            if (r1 >= vrat[0]) { vrat[1] = r1; chp[1] = 3; }
+                            else { vrat[1] = vrat[0]; chp[1] = chp[0]; vrat[0] = r1; chp[0] = 3; }
+                        } else {
+                            if (r1 >= vrat[1]) { vrat[2] = r1; chp[2] = 3; }
+                            else if (r1 >= vrat[0]) { vrat[2] = vrat[1]; chp[2] = chp[1]; vrat[1] = r1; chp[1] = 3; }
+                            else { vrat[2] = vrat[1]; chp[2] = chp[1]; vrat[1] = vrat[0]; chp[1] = chp[0]; vrat[0] = r1; chp[0] = 3; }
+                        }
+                    }
+                    vrat[nhp] = 1.0;
+                    chp[nhp] = 0;
+                    nhp++;
+                    double drr = (g.rgor - rgr) - (double)(ipro - 1) * g.dnr;
+                    double drx = (rgx - g.rgox) - (double)(ipxo - 1) * g.dnx;
+                    double drz = (rgz - g.rgoz) - (double)(ipzo - 1) * g.dnz;
+                    double vel = trilin(g, a.veln, ipzo, ipxo, ipro, drr, drx, drz);
+                    double ui[4], vi[4], wi[4], uio[4], vio[4], wio[4];
+                    drr = (g.gor - rgr) - (double)(ivro - 1) * g.dvr;
+                    drx = (rgx - g.gox) - (double)(ivxo - 1) * g.dvx;
+                    drz = (rgz - g.goz) - (double)(ivzo - 1) * g.dvz;
+                    bspl(drr / g.dvr, ui);
+                    bspl(drx / g.dvx, vi);
+                    bspl(drz / g.dvz, wi);
+                    int ivrt = ivro, ivxt = ivxo, ivzt = ivzo;
+                    for (int k = 0; k < nhp; ++k) {
+                        const double velo = vel;
+                        for (int m = 0; m < 4; ++m) { uio[m] = ui[m]; vio[m] = vi[m]; wio[m] = wi[m]; }
+                        if (k > 0) {
+                            if (chp[k - 1] == 1) ivrt = ivr;
+                            else if (chp[k - 1] == 2) ivxt = ivx;
+                            else if (chp[k - 1] == 3) ivzt = ivz;
+                        }
+                        const double rigz = rgz + vrat[k] * (nz - rgz);
+                        const double rigx = rgx + vrat[k] * (nx - rgx);
+                        const double rigr = rgr + vrat[k] * (nr - rgr);
+                        const int iprt = (int)floor((g.rgor - rigr) / g.dnr) + 1;
+                        const int ipxt = (int)floor((rigx - g.rgox) / g.dnx) + 1;
+                        const int ipzt = (int)floor((rigz - g.rgoz) / g.dnz) + 1;
+                        drr = (g.rgor - rigr) - (double)(iprt - 1) * g.dnr;
+                        drx = (rigx - g.rgox) - (double)(ipxt - 1) * g.dnx;
+                        drz = (rigz - g.rgoz) - (double)(ipzt - 1) * g.dnz;
+                        vel = trilin(g, a.veln, ipzt, ipxt, iprt, drr, drx, drz);
+                        drr = (g.gor - rigr) - (double)(ivrt - 1) * g.dvr;
+                        drx = (rigx - g.gox) - (double)(ivxt - 1) * g.dvx;
+                        drz = (rigz - g.goz) - (double)(ivzt - 1) * g.dvz;
+                        bspl(drr / g.dvr, ui);
+                        bspl(drx / g.dvx, vi);
+                        bspl(drz / g.dvz, wi);
+                        const double dinc = (k == 0) ? vrat[k] * dpl : (vrat[k] - vrat[k - 1]) * dpl;
+                        if (ivzt - 1 < 0 || ivzt + 2 > g.nvz + 1 || ivxt - 1 < 0 || ivxt + 2 > g.nvx + 1 ||
+                            ivrt - 1 < 0 || ivrt + 2 > g.nvr + 1) {
+                            st = 1;
+                            continue;
+                        }
+                        for (int n = 0; n < 4; ++n)
+                            for (int m = 0; m < 4; ++m) {
+                                float *rowp = fdm + (size_t)(ivrt - 1 + n) +
+                                              (size_t)(g.nvr + 2) * ((size_t)(ivxt - 1 + m) + (size_t)(g.nvx + 2) * (size_t)(ivzt - 1));
+                                const size_t zstride = (size_t)(g.nvr + 2) * (size_t)(g.nvx + 2);
+                                for (int l = 0; l < 4; ++l) {
+                                    double a1 = ui[n] * vi[m] * wi[l] / (vel * vel);
+                                    const double a2 = uio[n] * vio[m] * wio[l] / (velo * velo);
+                                    a1 = -(a1 + a2) * dinc / 2.0;
+                                    float *p = rowp + zstride * (size_t)l;
+                                    *p = (float)(a1 + (double)*p);
+                                }
+                            }
+                    }
+                }
+                rgr = nr; rgx = nx; rgz = nz;
+                if (stop) break;
+            }
+        }
+        if (a.endpoints) {
+            a.endpoints[3 * (size_t)q] = rgr;
+            a.endpoints[3 * (size_t)q + 1] = rgx;
+            a.endpoints[3 * (size_t)q + 2] = rgz;
+        }
+        if (a.nsteps) a.nsteps[q] = steps;
+        if (a.status) a.status[q] = st;
+    }
+}
+
+// Rows: count and compact entries with |f| >= 1e-6 (F:7739-7765).  One block
+// per row; the block scans the row in column order.
+__global__ void row_counts_kernel(const float *__restrict__ fdm, int nrows, int nmp, int64_t *__restrict__ counts)
+{
+    const float ftol = 1.0e-6f;
+    for (int row = blockIdx.x; row < nrows; row += gridDim.x) {
+        const float *f = fdm + (size_t)row * nmp;
+        int c = 0;
+        for (int q = threadIdx.x; q < nmp; q += blockDim.x) c += fabsf(f[q]) >= ftol ? 1 : 0;
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        __shared__ int red[32];
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int s = 0;
+            for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) s += red[w];
+            counts[row] = s;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void row_compact_kernel(const float *__restrict__ fdm, int nrows, int nmp, const int64_t *__restrict__ row_ptr,
+                                   int32_t *__restrict__ cols, float *__restrict__ vals)
+{
+    const float ftol = 1.0e-6f;
+    __shared__ int wsum[32];
+    __shared__ int64_t s_base;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    for (int row = blockIdx.x; row < nrows; row += gridDim.x) {
+        const float *f = fdm + (size_t)row * nmp;
+        if (threadIdx.x == 0) s_base = row_ptr[row];
+        __syncthreads();
+        for (int c0 = 0; c0 < nmp; c0 += blockDim.x) {
+            const int q = c0 + threadIdx.x;
+            const float v = q < nmp ? f[q] : 0.0f;
+            const bool keep = q < nmp && fabsf(v) >= ftol;
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (lane == 0) wsum[wid] = __popc(m);
+            __syncthreads();
+            int before = 0, total = 0;
+            for (int w = 0; w < nw; ++w) {
+                if (w < wid) before += wsum[w];
+                total += wsum[w];
+            }
+            if (keep) {
+                const int64_t pos = s_base + before + __popc(m & ((1u << lane) - 1u));
+                cols[pos] = q + 1;
+                vals[pos] = v;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) s_base += total;
+            __syncthreads();
+        }
+    }
+}
+
+void launch_rays(const RayArgs &a, cudaStream_t st)
+{
+    const int total = a.nev * a.nrc;
+    const int block = 64;
+    const int blocks = (total + block - 1) / block;
+    if (blocks <= 0) return;
+    if (a.prec == FM3DT_FP64)
+        rays_kernel<double><<<blocks, block, 0, st>>>(a);
+    else
+        rays_kernel<float><<<blocks, block, 0, st>>>(a);
+}
+
+void launch_row_counts(const float *fdm, int nrows, int nmp, int64_t *counts, cudaStream_t st)
+{
+    if (nrows <= 0) return;
+    row_counts_kernel<<<nrows < 152 * 16 ? nrows : 152 * 16, 256, 0, st>>>(fdm, nrows, nmp, counts);
+}
+
+void launch_row_compact(const float *fdm, int nrows, int nmp, const int64_t *row_ptr, int32_t *cols, float *vals,
+                        cudaStream_t st)
+{
+    if (nrows <= 0) return;
+    row_compact_kernel<<<nrows < 152 * 16 ? nrows : 152 * 16, 256, 0, st>>>(fdm, nrows, nmp, row_ptr, cols, vals);
+}
+
+}  // namespace fm3dt

@@ -1,0 +1,287 @@
+"""Python binding of libfm3dt_gpu (the C ABI in include/fm3dt_gpu.h).
+
+This is the host-side mirror of the reference program's per-source pipeline
+(fm3dt_parallel.f90): grid header in, velocity nodes in, boundary frames (or
+synthetic plane waves) in, traveltime fields, receiver times, rays and
+Frechet rows out.  Every call goes through the CUDA library; there is no CPU
+fallback, and loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(_PKG_ROOT, "libfm3dt_gpu.so")
+
+FP64 = 0
+FP32_OFFSET = 1
+
+OK, EINVAL, ENOMEM, ECUDA, ENOCONV, ERANGE, ESTATE, ENODEV = 0, -1, -2, -3, -4, -5, -6, -7
+_ERRNAMES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ECUDA: "ECUDA", ENOCONV: "ENOCONV",
+             ERANGE: "ERANGE", ESTATE: "ESTATE", ENODEV: "ENODEV"}
+
+
+class Fm3dtError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{_ERRNAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class GridDesc(C.Structure):
+    _fields_ = [
+        ("nvr", C.c_int), ("nvx", C.c_int), ("nvz", C.c_int),
+        ("gor", C.c_double), ("goxd", C.c_double), ("gozd", C.c_double),
+        ("dvr", C.c_double), ("dvxd", C.c_double), ("dvzd", C.c_double),
+        ("nnr", C.c_int), ("nnx", C.c_int), ("nnz", C.c_int),
+        ("rgor", C.c_double), ("rgoxd", C.c_double), ("rgozd", C.c_double),
+        ("dnr", C.c_double), ("dnxd", C.c_double), ("dnzd", C.c_double),
+        ("earth", C.c_double),
+        ("fom", C.c_int), ("precision", C.c_int), ("max_events", C.c_int),
+    ]
+
+
+class Status(C.Structure):
+    _fields_ = [("rounds", C.c_int), ("converged", C.c_int), ("tile_updates", C.c_int64),
+                ("node_passes", C.c_int64), ("tile_nodes", C.c_int64), ("ms", C.c_double),
+                ("round_ms", C.c_double), ("round_launches", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+EXPORTS = [
+    "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_planewave",
+    "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
+    "fm3dt_set_tuning", "fm3dt_tile_shapes", "fm3dt_tile_shape", "fm3dt_launch_count",
+    "fm3dt_last_error", "fm3dt_ctx_destroy",
+]
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"libfm3dt_gpu.so not built ({p}); run __graft_entry__.build()")
+    L = C.CDLL(p)
+    dp = C.POINTER(C.c_double)
+    vp = C.c_void_p
+    L.fm3dt_ctx_create.argtypes = [C.POINTER(GridDesc), C.POINTER(vp)]
+    L.fm3dt_set_velocity.argtypes = [vp, dp]
+    L.fm3dt_solve.argtypes = [vp, C.c_int, dp, C.POINTER(Status)]
+    L.fm3dt_solve_planewave.argtypes = [vp, C.c_int, dp, C.POINTER(Status)]
+    L.fm3dt_solve_device.argtypes = [vp, C.c_int, C.c_void_p, C.POINTER(Status)]
+    L.fm3dt_receiver_times.argtypes = [vp, C.c_int, dp, dp, dp, C.POINTER(C.c_float)]
+    L.fm3dt_rays_frechet.argtypes = [vp, C.c_int, dp, dp, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_float), C.c_int64, dp]
+    L.fm3dt_get_times.argtypes = [vp, C.c_int, dp]
+    L.fm3dt_set_times.argtypes = [vp, C.c_int, C.c_int, dp]
+    L.fm3dt_get_velocity.argtypes = [vp, dp]
+    L.fm3dt_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    L.fm3dt_tile_shapes.argtypes = [C.POINTER(C.c_int)]
+    L.fm3dt_tile_shape.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.fm3dt_launch_count.argtypes = [vp]
+    L.fm3dt_launch_count.restype = C.c_int64
+    L.fm3dt_last_error.argtypes = [vp]
+    L.fm3dt_last_error.restype = C.c_char_p
+    L.fm3dt_ctx_destroy.argtypes = [vp]
+    L.fm3dt_ctx_destroy.restype = None
+    _lib = L
+    return L
+
+
+def ref_pi() -> float:
+    """The value of pi the reference uses (its double-precision pi is set from
+    a single-precision literal, fm3dt_parallel.f90:61)."""
+    return float(np.float32(3.1415926535898))
+
+
+def latlon_to_rad(lat, lon):
+    """Latitude/longitude in degrees -> colatitude/longitude in radians, as
+    fm3dt_parallel.f90:6313-6314 converts receivers and sources."""
+    pi = ref_pi()
+    lat = np.asarray(lat, dtype=np.float64)
+    lon = np.asarray(lon, dtype=np.float64)
+    return (90.0 - lat) * pi / 180.0, lon * pi / 180.0
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def tile_shapes():
+    L = load()
+    n = C.c_int(0)
+    L.fm3dt_tile_shapes(C.byref(n))
+    out = []
+    for i in range(n.value):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        L.fm3dt_tile_shape(i, C.byref(a), C.byref(b), C.byref(c))
+        out.append((a.value, b.value, c.value))
+    return out
+
+
+class Solver:
+    """One solver context: a grid, a velocity model and up to max_events
+    device-resident traveltime fields."""
+
+    def __init__(self, header, fom: int = 1, precision: int = FP64, max_events: int = 1):
+        self._L = load()
+        h = header
+        d = GridDesc()
+        d.nvr, d.nvx, d.nvz = h.nv
+        d.gor, d.goxd, d.gozd = h.vorig
+        d.dvr, d.dvxd, d.dvzd = h.vstep
+        d.nnr, d.nnx, d.nnz = h.nn
+        d.rgor, d.rgoxd, d.rgozd = h.norig
+        d.dnr, d.dnxd, d.dnzd = h.nstep
+        d.earth = h.earth
+        d.fom = int(fom)
+        d.precision = int(precision)
+        d.max_events = int(max_events)
+        self.desc = d
+        self.header = h
+        self.nn = tuple(h.nn)
+        self.nv = tuple(h.nv)
+        self.max_events = int(max_events)
+        self.nev = 0
+        ctx = C.c_void_p()
+        rc = self._L.fm3dt_ctx_create(C.byref(d), C.byref(ctx))
+        if rc != OK:
+            raise Fm3dtError(rc, self._L.fm3dt_last_error(None).decode())
+        self._ctx = ctx
+
+    def _check(self, rc):
+        if rc != OK:
+            raise Fm3dtError(rc, self._L.fm3dt_last_error(self._ctx).decode())
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._L.fm3dt_ctx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def nmp(self) -> int:
+        nvr, nvx, nvz = self.nv
+        return (nvr + 2) * (nvx + 2) * (nvz + 2)
+
+    @property
+    def launch_count(self) -> int:
+        return int(self._L.fm3dt_launch_count(self._ctx))
+
+    def set_tuning(self, shape: int = 0, max_passes: int = 0, max_rounds: int = 0):
+        self._check(self._L.fm3dt_set_tuning(self._ctx, int(shape), int(max_passes), int(max_rounds)))
+
+    def set_velocity(self, velv):
+        velv = np.ascontiguousarray(velv, dtype=np.float64)
+        if velv.size != self.nmp:
+            raise ValueError("velv has the wrong size")
+        self._check(self._L.fm3dt_set_velocity(self._ctx, _d(velv)))
+
+    def solve(self, frames) -> dict:
+        frames = np.ascontiguousarray(frames, dtype=np.float64)
+        nnr, nnx, nnz = self.nn
+        nev = frames.size // (nnx * nnz)
+        if frames.size != nev * nnx * nnz:
+            raise ValueError("frames must be nev x nnx x nnz")
+        st = Status()
+        self._check(self._L.fm3dt_solve(self._ctx, nev, _d(frames), C.byref(st)))
+        self.nev = nev
+        return st.as_dict()
+
+    def solve_ptr(self, nev: int, frames_ptr: int, device: bool) -> dict:
+        """Solve from frames at a raw address: host memory (e.g. pinned) when
+        device is False, device memory when True."""
+        st = Status()
+        if device:
+            self._check(self._L.fm3dt_solve_device(self._ctx, int(nev), C.c_void_p(frames_ptr), C.byref(st)))
+        else:
+            self._check(self._L.fm3dt_solve(self._ctx, int(nev),
+                                            C.cast(C.c_void_p(frames_ptr), C.POINTER(C.c_double)), C.byref(st)))
+        self.nev = int(nev)
+        return st.as_dict()
+
+    def receiver_times_into(self, rcr, rcx, rcz, out_ptr: int):
+        """Receiver times into caller-owned host memory at out_ptr (nev x nrc floats)."""
+        self._check(self._L.fm3dt_receiver_times(self._ctx, len(rcr), _d(rcr), _d(rcx), _d(rcz),
+                                                 C.cast(C.c_void_p(out_ptr), C.POINTER(C.c_float))))
+
+    def solve_planewave(self, params) -> dict:
+        params = np.ascontiguousarray(params, dtype=np.float64).reshape(-1, 4)
+        st = Status()
+        self._check(self._L.fm3dt_solve_planewave(self._ctx, len(params), _d(params), C.byref(st)))
+        self.nev = len(params)
+        return st.as_dict()
+
+    def receiver_times(self, rcr, rcx, rcz) -> np.ndarray:
+        rcr = np.ascontiguousarray(rcr, dtype=np.float64)
+        rcx = np.ascontiguousarray(rcx, dtype=np.float64)
+        rcz = np.ascontiguousarray(rcz, dtype=np.float64)
+        out = np.zeros((self.nev, len(rcr)), dtype=np.float32)
+        self._check(self._L.fm3dt_receiver_times(self._ctx, len(rcr), _d(rcr), _d(rcx), _d(rcz),
+                                                 out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def rays_frechet(self, rcr, rcx, rcz, frechet: bool = True, cap: int | None = None):
+        rcr = np.ascontiguousarray(rcr, dtype=np.float64)
+        rcx = np.ascontiguousarray(rcx, dtype=np.float64)
+        rcz = np.ascontiguousarray(rcz, dtype=np.float64)
+        nrows = self.nev * len(rcr)
+        row_ptr = np.zeros(nrows + 1, dtype=np.int64)
+        ends = np.zeros((nrows, 3), dtype=np.float64)
+        if not frechet:
+            self._check(self._L.fm3dt_rays_frechet(self._ctx, len(rcr), _d(rcr), _d(rcx), _d(rcz),
+                                                   row_ptr.ctypes.data_as(C.POINTER(C.c_int64)), None, None,
+                                                   0, _d(ends)))
+            return None, None, None, ends
+        if cap is None:
+            cap = max(1, nrows * 1024)
+        while True:
+            cols = np.zeros(cap, dtype=np.int32)
+            vals = np.zeros(cap, dtype=np.float32)
+            rc = self._L.fm3dt_rays_frechet(self._ctx, len(rcr), _d(rcr), _d(rcx), _d(rcz),
+                                            row_ptr.ctypes.data_as(C.POINTER(C.c_int64)),
+                                            cols.ctypes.data_as(C.POINTER(C.c_int32)),
+                                            vals.ctypes.data_as(C.POINTER(C.c_float)), cap, _d(ends))
+            if rc == ERANGE and row_ptr[-1] > cap:
+                cap = int(row_ptr[-1])
+                continue
+            self._check(rc)
+            n = int(row_ptr[-1])
+            return row_ptr, cols[:n], vals[:n], ends
+
+    def get_times(self, event: int = 0) -> np.ndarray:
+        nnr, nnx, nnz = self.nn
+        out = np.zeros(nnr * nnx * nnz, dtype=np.float64)
+        self._check(self._L.fm3dt_get_times(self._ctx, int(event), _d(out)))
+        return out
+
+    def get_velocity(self) -> np.ndarray:
+        nnr, nnx, nnz = self.nn
+        out = np.zeros((nnr + 3) * (nnx + 3) * (nnz + 3), dtype=np.float64)
+        self._check(self._L.fm3dt_get_velocity(self._ctx, _d(out)))
+        return out
+
+    def set_times(self, event: int, nev_total: int, ttn):
+        ttn = np.ascontiguousarray(ttn, dtype=np.float64)
+        self._check(self._L.fm3dt_set_times(self._ctx, int(event), int(nev_total), _d(ttn)))
+        self.nev = int(nev_total)

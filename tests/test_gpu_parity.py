@@ -1,0 +1,255 @@
+"""GPU parity tests: the CUDA path through the C ABI against the CPU oracle.
+
+Tolerances (stated per test):
+* gridder, plane-wave frames, receiver interpolation: bit-exact (same double
+  precision operation order, no FMA contraction in those kernels);
+* solver, first order: the iterative fixed point equals the fast-marching
+  result to 1e-9 s;
+* solver, mixed order: receiver times within 1e-5 relative and 1 ms absolute
+  (the spec bar); field within 5 ms everywhere and 1e-6 s at 99.9% of
+  nodes (fast marching keeps a few sticky intermediate minima on rough
+  models that the fixed point does not);
+* single-precision offset mode vs double: receiver times within 1e-5 relative
+  and 1 ms;
+* rays through an identical field: endpoints within 1e-9 rad / 1e-6 km and
+  Frechet rows within 1e-5 relative of the row norm.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(cfg, scale, nev=1, events=None):
+    from fm3dt import synth
+    w = synth.config(cfg, scale=scale, nev=nev)
+    if events is not None:
+        w.events = np.asarray(events, dtype=np.float64).reshape(-1, 2)
+    return w
+
+
+def _oracle_grid(orc, h):
+    return orc.grid_from_header(h.nv, h.vorig, h.vstep, h.nn, h.norig, h.nstep, h.earth)
+
+
+def _params(w):
+    from fm3dt import synth
+    return np.array([synth.planewave_params(w.header, *ev) for ev in w.events])
+
+
+def _oracle_solve(orc, w, params, fom=1):
+    g = _oracle_grid(orc, w.header)
+    veln, ncl = orc.gridder(g, w.velv)
+    assert ncl == 0
+    out = []
+    for p in params:
+        fr = orc.planewave_frame(g, orc.PlaneWave(*p))
+        ttn, _ = orc.fmm(g, veln, fr, fom)
+        out.append(ttn)
+    return g, veln, out
+
+
+@pytest.mark.parametrize("cfg,scale", [(0, 24), (3, 20), (2, 18)])
+def test_gridder_bitwise(gpu_lib, orc, cfg, scale):
+    import fm3dt
+    w = _setup(cfg, scale)
+    g = _oracle_grid(orc, w.header)
+    ref, _ = orc.gridder(g, w.velv)
+    with fm3dt.Solver(w.header) as s:
+        s.set_velocity(w.velv)
+        got = s.get_velocity()
+    assert np.array_equal(got, ref)
+
+
+def test_planewave_frame_bitwise(gpu_lib, orc):
+    import fm3dt
+    w = _setup(1, 20, nev=3)
+    params = _params(w)
+    g = _oracle_grid(orc, w.header)
+    nnr, nnx, nnz = w.header.nn
+    with fm3dt.Solver(w.header, max_events=3) as s:
+        s.set_velocity(w.velv)
+        s.solve_planewave(params)
+        for e in range(3):
+            t = s.get_times(e).reshape(nnr, nnx * nnz)
+            ref = orc.planewave_frame(g, orc.PlaneWave(*params[e]))
+            assert np.array_equal(t[-1], ref)
+
+
+@pytest.mark.parametrize("cfg,scale,event", [
+    (0, 24, (60.0, 45.0)), (0, 33, (60.0, 45.0)), (1, 28, (35.0, 200.0)),
+    (1, 30, (80.0, 300.0)), (2, 26, (50.0, 100.0)), (3, 24, (45.0, 270.0))])
+def test_solve_fp64_matches_fast_marching(gpu_lib, orc, cfg, scale, event):
+    import fm3dt
+    w = _setup(cfg, scale, events=[event])
+    params = _params(w)
+    g, veln, refs = _oracle_solve(orc, w, params)
+    rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat, w.rec_lon)
+    with fm3dt.Solver(w.header, fom=1, precision=fm3dt.FP64) as s:
+        s.set_velocity(w.velv)
+        st = s.solve_planewave(params)
+        assert st["converged"] == 1
+        got = s.get_times(0)
+        trr = s.receiver_times(w.rec_elev, rcx, rcz)[0].astype(np.float64)
+    d = np.abs(got - refs[0])
+    assert d.max() < 5e-3
+    assert np.quantile(d, 0.999) < 1e-6
+    ref_trr = orc.srtimes(g, refs[0], w.rec_elev, rcx, rcz).astype(np.float64)
+    assert np.max(np.abs(trr - ref_trr)) <= 1e-3
+    assert np.max(np.abs(trr - ref_trr) / ref_trr) <= 1e-5
+
+
+@pytest.mark.parametrize("cfg,scale", [(0, 22), (2, 20)])
+def test_solve_first_order_equals_fast_marching(gpu_lib, orc, cfg, scale):
+    import fm3dt
+    w = _setup(cfg, scale)
+    params = _params(w)
+    _, _, refs = _oracle_solve(orc, w, params, fom=0)
+    with fm3dt.Solver(w.header, fom=0) as s:
+        s.set_velocity(w.velv)
+        s.solve_planewave(params)
+        got = s.get_times(0)
+    assert np.max(np.abs(got - refs[0])) < 1e-9
+
+
+def test_host_frames_equal_planewave(gpu_lib, orc):
+    import fm3dt
+    w = _setup(1, 20, nev=2)
+    params = _params(w)
+    g = _oracle_grid(orc, w.header)
+    frames = np.stack([orc.planewave_frame(g, orc.PlaneWave(*p)) for p in params])
+    with fm3dt.Solver(w.header, max_events=2) as s:
+        s.set_velocity(w.velv)
+        s.solve_planewave(params)
+        a = [s.get_times(e) for e in range(2)]
+        s.solve(frames)
+        b = [s.get_times(e) for e in range(2)]
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_unset_boundary_values(gpu_lib, orc):
+    """Boundary values <= 0 mean "no time" (F:6935-6936): those bottom nodes
+    are solved like any other node."""
+    import fm3dt
+    w = _setup(0, 22)
+    params = _params(w)
+    g, veln, _ = _oracle_solve(orc, w, params[:0])
+    fr = orc.planewave_frame(g, orc.PlaneWave(*params[0]))
+    rng = np.random.default_rng(5)
+    fr[rng.uniform(size=fr.size) < 0.2] = 0.0
+    fr[:5] = -1.0
+    ref, _ = orc.fmm(g, veln, fr, 1)
+    with fm3dt.Solver(w.header) as s:
+        s.set_velocity(w.velv)
+        s.solve(fr[None, :])
+        got = s.get_times(0)
+    assert np.max(np.abs(got - ref)) < 5e-3
+    assert np.quantile(np.abs(got - ref), 0.999) < 1e-6
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_batch_equals_alone_bitwise(gpu_lib, prec):
+    """Each event's field is identical solved alone and solved in a batch."""
+    import fm3dt
+    w = _setup(1, 26, nev=5)
+    params = _params(w)
+    with fm3dt.Solver(w.header, precision=prec, max_events=5) as s:
+        s.set_velocity(w.velv)
+        s.solve_planewave(params)
+        batch = [s.get_times(e) for e in range(5)]
+        for e in range(5):
+            s.solve_planewave(params[e:e + 1])
+            assert np.array_equal(s.get_times(0), batch[e])
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_tile_shapes_bitwise(gpu_lib, prec):
+    """The fixed point does not depend on the tile shape or schedule."""
+    import fm3dt
+    w = _setup(2, 30, nev=2)
+    params = _params(w)
+    ref = None
+    with fm3dt.Solver(w.header, precision=prec, max_events=2) as s:
+        s.set_velocity(w.velv)
+        for shape in range(len(fm3dt.tile_shapes())):
+            s.set_tuning(shape)
+            st = s.solve_planewave(params)
+            assert st["converged"] == 1
+            out = np.concatenate([s.get_times(e) for e in range(2)])
+            if ref is None:
+                ref = out
+            else:
+                assert np.array_equal(out, ref), f"shape {shape}"
+
+
+def test_fp32_offset_within_tolerance(gpu_lib):
+    import fm3dt
+    w = _setup(1, 40, nev=4)
+    params = _params(w)
+    rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat, w.rec_lon)
+    with fm3dt.Solver(w.header, precision=fm3dt.FP64, max_events=4) as s:
+        s.set_velocity(w.velv)
+        s.solve_planewave(params)
+        t64 = s.receiver_times(w.rec_elev, rcx, rcz).astype(np.float64)
+    with fm3dt.Solver(w.header, precision=fm3dt.FP32_OFFSET, max_events=4) as s:
+        s.set_velocity(w.velv)
+        s.solve_planewave(params)
+        t32 = s.receiver_times(w.rec_elev, rcx, rcz).astype(np.float64)
+    assert np.max(np.abs(t32 - t64)) <= 1e-3
+    assert np.max(np.abs(t32 - t64) / t64) <= 1e-5
+
+
+def test_receiver_times_bitwise_on_same_field(gpu_lib, orc):
+    import fm3dt
+    w = _setup(3, 22)
+    params = _params(w)
+    g, veln, refs = _oracle_solve(orc, w, params)
+    rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat, w.rec_lon)
+    ref = orc.srtimes(g, refs[0], w.rec_elev, rcx, rcz)
+    with fm3dt.Solver(w.header) as s:
+        s.set_velocity(w.velv)
+        s.set_times(0, 1, refs[0])
+        got = s.receiver_times(w.rec_elev, rcx, rcz)[0]
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("cfg,scale", [(0, 24), (2, 22)])
+def test_rays_frechet_on_same_field(gpu_lib, orc, cfg, scale):
+    import fm3dt
+    w = _setup(cfg, scale)
+    params = _params(w)
+    g, veln, refs = _oracle_solve(orc, w, params)
+    rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat, w.rec_lon)
+    fdm, ends, steps = orc.rays(g, refs[0], veln, w.rec_elev, rcx, rcz)
+    with fm3dt.Solver(w.header) as s:
+        s.set_velocity(w.velv)
+        s.set_times(0, 1, refs[0])
+        row_ptr, cols, vals, gends = s.rays_frechet(w.rec_elev, rcx, rcz)
+    assert np.max(np.abs(gends[:, 0] - ends[:, 0])) < 1e-6
+    assert np.max(np.abs(gends[:, 1:] - ends[:, 1:])) < 1e-9
+    nmp = orc.nmp(g)
+    for i in range(len(rcx)):
+        dense = np.zeros(nmp, dtype=np.float64)
+        c = cols[row_ptr[i]:row_ptr[i + 1]]
+        assert np.all(np.diff(c) > 0)
+        dense[c - 1] = vals[row_ptr[i]:row_ptr[i + 1]]
+        refrow = fdm[i].astype(np.float64)
+        refrow[np.abs(fdm[i]) < np.float32(1e-6)] = 0.0
+        scale_ = max(np.max(np.abs(refrow)), 1e-30)
+        assert np.max(np.abs(dense - refrow)) <= 1e-5 * scale_
+
+
+def test_errors_are_reported(gpu_lib):
+    import fm3dt
+    w = _setup(0, 16)
+    with fm3dt.Solver(w.header) as s:
+        with pytest.raises(fm3dt.Fm3dtError) as ei:
+            s.solve_planewave(_params(w))
+        assert ei.value.code == fm3dt.ESTATE
+        s.set_velocity(w.velv)
+        s.solve_planewave(_params(w))
+        with pytest.raises(fm3dt.Fm3dtError) as ei:
+            s.receiver_times(np.array([0.0]), np.array([0.1]), np.array([0.1]))
+        assert ei.value.code == fm3dt.ERANGE
+        assert s.launch_count > 0

@@ -1,0 +1,186 @@
+"""Known-answer tests pinning the CPU oracle (no GPU).
+
+The reference ships no tests or golden vectors and cannot be built here, so
+the oracle's restatement of fm3dt_parallel.f90 is pinned by analytic cases:
+* a homogeneous medium with a uniform bottom frame (vertical plane wave):
+  t = t_bottom + s * (height - bottom height) exactly, both schemes;
+* a 1-D linear velocity gradient, vertical plane wave: t = t_b + ln(v_b/v)/g,
+  to the discretisation error of each scheme;
+* straight vertical rays in a homogeneous medium: endpoint below the
+  receiver, Frechet row summing to -(integrated length)/v^2 (cubic B-splines
+  are a partition of unity);
+* trilinear receiver interpolation of a linear field is exact;
+plus the reference's literal conventions (single-precision pi, sparsity
+threshold, FP32 accumulation).
+"""
+import math
+
+import numpy as np
+import pytest
+
+
+def _header(n=20, nv=(8, 9, 9)):
+    from fm3dt import synth
+    return synth.section_header(n, n + 2, n + 1, *nv)
+
+
+def _grid(orc, h):
+    return orc.grid_from_header(h.nv, h.vorig, h.vstep, h.nn, h.norig, h.nstep, h.earth)
+
+
+def test_reference_pi(orc):
+    assert orc.ref_pi() == float(np.float32(3.1415926535898))
+    assert orc.ref_pi() != math.pi
+
+
+def test_header_conversion(orc):
+    h = _header()
+    g = _grid(orc, h)
+    pi = orc.ref_pi()
+    assert g.rgox == (90.0 - h.norig[1]) * pi / 180.0
+    assert g.dnz == h.nstep[2] * pi / 180.0
+    assert g.nnr == h.nn[0] and g.nvz == h.nv[2]
+
+
+@pytest.mark.parametrize("fom", [0, 1])
+def test_homogeneous_vertical_plane_wave(orc, fom):
+    from fm3dt import synth
+    h = _header(18)
+    g = _grid(orc, h)
+    v = 7.0
+    velv = np.full((h.nv[2] + 2) * (h.nv[1] + 2) * (h.nv[0] + 2), v)
+    veln, ncl = orc.gridder(g, velv)
+    assert ncl == 0
+    assert np.allclose(veln, v, rtol=1e-14)
+    tb = 500.0
+    frame = np.full(g.nnx * g.nnz, tb)
+    ttn, pops = orc.fmm(g, veln, frame, fom)
+    t = ttn.reshape(g.nnr, g.nnx, g.nnz)
+    depth_steps = (g.nnr - 1 - np.arange(g.nnr)) * g.dnr
+    expect = tb + depth_steps / v
+    assert np.max(np.abs(t - expect[:, None, None])) < 1e-9
+    assert pops == g.nnx * g.nnz * (g.nnr - 1) + 1
+
+
+def _gradient_error(orc, n, fom):
+    h = _header(n)
+    g = _grid(orc, h)
+    nvr, nvx, nvz = h.nv
+    heights = h.vorig[0] - (np.arange(nvr + 2) - 1.0) * h.vstep[0]
+    v0, grad = 5.0, 0.01      # v = v0 + grad * depth (B-splines reproduce it exactly)
+    vcol = v0 + grad * (-heights)
+    velv = np.broadcast_to(vcol[None, None, :], (nvz + 2, nvx + 2, nvr + 2)).reshape(-1).copy()
+    veln, _ = orc.gridder(g, velv)
+    tb = 400.0
+    ttn, _ = orc.fmm(g, veln, np.full(g.nnx * g.nnz, tb), fom)
+    t = ttn.reshape(g.nnr, g.nnx, g.nnz)[:, g.nnx // 2, g.nnz // 2]
+    depth = -(g.rgor - np.arange(g.nnr) * g.dnr)
+    vb = v0 + grad * depth[-1]
+    expect = tb + np.log(vb / (v0 + grad * depth)) / grad
+    return np.max(np.abs(t - expect))
+
+
+@pytest.mark.parametrize("fom,order", [(0, 1), (1, 2)])
+def test_linear_gradient_vertical_plane_wave(orc, fom, order):
+    """t = t_b + ln(v_b/v)/g; the first-order scheme converges as h, the
+    mixed-order scheme as h^2 (error ratio 2 resp. 4 per halving of h)."""
+    e1 = _gradient_error(orc, 21, fom)
+    e2 = _gradient_error(orc, 41, fom)
+    ratio = e1 / e2
+    assert 0.85 * 2 ** order < ratio < 1.15 * 2 ** order, (e1, e2)
+    assert e2 < (0.5 if fom == 0 else 0.03)
+
+
+def test_straight_vertical_rays(orc):
+    import fm3dt
+    h = _header(21)
+    g = _grid(orc, h)
+    v = 6.5
+    velv = np.full((h.nv[2] + 2) * (h.nv[1] + 2) * (h.nv[0] + 2), v)
+    veln, _ = orc.gridder(g, velv)
+    ttn, _ = orc.fmm(g, veln, np.full(g.nnx * g.nnz, 300.0), 1)
+    rng = np.random.default_rng(3)
+    lat = rng.uniform(h.norig[1] - 8 * h.nstep[1], h.norig[1] - 2 * h.nstep[1], 6)
+    lon = rng.uniform(h.norig[2] + 2 * h.nstep[2], h.norig[2] + 8 * h.nstep[2], 6)
+    rcx, rcz = orc.latlon_to_rad(lat, lon)
+    rcr = np.zeros(6)
+    fdm, ends, steps = orc.rays(g, ttn, veln, rcr, rcx, rcz)
+    bottom = g.rgor - (g.nnr - 1) * g.dnr
+    assert np.allclose(ends[:, 0], bottom, atol=1e-9)
+    assert np.allclose(ends[:, 1], rcx, atol=1e-12)
+    assert np.allclose(ends[:, 2], rcz, atol=1e-12)
+    depth = g.rgor - bottom
+    for i in range(6):
+        s = float(np.sum(fdm[i].astype(np.float64)))
+        # the clipped last step is integrated with the full nominal length
+        cands = [-(steps[i] * g.dnr) / v ** 2]
+        assert steps[i] in (g.nnr - 1, g.nnr)
+        assert abs(s - cands[0]) < 1e-4 * abs(cands[0])
+        assert steps[i] * g.dnr >= depth - 1e-9
+
+
+def test_receiver_interpolation_linear_field(orc):
+    h = _header(16)
+    g = _grid(orc, h)
+    ir, ix, iz = np.meshgrid(np.arange(g.nnr), np.arange(g.nnx), np.arange(g.nnz), indexing="ij")
+    ttn = (100.0 + 2.0 * ir + 0.5 * ix + 0.25 * iz).reshape(-1).astype(np.float64)
+    rng = np.random.default_rng(0)
+    lat = rng.uniform(h.norig[1] - 10 * h.nstep[1], h.norig[1] - 1 * h.nstep[1], 20)
+    lon = rng.uniform(h.norig[2] + 1 * h.nstep[2], h.norig[2] + 10 * h.nstep[2], 20)
+    rcx, rcz = orc.latlon_to_rad(lat, lon)
+    rcr = -rng.uniform(0, 5 * g.dnr, 20)
+    out = orc.srtimes(g, ttn, rcr, rcx, rcz)
+    fr = (g.rgor - rcr) / g.dnr
+    fx = (rcx - g.rgox) / g.dnx
+    fz = (rcz - g.rgoz) / g.dnz
+    expect = 100.0 + 2.0 * fr + 0.5 * fx + 0.25 * fz
+    assert out.dtype == np.float32
+    assert np.max(np.abs(out - expect)) < 1e-4
+
+
+def test_receiver_outside_is_an_error(orc):
+    h = _header(12)
+    g = _grid(orc, h)
+    ttn = np.ones(g.nnr * g.nnx * g.nnz)
+    with pytest.raises(RuntimeError):
+        orc.srtimes(g, ttn, np.array([0.0]), np.array([0.0]), np.array([0.0]))
+
+
+def test_sparsify_threshold(orc):
+    row = np.array([0.0, 1e-6, -1e-6, 9.9e-7, 2.0, -3e-7], dtype=np.float32)
+    cols, vals = orc.sparsify(row)
+    # |f| >= 1e-6 in single precision, 1-based columns (F:7739-7765)
+    assert cols.tolist() == [2, 3, 5]
+    assert vals.tolist() == [row[1], row[2], row[4]]
+
+
+def test_planewave_frame_formula(orc):
+    from fm3dt import synth
+    h = _header(14)
+    g = _grid(orc, h)
+    for delta, baz in [(30.0, 0.0), (60.0, 45.0), (90.0, 250.0)]:
+        p = synth.planewave_params(h, delta, baz)
+        pw = orc.planewave_params(g, delta, baz)
+        assert np.allclose([pw.t0, pw.p, pw.cos_az, pw.sin_az], p, rtol=1e-15, atol=1e-15)
+        fr = orc.planewave_frame(g, orc.PlaneWave(*p))
+        ref = synth.planewave_frames(h, [p])[0]
+        assert np.max(np.abs(fr - ref)) < 1e-9
+        assert fr.min() > 0
+
+
+def test_fmm_single_seed_and_unset_values(orc):
+    """Only the earliest positive boundary node seeds the heap; values <= 0
+    stay unset until the march reaches them (F:6926-6960)."""
+    from fm3dt import synth
+    w = synth.config(0, scale=14)
+    h = w.header
+    g = _grid(orc, h)
+    veln, _ = orc.gridder(g, w.velv)
+    frame = np.full(g.nnx * g.nnz, -1.0)
+    frame[g.nnz * (g.nnx // 2) + g.nnz // 2] = 50.0     # one source node
+    ttn, pops = orc.fmm(g, veln, frame, 1)
+    t = ttn.reshape(g.nnr, g.nnx * g.nnz)
+    assert t[-1].min() == 50.0 and np.all(ttn > 0)
+    assert pops == g.nnr * g.nnx * g.nnz
+    # times grow away from the point source
+    assert t[-1].argmin() == g.nnz * (g.nnx // 2) + g.nnz // 2
