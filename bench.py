@@ -152,10 +152,10 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-# Per-launch DRAM traffic of the tile-round kernel from one ncu capture,
-# scaled to the bench workload (profiles/round_kernel_config1.md).  None
-# until a capture exists.
-ROUND_KERNEL_TRAFFIC_BYTES = None
+# Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of
+# each solver kernel from one ncu capture, scaled to the bench workload; see
+# the summaries under profiles/.  Absent until a capture exists.
+KERNEL_TRAFFIC_BYTES = {}
 
 
 def _oracle_event(args):
@@ -285,14 +285,25 @@ def run_ours(a):
     lat = sorted(s["ms"] for s in sts)
     p50 = lat[len(lat) // 2]
     p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
+    # the two solver kernels: rounds (tile activations) and the directional
+    # sweep (every node staged once); the roofline line reports the one with
+    # the larger share of device time
     round_ms = sum(s["round_ms"] for s in sts)
     round_launches = sum(s["round_launches"] for s in sts)
     staged = sum(s["tile_nodes"] for s in sts)
-    alg_bytes = staged * B_NODE[a.prec]
-    achieved = alg_bytes / (round_ms / 1000.0) / 1e9 if round_ms > 0 else 0.0
+    sweep_ms = sum(s["sweep_ms"] for s in sts)
+    sweep_launches = sum(s["sweep_launches"] for s in sts)
+    sweep_nodes = sum(s["sweep_nodes"] for s in sts)
+    kernels = {
+        "round_kernel": (round_ms, round_launches, staged * B_NODE[a.prec]),
+        "sweep_kernel": (sweep_ms, sweep_launches, sweep_nodes * B_NODE[a.prec]),
+    }
+    top = max(kernels, key=lambda k: kernels[k][0])
+    k_ms, k_launches, alg_bytes = kernels[top]
+    achieved = alg_bytes / (k_ms / 1000.0) / 1e9 if k_ms > 0 else 0.0
     peak, peak_kind = measured_peak_hbm()
-    per_launch = alg_bytes / max(1, round_launches)
-    traffic = ROUND_KERNEL_TRAFFIC_BYTES
+    per_launch = alg_bytes / max(1, k_launches)
+    traffic = KERNEL_TRAFFIC_BYTES.get(top)
 
     extras = {}
     if not a.no_extras:
@@ -345,12 +356,16 @@ def run_ours(a):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "round_kernel", "peak_source": peak_kind,
+                     "kernel": top, "peak_source": peak_kind,
                      "alg_bytes_per_launch": per_launch,
-                     "avg_launch_ms": round_ms / max(1, round_launches)},
-        "solver": {"rounds_per_solve": round_launches / a.steps, "tile_activations": sum(s["tile_updates"] for s in sts) / a.steps,
+                     "avg_launch_ms": k_ms / max(1, k_launches)},
+        "solver": {"rounds_per_solve": round_launches / a.steps,
+                   "tile_activations": sum(s["tile_updates"] for s in sts) / a.steps,
                    "node_passes_per_solve": sum(s["node_passes"] for s in sts) / a.steps,
-                   "staged_nodes_per_solve": staged / a.steps, "device_ms_per_step": dev_ms / a.steps},
+                   "staged_nodes_per_solve": staged / a.steps, "device_ms_per_step": dev_ms / a.steps,
+                   "round_ms_per_step": round_ms / a.steps, "sweep_ms_per_step": sweep_ms / a.steps,
+                   "sweep_launches_per_step": sweep_launches / a.steps,
+                   "kernel_shares": {k: v[0] / max(1e-9, dev_ms) for k, v in kernels.items()}},
     }
     line.update(extras)
     if clk:

@@ -73,6 +73,9 @@ typedef struct {
     double ms;                /* device time of the whole solve */
     double round_ms;          /* device time inside the tile-round kernels */
     int round_launches;       /* tile-round kernel launches */
+    int sweep_launches;       /* directional-sweep kernel launches */
+    double sweep_ms;          /* device time of the directional sweep */
+    int64_t sweep_nodes;      /* grid nodes staged by the sweep */
 } fm3dt_status;
 
 typedef struct fm3dt_ctx fm3dt_ctx;
@@ -96,6 +99,12 @@ int fm3dt_solve(fm3dt_ctx *ctx, int nev, const double *boundary, fm3dt_status *s
  * (d_boundary is a device pointer, e.g. frames kept resident between
  * tomography iterations). */
 int fm3dt_solve_device(fm3dt_ctx *ctx, int nev, const double *d_boundary, fm3dt_status *st);
+
+/* Continues the fast-iterative rounds from the current fields of the last
+ * solved (or uploaded) events, every tile active, until no node changes.
+ * On a converged solve it changes nothing (a fixed-point check); after
+ * fm3dt_set_times with a field of a nearby model it is a warm start. */
+int fm3dt_solve_resume(fm3dt_ctx *ctx, fm3dt_status *st);
 
 /* Same solve with the boundary frames generated on the device from a
  * synthetic teleseismic plane wave per event: params is nev x 4 doubles
@@ -141,9 +150,10 @@ int fm3dt_get_velocity(fm3dt_ctx *ctx, double *veln);
  * fastest), e.g. to trace rays through a field computed elsewhere. */
 int fm3dt_set_times(fm3dt_ctx *ctx, int event, int nev_total, const double *ttn);
 
-/* Solver tuning: tile shape index, in-tile pass cap and round cap
- * (0 keeps the current value). */
-int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rounds);
+/* Solver tuning: tile shape index, in-tile pass cap and round cap (0 keeps
+ * the current value), directional sweep before the rounds (1 on, 0 off,
+ * -1 keep).  None of these changes the converged field. */
+int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rounds, int sweep);
 
 /* Number of available tile shapes and the shape (TR, TX, TZ) of one. */
 int fm3dt_tile_shapes(int *count);

@@ -60,6 +60,7 @@ def lib():
                                            C.c_double, C.POINTER(Grid)]
         L.orc_gridder.argtypes = [C.POINTER(Grid), dp, dp, C.POINTER(C.c_int)]
         L.orc_fmm.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.POINTER(C.c_longlong)]
+        L.orc_fixed_point.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.c_int, C.POINTER(C.c_int)]
         L.orc_srtimes.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, dp, C.POINTER(C.c_float)]
         L.orc_rays.argtypes = [C.POINTER(Grid), dp, dp, C.c_int, dp, dp, dp, C.POINTER(C.c_float),
                                dp, C.POINTER(C.c_int)]
@@ -122,6 +123,19 @@ def fmm(g: Grid, veln: np.ndarray, bottom: np.ndarray, fom: int = 1):
     if rc != 0:
         raise RuntimeError(f"orc_fmm failed: {rc}")
     return ttn, pops.value
+
+
+def fixed_point(g: Grid, veln: np.ndarray, bottom: np.ndarray, fom: int = 1, max_sweeps: int = 10000):
+    """Fixed point of the reference's stencil (order independent)."""
+    veln = np.ascontiguousarray(veln, dtype=np.float64)
+    bottom = np.ascontiguousarray(bottom, dtype=np.float64)
+    ttn = np.zeros(g.nnr * g.nnx * g.nnz, dtype=np.float64)
+    sweeps = C.c_int(0)
+    rc = lib().orc_fixed_point(C.byref(g), _d(veln), int(fom), _d(bottom), _d(ttn), int(max_sweeps),
+                               C.byref(sweeps))
+    if rc != 0:
+        raise RuntimeError(f"orc_fixed_point failed: {rc}")
+    return ttn, sweeps.value
 
 
 def srtimes(g: Grid, ttn: np.ndarray, rcr, rcx, rcz):

@@ -248,11 +248,251 @@ static int sw2(const fmm_state *s, int nb_alive, int nb2_in, int nb2_alive, doub
     return sw;
 }
 
+/* One octant of fouds2_all (F:710-993): the reference's branch table for
+ * the given upwind flags (ai/aj/ak: neighbour used; swi/swj/swk == 0: that
+ * axis second order).  Returns 1 and the octant time in *trav when some
+ * axis is used. */
+static int octant2(const fmm_state *s, int iz, int ix, int ir, int i, int j, int k, int i2, int j2, int k2,
+                   int ai, int aj, int ak, int swi, int swj, int swk, double ri, double risti, double slown,
+                   double *trav)
+{
+    const orc_grid *g = s->g;
+    const double dnr = g->dnr, dnx = g->dnx, dnz = g->dnz;
+        int swsol = 0;
+        double a = 0, b = 0, c = 0, u, v, w, em, en, tref = 0, tdiv = 1.0;
+        /* neighbour values; second neighbours are only read on the
+         * branches whose switch proved them in range */
+#define TIv TT(s, iz, ix, i)
+#define TI2 TT(s, iz, ix, i2)
+#define TJv TT(s, iz, j, ir)
+#define TJ2 TT(s, iz, j2, ir)
+#define TKv TT(s, k, ix, ir)
+#define TK2 TT(s, k2, ix, ir)
+        if (swi == 0) {
+            swsol = 1;
+            if (swj == 0) {
+                if (swk == 0) {
+                    u = 2.0 * dnr; v = 2.0 * ri * dnx; w = 2.0 * risti * dnz;
+                    em = 4.0 * TIv - TI2 - 4.0 * TJv; em = em + TJ2;
+                    en = 4.0 * TIv - TI2 - 4.0 * TKv; en = en + TK2;
+                    a = sq(v) * sq(w) + sq(u) * sq(w) + sq(u) * sq(v);
+                    b = 2.0 * sq(u) * (em * sq(w) + en * sq(v));
+                    c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(v) * sq(w) * sq(slown));
+                    tref = 4.0 * TIv - TI2; tdiv = 3.0;
+                } else if (ak) {
+                    u = risti * dnz; v = 2.0 * ri * dnx; w = 2.0 * dnr;
+                    em = 3.0 * TKv - 4.0 * TJv + TJ2;
+                    en = 3.0 * TKv - 4.0 * TIv + TI2;
+                    a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
+                    b = 6.0 * sq(u) * (em * sq(w) + en * sq(v));
+                    c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
+                    tref = TKv; tdiv = 1.0;
+                } else {
+                    u = 2.0 * dnr; v = 2.0 * ri * dnx;
+                    em = 4.0 * TIv - TI2 - 4.0 * TJv; em = em + TJ2;
+                    a = sq(v) + sq(u);
+                    b = 2.0 * em * sq(u);
+                    c = sq(u) * (sq(em) - sq(slown) * sq(v));
+                    tref = 4.0 * TIv - TI2; tdiv = 3.0;
+                }
+            } else if (aj) {
+                if (swk == 0) {
+                    u = ri * dnx; v = 2.0 * dnr; w = 2.0 * risti * dnz;
+                    em = 3.0 * TJv - 4.0 * TIv + TI2;
+                    en = 3.0 * TJv - 4.0 * TKv + TK2;
+                    a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
+                    b = 6.0 * sq(u) * (em * sq(w) + en * sq(v));
+                    c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
+                    tref = TJv; tdiv = 1.0;
+                } else if (ak) {
+                    u = ri * dnx; v = 2.0 * dnr; w = risti * dnz;
+                    em = 3.0 * TJv - 4.0 * TIv + TI2;
+                    en = TJv - TKv;
+                    a = sq(w) * sq(v) + 9.0 * sq(u) * sq(w) + sq(u) * sq(v);
+                    b = sq(u) * (6.0 * em * sq(w) + 2.0 * en * sq(v));
+                    c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
+                    tref = TJv; tdiv = 1.0;
+                } else {
+                    u = ri * dnx; v = 2.0 * dnr;
+                    em = 3.0 * TJv - 4.0 * TIv + TI2;
+                    a = sq(v) + 9.0 * sq(u);
+                    b = 6.0 * em * sq(u);
+                    c = sq(u) * (sq(em) - sq(slown) * sq(v));
+                    tref = TJv; tdiv = 1.0;
+                }
+            } else {
+                if (swk == 0) {
+                    u = 2.0 * dnr; v = 2.0 * risti * dnz;
+                    em = 4.0 * TIv - TI2 - 4.0 * TKv; em = em + TK2;
+                    a = sq(u) + sq(v);
+                    b = 2.0 * em * sq(u);
+                    c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                    tref = 4.0 * TIv - TI2; tdiv = 3.0;
+                } else if (ak) {
+                    u = risti * dnz; v = 2.0 * dnr;
+                    em = 3.0 * TKv - 4.0 * TIv + TI2;
+                    a = sq(v) + 9.0 * sq(u);
+                    b = 6.0 * em * sq(u);
+                    c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                    tref = TKv; tdiv = 1.0;
+                } else {
+                    u = 2.0 * dnr;
+                    a = 1.0; b = 0.0;
+                    c = -sq(u) * sq(slown);
+                    tref = 4.0 * TIv - TI2; tdiv = 3.0;
+                }
+            }
+        } else if (ai) {
+            swsol = 1;
+            if (swj == 0) {
+                if (swk == 0) {
+                    u = dnr; v = 2.0 * ri * dnx; w = 2.0 * risti * dnz;
+                    em = 3.0 * TIv - 4.0 * TJv + TJ2;
+                    en = 3.0 * TIv - 4.0 * TKv + TK2;
+                    a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
+                    b = 6.0 * sq(u) * (em * sq(w) + en * sq(v));
+                    c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
+                    tref = TIv; tdiv = 1.0;
+                } else if (ak) {
+                    u = dnr; v = 2.0 * ri * dnx; w = risti * dnz;
+                    em = 3.0 * TIv - 4.0 * TJv + TJ2;
+                    en = TIv - TKv;
+                    a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + sq(u) * sq(v);
+                    b = sq(u) * (6.0 * em * sq(w) + 2.0 * en * sq(v));
+                    c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(v) * sq(w) * sq(slown));
+                    tref = TIv; tdiv = 1.0;
+                } else {
+                    u = dnr; v = 2.0 * ri * dnx;
+                    em = 3.0 * TIv - 4.0 * TJv + TJ2;
+                    a = sq(v) + 9.0 * sq(u);
+                    b = 6.0 * em * sq(u);
+                    c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                    tref = TIv; tdiv = 1.0;
+                }
+            } else if (aj) {
+                if (swk == 0) {
+                    u = dnr; v = ri * dnx; w = 2.0 * risti * dnz;
+                    em = TIv - TJv;
+                    en = 3.0 * TIv - 4.0 * TKv + TK2;
+                    a = sq(v) * sq(w) + sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
+                    b = sq(u) * (2.0 * em * sq(w) + 6.0 * en * sq(v));
+                    c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(v) * sq(w) * sq(slown));
+                    tref = TIv; tdiv = 1.0;
+                } else if (ak) {
+                    u = dnr; v = ri * dnx; w = risti * dnz;
+                    em = TJv - TIv;
+                    en = TKv - TIv;
+                    a = sq(v) * sq(w) + sq(u) * sq(w) + sq(u) * sq(v);
+                    b = -2.0 * sq(u) * (em * sq(w) + en * sq(v));
+                    c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
+                    tref = TIv; tdiv = 1.0;
+                } else {
+                    u = dnr; v = ri * dnx;
+                    em = TJv - TIv;
+                    a = sq(u) + sq(v);
+                    b = -2.0 * sq(u) * em;
+                    c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                    tref = TIv; tdiv = 1.0;
+                }
+            } else {
+                if (swk == 0) {
+                    u = dnr; v = 2.0 * risti * dnz;
+                    em = 3.0 * TIv - 4.0 * TKv + TK2;
+                    a = sq(v) + 9.0 * sq(u);
+                    b = 6.0 * em * sq(u);
+                    c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                    tref = TIv; tdiv = 1.0;
+                } else if (ak) {
+                    u = dnr; v = risti * dnz;
+                    em = TKv - TIv;
+                    a = sq(u) + sq(v);
+                    b = -2.0 * sq(u) * em;
+                    c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                    tref = TIv; tdiv = 1.0;
+                } else {
+                    a = 1.0; b = 0.0;
+                    c = -sq(slown) * sq(dnr);
+                    tref = TIv; tdiv = 1.0;
+                }
+            }
+        } else {
+            if (swj == 0) {
+                swsol = 1;
+                if (swk == 0) {
+                    u = 2.0 * ri * dnx; v = 2.0 * risti * dnz;
+                    em = 4.0 * TJv - TJ2 - 4.0 * TKv; em = em + TK2;
+                    a = sq(v) + sq(u);
+                    b = 2.0 * em * sq(u);
+                    c = sq(u) * (sq(em) - sq(slown) * sq(v));
+                    tref = 4.0 * TJv - TJ2; tdiv = 3.0;
+                } else if (ak) {
+                    u = risti * dnz; v = 2.0 * ri * dnx;
+                    em = 3.0 * TKv - 4.0 * TJv + TJ2;
+                    a = sq(v) + 9.0 * sq(u);
+                    b = 6.0 * em * sq(u);
+                    c = sq(u) * (sq(em) - sq(slown) * sq(v));
+                    tref = TKv; tdiv = 1.0;
+                } else {
+                    u = 2.0 * ri * dnx;
+                    a = 1.0; b = 0.0;
+                    c = -sq(u) * sq(slown);
+                    tref = 4.0 * TJv - TJ2; tdiv = 3.0;
+                }
+            } else if (aj) {
+                swsol = 1;
+                if (swk == 0) {
+                    u = ri * dnx; v = 2.0 * risti * dnz;
+                    em = 3.0 * TJv - 4.0 * TKv + TK2;
+                    a = sq(v) + 9.0 * sq(u);
+                    b = 6.0 * em * sq(u);
+                    c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                    tref = TJv; tdiv = 1.0;
+                } else if (ak) {
+                    u = ri * dnx; v = risti * dnz;
+                    em = TKv - TJv;
+                    a = sq(u) + sq(v);
+                    b = -2.0 * sq(u) * em;
+                    c = sq(u) * (sq(em) - sq(v) * sq(slown));
+                    tref = TJv; tdiv = 1.0;
+                } else {
+                    a = 1.0; b = 0.0;
+                    c = -sq(slown) * sq(ri) * sq(dnx);
+                    tref = TJv; tdiv = 1.0;
+                }
+            } else {
+                if (swk == 0) {
+                    swsol = 1;
+                    u = 2.0 * risti * dnz;
+                    a = 1.0; b = 0.0;
+                    c = -sq(u) * sq(slown);
+                    tref = 4.0 * TKv - TK2; tdiv = 3.0;
+                } else if (ak) {
+                    swsol = 1;
+                    a = 1.0; b = 0.0;
+                    c = -sq(slown) * sq(risti) * sq(dnz);
+                    tref = TKv; tdiv = 1.0;
+                }
+            }
+        }
+#undef TIv
+#undef TI2
+#undef TJv
+#undef TJ2
+#undef TKv
+#undef TK2
+        if (swsol) {
+        double rd1 = sq(b) - 4.0 * a * c;
+        if (rd1 < 0.0) rd1 = 0.0;
+        const double tdsh = (-b + sqrt(rd1)) / (2.0 * a);
+        *trav = (tref + tdsh) / tdiv;
+    }
+    return swsol;
+}
+
 /* fouds2_all: mixed-order update over the eight octants (F:635-1004). */
 static void fouds2(fmm_state *s, int iz, int ix, int ir)
 {
     const orc_grid *g = s->g;
-    const double dnr = g->dnr, dnx = g->dnx, dnz = g->dnz;
     double ri, risti;
     centre_geom(s, ix, ir, &ri, &risti);
     const double slown = 1.0 / s->veln[VELN(g, iz, ix, ir)];
@@ -274,234 +514,9 @@ static void fouds2(fmm_state *s, int iz, int ix, int ir)
                 const int swk = sw2(s, NS(s, k, ix, ir) == 0, k2in, k2in && NS(s, k2, ix, ir) == 0,
                                     TT(s, k, ix, ir), k2in ? TT(s, k2, ix, ir) : 0.0);
                 if (i < 1 || i > s->nnr || j < 1 || j > s->nnx || k < 1 || k > s->nnz) continue;
-                int swsol = 0;
-                double a = 0, b = 0, c = 0, u, v, w, em, en, tref = 0, tdiv = 1.0;
                 const int ai = NS(s, iz, ix, i) == 0, aj = NS(s, iz, j, ir) == 0, ak = NS(s, k, ix, ir) == 0;
-                /* neighbour values; second neighbours are only read on the
-                 * branches whose switch proved them in range */
-#define TIv TT(s, iz, ix, i)
-#define TI2 TT(s, iz, ix, i2)
-#define TJv TT(s, iz, j, ir)
-#define TJ2 TT(s, iz, j2, ir)
-#define TKv TT(s, k, ix, ir)
-#define TK2 TT(s, k2, ix, ir)
-                if (swi == 0) {
-                    swsol = 1;
-                    if (swj == 0) {
-                        if (swk == 0) {
-                            u = 2.0 * dnr; v = 2.0 * ri * dnx; w = 2.0 * risti * dnz;
-                            em = 4.0 * TIv - TI2 - 4.0 * TJv; em = em + TJ2;
-                            en = 4.0 * TIv - TI2 - 4.0 * TKv; en = en + TK2;
-                            a = sq(v) * sq(w) + sq(u) * sq(w) + sq(u) * sq(v);
-                            b = 2.0 * sq(u) * (em * sq(w) + en * sq(v));
-                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(v) * sq(w) * sq(slown));
-                            tref = 4.0 * TIv - TI2; tdiv = 3.0;
-                        } else if (ak) {
-                            u = risti * dnz; v = 2.0 * ri * dnx; w = 2.0 * dnr;
-                            em = 3.0 * TKv - 4.0 * TJv + TJ2;
-                            en = 3.0 * TKv - 4.0 * TIv + TI2;
-                            a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
-                            b = 6.0 * sq(u) * (em * sq(w) + en * sq(v));
-                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
-                            tref = TKv; tdiv = 1.0;
-                        } else {
-                            u = 2.0 * dnr; v = 2.0 * ri * dnx;
-                            em = 4.0 * TIv - TI2 - 4.0 * TJv; em = em + TJ2;
-                            a = sq(v) + sq(u);
-                            b = 2.0 * em * sq(u);
-                            c = sq(u) * (sq(em) - sq(slown) * sq(v));
-                            tref = 4.0 * TIv - TI2; tdiv = 3.0;
-                        }
-                    } else if (aj) {
-                        if (swk == 0) {
-                            u = ri * dnx; v = 2.0 * dnr; w = 2.0 * risti * dnz;
-                            em = 3.0 * TJv - 4.0 * TIv + TI2;
-                            en = 3.0 * TJv - 4.0 * TKv + TK2;
-                            a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
-                            b = 6.0 * sq(u) * (em * sq(w) + en * sq(v));
-                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
-                            tref = TJv; tdiv = 1.0;
-                        } else if (ak) {
-                            u = ri * dnx; v = 2.0 * dnr; w = risti * dnz;
-                            em = 3.0 * TJv - 4.0 * TIv + TI2;
-                            en = TJv - TKv;
-                            a = sq(w) * sq(v) + 9.0 * sq(u) * sq(w) + sq(u) * sq(v);
-                            b = sq(u) * (6.0 * em * sq(w) + 2.0 * en * sq(v));
-                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
-                            tref = TJv; tdiv = 1.0;
-                        } else {
-                            u = ri * dnx; v = 2.0 * dnr;
-                            em = 3.0 * TJv - 4.0 * TIv + TI2;
-                            a = sq(v) + 9.0 * sq(u);
-                            b = 6.0 * em * sq(u);
-                            c = sq(u) * (sq(em) - sq(slown) * sq(v));
-                            tref = TJv; tdiv = 1.0;
-                        }
-                    } else {
-                        if (swk == 0) {
-                            u = 2.0 * dnr; v = 2.0 * risti * dnz;
-                            em = 4.0 * TIv - TI2 - 4.0 * TKv; em = em + TK2;
-                            a = sq(u) + sq(v);
-                            b = 2.0 * em * sq(u);
-                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
-                            tref = 4.0 * TIv - TI2; tdiv = 3.0;
-                        } else if (ak) {
-                            u = risti * dnz; v = 2.0 * dnr;
-                            em = 3.0 * TKv - 4.0 * TIv + TI2;
-                            a = sq(v) + 9.0 * sq(u);
-                            b = 6.0 * em * sq(u);
-                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
-                            tref = TKv; tdiv = 1.0;
-                        } else {
-                            u = 2.0 * dnr;
-                            a = 1.0; b = 0.0;
-                            c = -sq(u) * sq(slown);
-                            tref = 4.0 * TIv - TI2; tdiv = 3.0;
-                        }
-                    }
-                } else if (ai) {
-                    swsol = 1;
-                    if (swj == 0) {
-                        if (swk == 0) {
-                            u = dnr; v = 2.0 * ri * dnx; w = 2.0 * risti * dnz;
-                            em = 3.0 * TIv - 4.0 * TJv + TJ2;
-                            en = 3.0 * TIv - 4.0 * TKv + TK2;
-                            a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
-                            b = 6.0 * sq(u) * (em * sq(w) + en * sq(v));
-                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
-                            tref = TIv; tdiv = 1.0;
-                        } else if (ak) {
-                            u = dnr; v = 2.0 * ri * dnx; w = risti * dnz;
-                            em = 3.0 * TIv - 4.0 * TJv + TJ2;
-                            en = TIv - TKv;
-                            a = sq(v) * sq(w) + 9.0 * sq(u) * sq(w) + sq(u) * sq(v);
-                            b = sq(u) * (6.0 * em * sq(w) + 2.0 * en * sq(v));
-                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(v) * sq(w) * sq(slown));
-                            tref = TIv; tdiv = 1.0;
-                        } else {
-                            u = dnr; v = 2.0 * ri * dnx;
-                            em = 3.0 * TIv - 4.0 * TJv + TJ2;
-                            a = sq(v) + 9.0 * sq(u);
-                            b = 6.0 * em * sq(u);
-                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
-                            tref = TIv; tdiv = 1.0;
-                        }
-                    } else if (aj) {
-                        if (swk == 0) {
-                            u = dnr; v = ri * dnx; w = 2.0 * risti * dnz;
-                            em = TIv - TJv;
-                            en = 3.0 * TIv - 4.0 * TKv + TK2;
-                            a = sq(v) * sq(w) + sq(u) * sq(w) + 9.0 * sq(u) * sq(v);
-                            b = sq(u) * (2.0 * em * sq(w) + 6.0 * en * sq(v));
-                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(v) * sq(w) * sq(slown));
-                            tref = TIv; tdiv = 1.0;
-                        } else if (ak) {
-                            u = dnr; v = ri * dnx; w = risti * dnz;
-                            em = TJv - TIv;
-                            en = TKv - TIv;
-                            a = sq(v) * sq(w) + sq(u) * sq(w) + sq(u) * sq(v);
-                            b = -2.0 * sq(u) * (em * sq(w) + en * sq(v));
-                            c = sq(u) * (sq(em) * sq(w) + sq(en) * sq(v) - sq(slown) * sq(v) * sq(w));
-                            tref = TIv; tdiv = 1.0;
-                        } else {
-                            u = dnr; v = ri * dnx;
-                            em = TJv - TIv;
-                            a = sq(u) + sq(v);
-                            b = -2.0 * sq(u) * em;
-                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
-                            tref = TIv; tdiv = 1.0;
-                        }
-                    } else {
-                        if (swk == 0) {
-                            u = dnr; v = 2.0 * risti * dnz;
-                            em = 3.0 * TIv - 4.0 * TKv + TK2;
-                            a = sq(v) + 9.0 * sq(u);
-                            b = 6.0 * em * sq(u);
-                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
-                            tref = TIv; tdiv = 1.0;
-                        } else if (ak) {
-                            u = dnr; v = risti * dnz;
-                            em = TKv - TIv;
-                            a = sq(u) + sq(v);
-                            b = -2.0 * sq(u) * em;
-                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
-                            tref = TIv; tdiv = 1.0;
-                        } else {
-                            a = 1.0; b = 0.0;
-                            c = -sq(slown) * sq(dnr);
-                            tref = TIv; tdiv = 1.0;
-                        }
-                    }
-                } else {
-                    if (swj == 0) {
-                        swsol = 1;
-                        if (swk == 0) {
-                            u = 2.0 * ri * dnx; v = 2.0 * risti * dnz;
-                            em = 4.0 * TJv - TJ2 - 4.0 * TKv; em = em + TK2;
-                            a = sq(v) + sq(u);
-                            b = 2.0 * em * sq(u);
-                            c = sq(u) * (sq(em) - sq(slown) * sq(v));
-                            tref = 4.0 * TJv - TJ2; tdiv = 3.0;
-                        } else if (ak) {
-                            u = risti * dnz; v = 2.0 * ri * dnx;
-                            em = 3.0 * TKv - 4.0 * TJv + TJ2;
-                            a = sq(v) + 9.0 * sq(u);
-                            b = 6.0 * em * sq(u);
-                            c = sq(u) * (sq(em) - sq(slown) * sq(v));
-                            tref = TKv; tdiv = 1.0;
-                        } else {
-                            u = 2.0 * ri * dnx;
-                            a = 1.0; b = 0.0;
-                            c = -sq(u) * sq(slown);
-                            tref = 4.0 * TJv - TJ2; tdiv = 3.0;
-                        }
-                    } else if (aj) {
-                        swsol = 1;
-                        if (swk == 0) {
-                            u = ri * dnx; v = 2.0 * risti * dnz;
-                            em = 3.0 * TJv - 4.0 * TKv + TK2;
-                            a = sq(v) + 9.0 * sq(u);
-                            b = 6.0 * em * sq(u);
-                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
-                            tref = TJv; tdiv = 1.0;
-                        } else if (ak) {
-                            u = ri * dnx; v = risti * dnz;
-                            em = TKv - TJv;
-                            a = sq(u) + sq(v);
-                            b = -2.0 * sq(u) * em;
-                            c = sq(u) * (sq(em) - sq(v) * sq(slown));
-                            tref = TJv; tdiv = 1.0;
-                        } else {
-                            a = 1.0; b = 0.0;
-                            c = -sq(slown) * sq(ri) * sq(dnx);
-                            tref = TJv; tdiv = 1.0;
-                        }
-                    } else {
-                        if (swk == 0) {
-                            swsol = 1;
-                            u = 2.0 * risti * dnz;
-                            a = 1.0; b = 0.0;
-                            c = -sq(u) * sq(slown);
-                            tref = 4.0 * TKv - TK2; tdiv = 3.0;
-                        } else if (ak) {
-                            swsol = 1;
-                            a = 1.0; b = 0.0;
-                            c = -sq(slown) * sq(risti) * sq(dnz);
-                            tref = TKv; tdiv = 1.0;
-                        }
-                    }
-                }
-#undef TIv
-#undef TI2
-#undef TJv
-#undef TJ2
-#undef TKv
-#undef TK2
-                if (swsol) {
-                    double rd1 = sq(b) - 4.0 * a * c;
-                    if (rd1 < 0.0) rd1 = 0.0;
-                    const double tdsh = (-b + sqrt(rd1)) / (2.0 * a);
-                    const double trav = (tref + tdsh) / tdiv;
+                double trav;
+                if (octant2(s, iz, ix, ir, i, j, k, i2, j2, k2, ai, aj, ak, swi, swj, swk, ri, risti, slown, &trav)) {
                     if (tsw1) travm = fmin(trav, travm);
                     else { travm = trav; tsw1 = 1; }
                 }
@@ -511,6 +526,181 @@ static void fouds2(fmm_state *s, int iz, int ix, int ir)
     /* F:1001: travm is undefined in the reference when no octant solved;
      * that cannot happen for a neighbour of a popped node. */
     if (TT(s, iz, ix, ir) == 0.0 || TT(s, iz, ix, ir) > travm) TT(s, iz, ix, ir) = travm;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Fixed point of the reference's stencil (order-independent restatement)    */
+/* ------------------------------------------------------------------------ */
+/* One octant of fouds1_all (F:547-621) for given upwind flags. */
+static int octant1(const fmm_state *s, int iz, int ix, int ir, int i, int j, int k, int ai, int aj, int ak,
+                   double ri, double risti, double slown, double *trav)
+{
+    const orc_grid *g = s->g;
+    const double dnr = g->dnr, dnx = g->dnx, dnz = g->dnz;
+    double a = 0, b = 0, c = 0, tref = 0;
+    int swsol = 0;
+    if (ai) {
+        swsol = 1;
+        if (aj && ak) {
+            const double u = dnr, v = ri * dnx, w = risti * dnz;
+            const double em = TT(s, iz, j, ir) - TT(s, iz, ix, i);
+            const double en = TT(s, k, ix, ir) - TT(s, iz, ix, i);
+            const double rd1 = sq(v) * sq(w), rd2 = sq(u) * sq(w), rd3 = sq(u) * sq(v);
+            a = rd1 + rd2 + rd3;
+            b = -2.0 * (em * rd2 + en * rd3);
+            c = sq(em) * rd2 + sq(en) * rd3 - sq(slown) * sq(u) * rd1;
+        } else if (aj) {
+            const double u = dnr, v = ri * dnx;
+            const double em = TT(s, iz, j, ir) - TT(s, iz, ix, i);
+            a = sq(u) + sq(v);
+            b = -2.0 * sq(u) * em;
+            c = sq(u) * (sq(em) - sq(v) * sq(slown));
+        } else if (ak) {
+            const double u = dnr, v = risti * dnz;
+            const double em = TT(s, k, ix, ir) - TT(s, iz, ix, i);
+            a = sq(u) + sq(v);
+            b = -2.0 * sq(u) * em;
+            c = sq(u) * (sq(em) - sq(v) * sq(slown));
+        } else {
+            a = 1.0; b = 0.0;
+            c = -sq(slown) * sq(dnr);
+        }
+        tref = TT(s, iz, ix, i);
+    } else if (aj) {
+        swsol = 1;
+        if (ak) {
+            const double u = ri * dnx, v = risti * dnz;
+            const double em = TT(s, k, ix, ir) - TT(s, iz, j, ir);
+            a = sq(u) + sq(v);
+            b = -2.0 * sq(u) * em;
+            c = sq(u) * (sq(em) - sq(v) * sq(slown));
+        } else {
+            a = 1.0; b = 0.0;
+            c = -sq(slown) * sq(ri) * sq(dnx);
+        }
+        tref = TT(s, iz, j, ir);
+    } else if (ak) {
+        swsol = 1;
+        a = 1.0; b = 0.0;
+        c = -sq(slown * risti * dnz);
+        tref = TT(s, k, ix, ir);
+    }
+    if (swsol) {
+        double rd1 = sq(b) - 4.0 * a * c;
+        if (rd1 < 0.0) rd1 = 0.0;
+        *trav = tref + (-b + sqrt(rd1)) / (2.0 * a);
+    }
+    return swsol;
+}
+
+/* Node value at the fixed point's self-consistency condition: in every
+ * octant the neighbours are added in ascending time while earlier than the
+ * octant's current solution ("alive" of the heap restated as "earlier than
+ * the node"), each partial set solved with the reference's own formulas;
+ * minimum over octants.  Unset nodes hold +infinity. */
+static double fp_update(fmm_state *s, int fom, int iz, int ix, int ir)
+{
+    const orc_grid *g = s->g;
+    double ri, risti;
+    centre_geom(s, ix, ir, &ri, &risti);
+    const double slown = 1.0 / s->veln[VELN(g, iz, ix, ir)];
+    double best = INFINITY;
+    for (int i = ir - 1; i <= ir + 1; i += 2)
+        for (int j = ix - 1; j <= ix + 1; j += 2)
+            for (int k = iz - 1; k <= iz + 1; k += 2) {
+                if (i < 1 || i > s->nnr || j < 1 || j > s->nnx || k < 1 || k > s->nnz) continue;
+                const int i2 = (i == ir - 1) ? i - 1 : i + 1;
+                const int j2 = (j == ix - 1) ? j - 1 : j + 1;
+                const int k2 = (k == iz - 1) ? k - 1 : k + 1;
+                const int i2in = i2 >= 1 && i2 <= s->nnr, j2in = j2 >= 1 && j2 <= s->nnx, k2in = k2 >= 1 && k2 <= s->nnz;
+                double val[3] = {TT(s, iz, ix, i), TT(s, iz, j, ir), TT(s, k, ix, ir)};
+                int ord[3] = {0, 1, 2};
+                /* ascending, ties keep r, theta, phi order */
+                if (val[ord[1]] < val[ord[0]]) { int q = ord[0]; ord[0] = ord[1]; ord[1] = q; }
+                if (val[ord[2]] < val[ord[1]]) { int q = ord[1]; ord[1] = ord[2]; ord[2] = q; }
+                if (val[ord[1]] < val[ord[0]]) { int q = ord[0]; ord[0] = ord[1]; ord[1] = q; }
+                int al[3] = {0, 0, 0};
+                double cur = INFINITY;
+                int have = 0;
+                for (int m = 0; m < 3; ++m) {
+                    const double v = val[ord[m]];
+                    if (!(v < INFINITY)) break;
+                    if (have && !(v < cur)) break;
+                    al[ord[m]] = 1;
+                    double trav = 0.0;
+                    int ok;
+                    if (fom == 0) {
+                        ok = octant1(s, iz, ix, ir, i, j, k, al[0], al[1], al[2], ri, risti, slown, &trav);
+                    } else {
+                        const int swi = (al[0] && i2in && TT(s, iz, ix, i2) < val[0]) ? 0 : -1;
+                        const int swj = (al[1] && j2in && TT(s, iz, j2, ir) < val[1]) ? 0 : -1;
+                        const int swk = (al[2] && k2in && TT(s, k2, ix, ir) < val[2]) ? 0 : -1;
+                        ok = octant2(s, iz, ix, ir, i, j, k, i2, j2, k2, al[0], al[1], al[2], swi, swj, swk,
+                                     ri, risti, slown, &trav);
+                    }
+                    if (!ok) break;
+                    cur = trav;
+                    have = 1;
+                }
+                if (have && cur < best) best = cur;
+            }
+    return best;
+}
+
+int orc_fixed_point(const orc_grid *g, const double *veln, int fom, const double *bottom, double *ttn,
+                    int max_sweeps, int *sweeps)
+{
+    fmm_state s;
+    memset(&s, 0, sizeof s);
+    s.g = g; s.veln = veln;
+    s.nnr = g->nnr; s.nnx = g->nnx; s.nnz = g->nnz;
+    s.NZ2 = g->nnz + 2; s.NX2 = g->nnx + 2;
+    const size_t npad = (size_t)s.NZ2 * (size_t)s.NX2 * (size_t)(g->nnr + 2);
+    s.ttn = (double *)malloc(npad * sizeof(double));
+    unsigned char *fixed = (unsigned char *)calloc(npad, 1);
+    if (!s.ttn || !fixed) { free(s.ttn); free(fixed); return -3; }
+    for (size_t q = 0; q < npad; ++q) s.ttn[q] = INFINITY;
+    const int rn = g->nnr;
+    for (int i = 1; i <= g->nnx; ++i)
+        for (int j = 1; j <= g->nnz; ++j) {
+            const double v = bottom[(size_t)(j - 1) + (size_t)g->nnz * (size_t)(i - 1)];
+            if (v > 0.0) {   /* F:6932-6936 */
+                TT(&s, j, i, rn) = v;
+                fixed[TI(&s, j, i, rn)] = 1;
+            }
+        }
+    int it;
+    int converged = 0;
+    for (it = 0; it < max_sweeps; ++it) {
+        long changed = 0;
+        const int o = it % 8;
+        const int sr = (o & 4) ? 1 : -1, sx = (o & 2) ? 1 : -1, sz = (o & 1) ? 1 : -1;
+        for (int a = 0; a < g->nnr; ++a) {
+            const int ir = sr > 0 ? 1 + a : g->nnr - a;
+            for (int b = 0; b < g->nnx; ++b) {
+                const int ix = sx > 0 ? 1 + b : g->nnx - b;
+                for (int c = 0; c < g->nnz; ++c) {
+                    const int iz = sz > 0 ? 1 + c : g->nnz - c;
+                    if (fixed[TI(&s, iz, ix, ir)]) continue;
+                    const double nv = fp_update(&s, fom, iz, ix, ir);
+                    const double ov = TT(&s, iz, ix, ir);
+                    if (memcmp(&nv, &ov, sizeof nv) != 0) { TT(&s, iz, ix, ir) = nv; changed++; }
+                }
+            }
+        }
+        if (!changed) { converged = 1; break; }
+    }
+    for (int ir = 1; ir <= g->nnr; ++ir)
+        for (int ix = 1; ix <= g->nnx; ++ix)
+            for (int iz = 1; iz <= g->nnz; ++iz) {
+                const double v = TT(&s, iz, ix, ir);
+                ttn[(size_t)(iz - 1) + (size_t)g->nnz * ((size_t)(ix - 1) + (size_t)g->nnx * (size_t)(ir - 1))] =
+                    v < INFINITY ? v : 0.0;
+            }
+    if (sweeps) *sweeps = it + 1;
+    free(s.ttn);
+    free(fixed);
+    return converged ? 0 : -4;
 }
 
 /* Heap operations (F:1006-1098). Ties keep the reference's order. */

@@ -75,6 +75,16 @@ int orc_gridder(const orc_grid *g, const double *velv, double *veln, int *nclamp
 int orc_fmm(const orc_grid *g, const double *veln, int fom, const double *bottom,
             double *ttn, long long *npops);
 
+/* Fixed point of the reference's stencil: the same octant formulas
+ * (fouds1_all / fouds2_all) with the heap's "alive" test restated as
+ * "earlier than the node", iterated by Gauss-Seidel sweeps in alternating
+ * directions until a sweep changes no bit.  Order independent; equals the
+ * fast-marching result wherever the heap order is causal (e.g. a full
+ * teleseismic frame on a smooth model).  Returns 0, or -4 if max_sweeps was
+ * reached first. */
+int orc_fixed_point(const orc_grid *g, const double *veln, int fom, const double *bottom,
+                    double *ttn, int max_sweeps, int *sweeps);
+
 /* Receiver traveltimes (F:7040-7248): trilinear interpolation accumulated
  * in single precision.  Returns 0, or -(1+k) if receiver k lies outside the
  * propagation grid. */

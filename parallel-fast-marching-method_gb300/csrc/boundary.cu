@@ -73,6 +73,37 @@ __global__ void finalize_kernel(Geom g, const double *__restrict__ frames, R *__
     }
 }
 
+// One block per event: the dominant lateral propagation direction of the
+// boundary frame (sign of its summed theta and phi differences over pairs of
+// fixed nodes), which orders the solver's sweep.  bit 0: times grow with
+// theta (sweep +theta), bit 1: times grow with phi.
+__global__ void directions_kernel(Geom g, const double *__restrict__ frames, int *__restrict__ dir)
+{
+    const int e = blockIdx.x;
+    const long long nb = (long long)g.nnx * g.nnz;
+    const double *fr = frames + (size_t)e * nb;
+    double sx = 0.0, sz = 0.0;
+    for (long long q = threadIdx.x; q < nb; q += blockDim.x) {
+        const int iz = (int)(q % g.nnz), ix = (int)(q / g.nnz);
+        const double v = fr[q];
+        if (!(v > 0.0)) continue;
+        if (ix + 1 < g.nnx && fr[q + g.nnz] > 0.0) sx += fr[q + g.nnz] - v;
+        if (iz + 1 < g.nnz && fr[q + 1] > 0.0) sz += fr[q + 1] - v;
+    }
+    __shared__ double rx[32], rz[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sz += __shfl_xor_sync(0xffffffffu, sz, o);
+    }
+    if ((threadIdx.x & 31) == 0) { rx[threadIdx.x >> 5] = sx; rz[threadIdx.x >> 5] = sz; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ax = 0.0, az = 0.0;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) { ax += rx[w]; az += rz[w]; }
+        dir[e] = (ax >= 0.0 ? 1 : 0) | (az >= 0.0 ? 2 : 0);
+    }
+}
+
 template <typename R>
 __global__ void fill_inf_kernel(R *__restrict__ T, size_t n)
 {
@@ -132,6 +163,11 @@ void launch_finalize_frames(const Geom &g, int nev, int prec, const double *fram
         finalize_kernel<double><<<nev, 512, 0, st>>>(g, frames, (double *)T, frozen, base, 0);
     else
         finalize_kernel<float><<<nev, 512, 0, st>>>(g, frames, (float *)T, frozen, base, 1);
+}
+
+void launch_sweep_directions(const Geom &g, int nev, const double *frames, int *dir, cudaStream_t st)
+{
+    directions_kernel<<<nev, 256, 0, st>>>(g, frames, dir);
 }
 
 void launch_fill_inf(void *T, size_t n, int prec, cudaStream_t st)

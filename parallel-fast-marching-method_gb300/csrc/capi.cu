@@ -91,18 +91,25 @@ int tiles_per_event(const Geom &g, int shape, int *ntr, int *ntx, int *ntz)
 }
 
 template <typename R>
-void fill_geometry(const Geom &g, std::vector<R> &hx, std::vector<R> &hz)
+void fill_geometry(const Geom &g, std::vector<R> &hx, std::vector<R> &hz, std::vector<R> &wx, std::vector<R> &wz)
 {
     // spacings at each node as the stencil evaluates them (F:642-644, 712ff):
-    // dr, r*dtheta, r*sin(theta)*dphi with r = rgor - (ir-1)*dnr + earth
+    // dr, r*dtheta, r*sin(theta)*dphi with r = rgor - (ir-1)*dnr + earth,
+    // and their inverse squares
     hx.resize(g.nnr);
+    wx.resize(g.nnr);
     hz.resize((size_t)g.nnr * g.nnx);
+    wz.resize((size_t)g.nnr * g.nnx);
     for (int ir = 0; ir < g.nnr; ++ir) {
         const double ri = g.rgor - (double)ir * g.dnr + g.earth;
-        hx[ir] = (R)(ri * g.dnx);
+        const double v = ri * g.dnx;
+        hx[ir] = (R)v;
+        wx[ir] = (R)(1.0 / (v * v));
         for (int ix = 0; ix < g.nnx; ++ix) {
             const double risti = ri * std::sin(g.rgox + (double)ix * g.dnx);
-            hz[(size_t)ir * g.nnx + ix] = (R)(risti * g.dnz);
+            const double w = risti * g.dnz;
+            hz[(size_t)ir * g.nnx + ix] = (R)w;
+            wz[(size_t)ir * g.nnx + ix] = (R)(1.0 / (w * w));
         }
     }
 }
@@ -110,33 +117,120 @@ void fill_geometry(const Geom &g, std::vector<R> &hx, std::vector<R> &hz)
 template <typename R>
 int upload_geometry(fm3dt_ctx *ctx)
 {
-    std::vector<R> hx, hz;
-    fill_geometry<R>(ctx->g, hx, hz);
+    std::vector<R> hx, hz, wx, wz;
+    fill_geometry<R>(ctx->g, hx, hz, wx, wz);
     CK(cudaMemcpy(ctx->d_hx, hx.data(), hx.size() * sizeof(R), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_hz, hz.data(), hz.size() * sizeof(R), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_wx, wx.data(), wx.size() * sizeof(R), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_wz, wz.data(), wz.size() * sizeof(R), cudaMemcpyHostToDevice));
     return FM3DT_OK;
 }
 
-int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st)
+// Tile hyperplanes a' + b' + c' = h of the swept tile coordinates of a shape
+// (a' counts tile layers upward from the bottom), packed a'<<20 | b'<<10 | c'.
+int ensure_planes(fm3dt_ctx *ctx, int shape)
+{
+    auto &P = ctx->planes[shape];
+    if (P.shape == shape) return FM3DT_OK;
+    int ntr, ntx, ntz;
+    tiles_per_event(ctx->g, shape, &ntr, &ntx, &ntz);
+    if (ntr > 2047 || ntx > 1023 || ntz > 1023) return fail(ctx, FM3DT_EINVAL, "too many tiles along one axis");
+    const int H = ntr + ntx + ntz - 2;
+    std::vector<std::vector<int>> by(H);
+    for (int a = 0; a < ntr; ++a)
+        for (int b = 0; b < ntx; ++b)
+            for (int c = 0; c < ntz; ++c) by[a + b + c].push_back((a << 20) | (b << 10) | c);
+    std::vector<int> flat;
+    P.off.assign(H, 0);
+    P.cnt.assign(H, 0);
+    for (int h = 0; h < H; ++h) {
+        P.off[h] = (int)flat.size();
+        P.cnt[h] = (int)by[h].size();
+        flat.insert(flat.end(), by[h].begin(), by[h].end());
+    }
+    CK(cudaMalloc(&P.d_tiles, flat.size() * sizeof(int)));
+    CK(cudaMemcpy(P.d_tiles, flat.data(), flat.size() * sizeof(int), cudaMemcpyHostToDevice));
+    P.shape = shape;
+    return FM3DT_OK;
+}
+
+// resume: keep the current fields (no initialisation, no sweep) and run the
+// rounds with every tile active.
+int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, bool resume = false)
 {
     cudaStream_t s = ctx->stream;
     const Geom &g = ctx->g;
-    cudaEvent_t ev0, ev1;
+    cudaEvent_t ev0, ev1, sw0, sw1;
     CK(cudaEventCreate(&ev0));
     CK(cudaEventCreate(&ev1));
+    CK(cudaEventCreate(&sw0));
+    CK(cudaEventCreate(&sw1));
     CK(cudaEventRecord(ev0, s));
+    const bool do_sweep = ctx->sweep && !resume;
 
-    launch_fill_inf(ctx->d_T, (size_t)nev * ctx->N, ctx->prec, s);
-    launch_finalize_frames(g, nev, ctx->prec, ctx->d_frames, ctx->d_T, ctx->d_frozen, ctx->d_base, s);
-    ctx->launches += 2;
-    CKL();
+    if (!resume) {
+        launch_fill_inf(ctx->d_T, (size_t)nev * ctx->N, ctx->prec, s);
+        launch_finalize_frames(g, nev, ctx->prec, ctx->d_frames, ctx->d_T, ctx->d_frozen, ctx->d_base, s);
+        launch_sweep_directions(g, nev, ctx->d_frames, ctx->d_dir, s);
+        ctx->launches += 3;
+        CKL();
+    }
 
     const int shape = ctx->shape;
     const TileShape ts = kShapes[shape];
     int ntr, ntx, ntz;
     const int tpe = tiles_per_event(g, shape, &ntr, &ntx, &ntz);
-    // tiles whose nodes or 2-deep halos include the bottom layer
-    const int tlo = std::max(0, (g.nnr - 3) / ts.tr);
+
+    FieldArgs<double> f64{};
+    FieldArgs<float> f32{};
+    auto fill_field = [&](auto &f, auto *T, auto *sl, auto *hx, auto *hz, auto *wx, auto *wz) {
+        f.T = T; f.s = sl; f.hx = hx; f.hz = hz; f.wx = wx; f.wz = wz;
+        f.frozen = ctx->d_frozen;
+        f.nnr = g.nnr; f.nnx = g.nnx; f.nnz = g.nnz;
+        f.ntr = ntr; f.ntx = ntx; f.ntz = ntz;
+        f.tiles_per_event = tpe;
+        f.order2 = ctx->desc.fom ? 1 : 0;
+    };
+    if (ctx->prec == FM3DT_FP64) {
+        fill_field(f64, (double *)ctx->d_T, (const double *)ctx->d_s, (const double *)ctx->d_hx,
+                   (const double *)ctx->d_hz, (const double *)ctx->d_wx, (const double *)ctx->d_wz);
+        f64.hr = g.dnr;
+        f64.wr = 1.0 / (g.dnr * g.dnr);
+    } else {
+        fill_field(f32, (float *)ctx->d_T, (const float *)ctx->d_s, (const float *)ctx->d_hx,
+                   (const float *)ctx->d_hz, (const float *)ctx->d_wx, (const float *)ctx->d_wz);
+        f32.hr = (float)g.dnr;
+        f32.wr = (float)(1.0 / (g.dnr * g.dnr));
+    }
+
+    // 1. directional sweep, one launch per tile hyperplane
+    int sweep_launches = 0;
+    CK(cudaEventRecord(sw0, s));
+    if (do_sweep) {
+        int rc = ensure_planes(ctx, shape);
+        if (rc) return rc;
+        const auto &P = ctx->planes[shape];
+        const int sgrid = std::max(1, sweep_blocks_per_sm(shape, ctx->prec)) * sm_count();
+        for (size_t h = 0; h < P.off.size(); ++h) {
+            const long long items = (long long)P.cnt[h] * nev;
+            const int grid = (int)std::min<long long>(items, sgrid);
+            if (ctx->prec == FM3DT_FP64) {
+                SweepArgs<double> a{f64, P.d_tiles, P.off[h], P.cnt[h], ctx->d_dir, nev};
+                launch_sweep_f64(shape, grid, a, s);
+            } else {
+                SweepArgs<float> a{f32, P.d_tiles, P.off[h], P.cnt[h], ctx->d_dir, nev};
+                launch_sweep_f32(shape, grid, a, s);
+            }
+            ++sweep_launches;
+        }
+        ctx->launches += sweep_launches;
+        CKL();
+    }
+    CK(cudaEventRecord(sw1, s));
+
+    // 2. rounds until no tile changes: all tiles after a sweep, else the
+    //    tiles whose nodes or 2-deep halos include the bottom layer
+    const int tlo = (do_sweep || resume) ? 0 : std::max(0, (g.nnr - 3) / ts.tr);
     const int first = tlo * ntx * ntz;
     const int cnt = (ntr - tlo) * ntx * ntz;
     CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
@@ -150,29 +244,13 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st)
     const int grid = bps * sm_count();
     const int max_rounds = ctx->max_rounds > 0 ? ctx->max_rounds : 64 * (ntr + ntx + ntz) + 256;
     const int chunk = 8;
-
     RoundArgs<double> a64{};
     RoundArgs<float> a32{};
-    auto fill_args = [&](auto &a, auto *T, auto *sl, auto *hx, auto *hz) {
-        a.T = T; a.s = sl; a.hx = hx; a.hz = hz;
-        a.frozen = ctx->d_frozen;
-        a.nnr = g.nnr; a.nnx = g.nnx; a.nnz = g.nnz;
-        a.ntr = ntr; a.ntx = ntx; a.ntz = ntz;
-        a.tiles_per_event = tpe;
-        a.flag = ctx->d_flag;
-        a.max_passes = ctx->max_passes;
-        a.order2 = ctx->desc.fom ? 1 : 0;
-        a.stats = ctx->d_stats;
-    };
-    if (ctx->prec == FM3DT_FP64) {
-        fill_args(a64, (double *)ctx->d_T, (const double *)ctx->d_s, (const double *)ctx->d_hx,
-                  (const double *)ctx->d_hz);
-        a64.hr = g.dnr;
-    } else {
-        fill_args(a32, (float *)ctx->d_T, (const float *)ctx->d_s, (const float *)ctx->d_hx,
-                  (const float *)ctx->d_hz);
-        a32.hr = (float)g.dnr;
-    }
+    a64.f = f64;
+    a32.f = f32;
+    a64.flag = a32.flag = ctx->d_flag;
+    a64.max_passes = a32.max_passes = ctx->max_passes;
+    a64.stats = a32.stats = ctx->d_stats;
 
     int rounds = 0;
     bool done = false;
@@ -202,7 +280,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st)
             ctx->launches += 1;
         }
         CKL();
-        const int last_next = (rounds - 1) & 1 ? 0 : 1;
+        const int last_next = ((rounds - 1) & 1) ^ 1;
         CK(cudaMemcpyAsync(ctx->h_count, ctx->d_count[last_next], sizeof(int), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         for (int q = 0; q < rounds - first_round; ++q) {
@@ -217,10 +295,13 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st)
     ctx->h_base.resize(nev);
     CK(cudaMemcpyAsync(ctx->h_base.data(), ctx->d_base, nev * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    float ms = 0.0f;
+    float ms = 0.0f, sms = 0.0f;
     cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventElapsedTime(&sms, sw0, sw1);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
+    cudaEventDestroy(sw0);
+    cudaEventDestroy(sw1);
     ctx->nev_solved = nev;
     if (st) {
         st->rounds = rounds;
@@ -231,6 +312,9 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st)
         st->ms = ms;
         st->round_ms = round_ms;
         st->round_launches = rounds;
+        st->sweep_ms = do_sweep ? sms : 0.0;
+        st->sweep_launches = sweep_launches;
+        st->sweep_nodes = do_sweep ? (int64_t)nev * (int64_t)ctx->N : 0;
     }
     if (!done) return fail(ctx, FM3DT_ENOCONV, "solver round limit reached before convergence");
     return FM3DT_OK;
@@ -306,6 +390,9 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMalloc(&ctx->d_s, ctx->N * rs));
     CKC(cudaMalloc(&ctx->d_hx, (size_t)d.nnr * rs));
     CKC(cudaMalloc(&ctx->d_hz, (size_t)d.nnr * d.nnx * rs));
+    CKC(cudaMalloc(&ctx->d_wx, (size_t)d.nnr * rs));
+    CKC(cudaMalloc(&ctx->d_wz, (size_t)d.nnr * d.nnx * rs));
+    CKC(cudaMalloc(&ctx->d_dir, ctx->maxev * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_T, ctx->N * ctx->maxev * rs));
     CKC(cudaMalloc(&ctx->d_frames, ctx->NB * ctx->maxev * sizeof(double)));
     CKC(cudaMalloc(&ctx->d_base, ctx->maxev * sizeof(double)));
@@ -363,6 +450,13 @@ int fm3dt_solve_device(fm3dt_ctx *ctx, int nev, const double *d_boundary, fm3dt_
     CK(cudaMemcpyAsync(ctx->d_frames, d_boundary, (size_t)nev * ctx->NB * sizeof(double), cudaMemcpyDeviceToDevice,
                        ctx->stream));
     return solve_common(ctx, nev, st);
+}
+
+int fm3dt_solve_resume(fm3dt_ctx *ctx, fm3dt_status *st)
+{
+    if (!ctx) return FM3DT_EINVAL;
+    if (ctx->nev_solved < 1) return fail(ctx, FM3DT_ESTATE, "no solved events to resume");
+    return solve_common(ctx, ctx->nev_solved, st, true);
 }
 
 int fm3dt_solve_planewave(fm3dt_ctx *ctx, int nev, const double *params, fm3dt_status *st)
@@ -579,13 +673,14 @@ int fm3dt_set_times(fm3dt_ctx *ctx, int event, int nev_total, const double *ttn)
     return FM3DT_OK;
 }
 
-int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rounds)
+int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rounds, int sweep)
 {
     if (!ctx) return FM3DT_EINVAL;
     if (tile_shape < 0 || tile_shape >= kNumShapes) return fail(ctx, FM3DT_EINVAL, "tile shape out of range");
     ctx->shape = tile_shape;
     if (max_passes > 0) ctx->max_passes = max_passes;
     if (max_rounds > 0) ctx->max_rounds = max_rounds;
+    if (sweep >= 0) ctx->sweep = sweep ? 1 : 0;
     return FM3DT_OK;
 }
 
@@ -620,6 +715,10 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_s);
     cudaFree(ctx->d_hx);
     cudaFree(ctx->d_hz);
+    cudaFree(ctx->d_wx);
+    cudaFree(ctx->d_wz);
+    cudaFree(ctx->d_dir);
+    for (auto &P : ctx->planes) cudaFree(P.d_tiles);
     cudaFree(ctx->d_T);
     cudaFree(ctx->d_frames);
     cudaFree(ctx->d_base);

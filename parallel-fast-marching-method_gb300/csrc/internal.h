@@ -24,33 +24,62 @@ struct Geom {
 // contiguous axis).  One thread owns one (theta, phi) column of TR nodes.
 struct TileShape { int tr, tx, tz; };
 constexpr int kNumShapes = 6;
-constexpr TileShape kShapes[kNumShapes] = {{4, 8, 32}, {8, 8, 32}, {4, 4, 32}, {8, 4, 32}, {2, 8, 32}, {4, 16, 16}};
+constexpr TileShape kShapes[kNumShapes] = {{4, 8, 32}, {8, 8, 32}, {16, 8, 32}, {8, 4, 32}, {16, 4, 32}, {32, 4, 32}};
 
-// Arguments of one solver round.
+// Field, model and tiling shared by the solver kernels.
 template <typename R>
-struct RoundArgs {
+struct FieldArgs {
     R *T;                       // [E][nnr][nnx][nnz]
     const R *s;                 // [nnr][nnx][nnz] slowness
-    const R *hx;                // [nnr]      r * dtheta
-    const R *hz;                // [nnr*nnx]  r * sin(theta) * dphi
-    R hr;                       // dr
+    const R *hx, *wx;           // [nnr]      r*dtheta and its inverse square
+    const R *hz, *wz;           // [nnr*nnx]  r*sin(theta)*dphi and its inverse square
+    R hr, wr;                   // dr and 1/dr^2
     const uint8_t *frozen;      // [E][nnx*nnz] fixed bottom-layer nodes
     int nnr, nnx, nnz;
     int ntr, ntx, ntz;          // tiles per axis
     int tiles_per_event;
+    int order2;
+};
+
+// Arguments of one solver round.
+template <typename R>
+struct RoundArgs {
+    FieldArgs<R> f;
     int *flag;                  // [E*tiles] 1 while a tile is queued
     const int *cur_list;
     const int *cur_count;
     int *next_list;
     int *next_count;
     int max_passes;
-    int order2;
     unsigned long long *stats;  // [0] tiles processed, [1] node updates, [2] staged nodes
+};
+
+// Arguments of one sweep launch (one tile hyperplane).
+template <typename R>
+struct SweepArgs {
+    FieldArgs<R> f;
+    const int *hp_tiles;        // swept tile coordinates (r' << 20 | x' << 10 | z'), by hyperplane
+    int hoff, hcount;           // this hyperplane's slice of hp_tiles
+    const int *dir;             // [E] bit 0: sweep +theta, bit 1: sweep +phi
+    int nev;
 };
 
 void launch_round_f64(int shape, int grid, const RoundArgs<double> &a, cudaStream_t st);
 void launch_round_f32(int shape, int grid, const RoundArgs<float> &a, cudaStream_t st);
-int round_blocks_per_sm(int shape, int prec);
+void launch_sweep_f64(int shape, int grid, const SweepArgs<double> &a, cudaStream_t st);
+void launch_sweep_f32(int shape, int grid, const SweepArgs<float> &a, cudaStream_t st);
+int occupancy_round_f32(int shape);
+int occupancy_round_f64(int shape);
+int occupancy_sweep_f32(int shape);
+int occupancy_sweep_f64(int shape);
+inline int round_blocks_per_sm(int shape, int prec)
+{
+    return prec == FM3DT_FP64 ? occupancy_round_f64(shape) : occupancy_round_f32(shape);
+}
+inline int sweep_blocks_per_sm(int shape, int prec)
+{
+    return prec == FM3DT_FP64 ? occupancy_sweep_f64(shape) : occupancy_sweep_f32(shape);
+}
 
 // model.cu
 void launch_gridder(const Geom &g, const double *velv, double *veln, cudaStream_t st);
@@ -63,6 +92,7 @@ void launch_planewave_frames(const Geom &g, const PlaneWaveGeom &pg, int nev, co
 void launch_finalize_frames(const Geom &g, int nev, int prec, const double *frames, void *T,
                             uint8_t *frozen, double *base, cudaStream_t st);
 void launch_fill_inf(void *T, size_t n, int prec, cudaStream_t st);
+void launch_sweep_directions(const Geom &g, int nev, const double *frames, int *dir, cudaStream_t st);
 void launch_initial_tiles(int nev, int tiles_per_event, int first_tile, int count_per_event,
                           int *list, int *count, int *flag, cudaStream_t st);
 void launch_to_absolute(const Geom &g, int prec, const void *T, size_t offset, double base, double *out,
@@ -109,6 +139,9 @@ struct fm3dt_ctx {
     void *d_s = nullptr;
     void *d_hx = nullptr;
     void *d_hz = nullptr;
+    void *d_wx = nullptr;
+    void *d_wz = nullptr;
+    int *d_dir = nullptr;
     void *d_T = nullptr;
     double *d_frames = nullptr;
     double *d_base = nullptr;
@@ -128,6 +161,10 @@ struct fm3dt_ctx {
     int shape = 0;
     int max_passes = 64;
     int max_rounds = 0;           // 0 = automatic
+    int sweep = 1;                // directional sweep before the rounds
+    // tile hyperplanes of each shape (device list + host offsets)
+    struct Planes { int shape = -1; int *d_tiles = nullptr; std::vector<int> off, cnt; };
+    Planes planes[fm3dt::kNumShapes];
     size_t flag_capacity = 0;     // tiles allocated for flags/lists
     int64_t launches = 0;
     std::string err;

@@ -1,0 +1,328 @@
+// solver.cu -- kernel (b): block-parallel fast-iterative eikonal solver.
+//
+// Replaces the reference's heap-ordered fast marching (local_fmm, F:78-155),
+// its cross-subdomain re-march (order_overlap, F:157-416) and the BSP round
+// loop with halo exchange (F:6371-6451, 6691-6892) by two device-side passes
+// over tiles of the grid:
+//
+//  1. Sweep.  Tiles are visited in wavefront order of the event's dominant
+//     propagation direction (upward from the bottom face, and along +/-theta
+//     and +/-phi as the boundary frame's gradient says): one launch per tile
+//     hyperplane, every tile's upwind neighbour tiles already done.  Inside a
+//     tile the nodes are swept as a pipelined wavefront: at step s the thread
+//     owning column (x', z') updates layer r' = s - x' - z' (swept
+//     coordinates), so each node sees its upwind neighbours' final values.
+//     Where every node's upwind neighbours lie in that octant, one sweep
+//     already gives the converged field.
+//  2. Rounds.  Every tile starts active; a work item is one (event, tile)
+//     pair from a device active list.  The tile plus 2-deep face halos (the
+//     second-order stencil reaches two nodes along each axis) are staged in
+//     shared memory; each thread owns a (theta, phi) column and sweeps it in r
+//     (upward on even passes, downward on odd ones) until a __syncthreads_or
+//     vote finds no node changed.  Changed nodes are written back and every
+//     face neighbour whose halo changed is queued for the next round (dedup by
+//     a per-tile flag).  The solve ends when a round leaves the list empty.
+//
+// Updates overwrite (T <- F(T)) with the causal octant stencil of
+// stencil.cuh.  The fixed point of that map is unique, so the converged field
+// does not depend on update order, tile shape, schedule or batch
+// composition: racing neighbour reads inside and between tiles, and the
+// sweep, only change how fast the fixed point is reached, never its bits.
+#pragma once
+#include "internal.h"
+#include "stencil.cuh"
+
+namespace fm3dt {
+
+__device__ __forceinline__ unsigned long long fbits(float v) { return __float_as_uint(v); }
+__device__ __forceinline__ unsigned long long fbits(double v) { return (unsigned long long)__double_as_longlong(v); }
+
+template <typename R, int TR, int TX, int TZ>
+struct Tile {
+    static constexpr int NT = TX * TZ;
+    static constexpr int BR = TR + 4, BX = TX + 4, BZ = TZ + 4;
+    static constexpr int SR = BX * BZ;     // shared stride of one r layer
+    static constexpr int NBOX = BR * BX * BZ;
+
+    // stage tile + face halos (edges/corners are never read by the stencil);
+    // outside the grid reads as unset
+    static __device__ void load(R *box, const R *Te, const FieldArgs<R> &a, int r0, int x0, int z0)
+    {
+        const R INF = Lim<R>::inf();
+        for (int q = threadIdx.x; q < NBOX; q += NT) {
+            const int bz = q % BZ, bx = (q / BZ) % BX, br = q / SR;
+            const int out = (bz < 2 || bz >= TZ + 2) + (bx < 2 || bx >= TX + 2) + (br < 2 || br >= TR + 2);
+            R v = INF;
+            if (out <= 1) {
+                const int gr = r0 + br - 2, gx = x0 + bx - 2, gz = z0 + bz - 2;
+                if (gr >= 0 && gr < a.nnr && gx >= 0 && gx < a.nnx && gz >= 0 && gz < a.nnz)
+                    v = __ldcg(Te + ((size_t)gr * a.nnx + gx) * a.nnz + gz);
+            }
+            box[q] = v;
+        }
+    }
+
+    // one node update from the shared box; returns the new value
+    static __device__ __forceinline__ R update(const R *box, int c, const FieldArgs<R> &a, int gr, int gx, int gz)
+    {
+        R t1[6], t2[6];
+        t1[0] = box[c - SR];     t2[0] = box[c - 2 * SR];
+        t1[1] = box[c + SR];     t2[1] = box[c + 2 * SR];
+        t1[2] = box[c - BZ];     t2[2] = box[c - 2 * BZ];
+        t1[3] = box[c + BZ];     t2[3] = box[c + 2 * BZ];
+        t1[4] = box[c - 1];      t2[4] = box[c - 2];
+        t1[5] = box[c + 1];      t2[5] = box[c + 2];
+        const unsigned inb = (gr > 0 ? 1u : 0u) | (gr < a.nnr - 1 ? 2u : 0u) | (gx > 0 ? 4u : 0u) |
+                             (gx < a.nnx - 1 ? 8u : 0u) | (gz > 0 ? 16u : 0u) | (gz < a.nnz - 1 ? 32u : 0u);
+        Spacing<R> sp;
+        sp.h[0] = a.hr;
+        sp.w[0] = a.wr;
+        sp.h[1] = __ldg(a.hx + gr);
+        sp.w[1] = __ldg(a.wx + gr);
+        const size_t q = (size_t)gr * a.nnx + gx;
+        sp.h[2] = __ldg(a.hz + q);
+        sp.w[2] = __ldg(a.wz + q);
+        const R sv = __ldg(a.s + q * a.nnz + gz);
+        return fm_update<R>(sv, t1, t2, inb, sp, a.order2);
+    }
+
+    static __device__ __forceinline__ bool frozen(const FieldArgs<R> &a, int e, int gr, int gx, int gz)
+    {
+        return gr == a.nnr - 1 && a.frozen[(size_t)e * a.nnx * a.nnz + (size_t)gx * a.nnz + gz] != 0;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Rounds (fast-iterative cleanup until the fixed point)
+// ---------------------------------------------------------------------------
+template <typename R, int TR, int TX, int TZ>
+__global__ void __launch_bounds__(TX * TZ) round_kernel(RoundArgs<R> a)
+{
+    using TL = Tile<R, TR, TX, TZ>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *box = reinterpret_cast<R *>(smem_raw);
+    __shared__ int s_face;
+    __shared__ int s_w;
+    const FieldArgs<R> &f = a.f;
+    const int tid = threadIdx.x;
+    const int tz = tid % TZ, tx = tid / TZ;
+    const int count = *((volatile const int *)a.cur_count);
+    const size_t N = (size_t)f.nnx * f.nnz * (size_t)f.nnr;
+    unsigned long long my_tiles = 0, my_nodes = 0, my_staged = 0;
+
+    for (int item = blockIdx.x; item < count; item += gridDim.x) {
+        if (tid == 0) {
+            const int w = a.cur_list[item];
+            s_w = w;
+            s_face = 0;
+            atomicExch(&a.flag[w], 0);   // later activations re-queue this tile
+            __threadfence();
+        }
+        __syncthreads();
+        const int w = s_w;
+        const int e = w / f.tiles_per_event;
+        const int t = w - e * f.tiles_per_event;
+        const int tzi = t % f.ntz;
+        const int txi = (t / f.ntz) % f.ntx;
+        const int tri = t / (f.ntz * f.ntx);
+        const int r0 = tri * TR, x0 = txi * TX, z0 = tzi * TZ;
+        R *Te = f.T + (size_t)e * N;
+        TL::load(box, Te, f, r0, x0, z0);
+
+        const int gx = x0 + tx, gz = z0 + tz;
+        const bool colv = gx < f.nnx && gz < f.nnz;
+        unsigned updm = 0;
+#pragma unroll
+        for (int r = 0; r < TR; ++r) {
+            const int gr = r0 + r;
+            if (colv && gr < f.nnr && !TL::frozen(f, e, gr, gx, gz)) updm |= 1u << r;
+        }
+        __syncthreads();
+
+        unsigned chm = 0;
+        int passes = 0;
+        bool last_changed = false;
+        const int cbase = (2 * TL::BX + (tx + 2)) * TL::BZ + (tz + 2);
+        auto node = [&](int r, bool &ch) {
+            if (!((updm >> r) & 1u)) return;
+            const int c = cbase + r * TL::SR;
+            const R nv = TL::update(box, c, f, r0 + r, gx, gz);
+            if (fbits(nv) != fbits(box[c])) {
+                box[c] = nv;
+                ch = true;
+                chm |= 1u << r;
+            }
+        };
+        for (int p = 0; p < a.max_passes; ++p) {
+            bool ch = false;
+            // r changes only shared-memory offsets and mask bits: no unrolling
+            const int k0 = (p & 1) ? 0 : TR - 1, dk = (p & 1) ? 1 : -1;
+#pragma unroll 1
+            for (int i = 0, k = k0; i < TR; ++i, k += dk) node(k, ch);
+            ++passes;
+            last_changed = __syncthreads_or(ch) != 0;
+            if (!last_changed) break;
+        }
+
+#pragma unroll
+        for (int r = 0; r < TR; ++r)
+            if ((chm >> r) & 1u)
+                Te[((size_t)(r0 + r) * f.nnx + gx) * f.nnz + gz] = box[cbase + r * TL::SR];
+
+        int fb = 0;
+        if (chm & 3u) fb |= 1;                       // read by the tile above
+        if (chm >> (TR - 2)) fb |= 2;                // read by the tile below
+        if (chm && tx < 2) fb |= 4;
+        if (chm && tx >= TX - 2) fb |= 8;
+        if (chm && tz < 2) fb |= 16;
+        if (chm && tz >= TZ - 2) fb |= 32;
+        if (fb) atomicOr(&s_face, fb);
+        __threadfence();
+        __syncthreads();
+        if (tid < 7) {
+            int fl = s_face;
+            if (tid == 6 && last_changed) fl |= 64;   // pass cap hit: run again
+            if ((fl >> tid) & 1) {
+                int nb = -1;
+                const int sl = f.ntx * f.ntz;
+                switch (tid) {
+                    case 0: nb = tri > 0 ? w - sl : -1; break;
+                    case 1: nb = tri < f.ntr - 1 ? w + sl : -1; break;
+                    case 2: nb = txi > 0 ? w - f.ntz : -1; break;
+                    case 3: nb = txi < f.ntx - 1 ? w + f.ntz : -1; break;
+                    case 4: nb = tzi > 0 ? w - 1 : -1; break;
+                    case 5: nb = tzi < f.ntz - 1 ? w + 1 : -1; break;
+                    default: nb = w; break;
+                }
+                if (nb >= 0 && atomicExch(&a.flag[nb], 1) == 0) {
+                    const int pos = atomicAdd(a.next_count, 1);
+                    a.next_list[pos] = nb;
+                }
+            }
+        }
+        if (tid == 0) {
+            const int vr = min(TR, f.nnr - r0), vx = min(TX, f.nnx - x0), vz = min(TZ, f.nnz - z0);
+            my_tiles += 1;
+            my_nodes += (unsigned long long)passes * (unsigned long long)(vr * vx * vz);
+            my_staged += (unsigned long long)(vr * vx * vz);
+        }
+        __syncthreads();
+    }
+    if (tid == 0 && my_tiles) {
+        atomicAdd(&a.stats[0], my_tiles);
+        atomicAdd(&a.stats[1], my_nodes);
+        atomicAdd(&a.stats[2], my_staged);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sweep (one launch per tile hyperplane of the event's dominant direction)
+// ---------------------------------------------------------------------------
+template <typename R, int TR, int TX, int TZ>
+__global__ void __launch_bounds__(TX * TZ) sweep_kernel(SweepArgs<R> a)
+{
+    using TL = Tile<R, TR, TX, TZ>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *box = reinterpret_cast<R *>(smem_raw);
+    const FieldArgs<R> &f = a.f;
+    const int tid = threadIdx.x;
+    const int tz = tid % TZ, tx = tid / TZ;
+    const long long count = (long long)a.hcount * a.nev;
+    const size_t N = (size_t)f.nnx * f.nnz * (size_t)f.nnr;
+    for (long long item = blockIdx.x; item < count; item += gridDim.x) {
+        const int e = (int)(item / a.hcount);
+        const int j = (int)(item - (long long)e * a.hcount);
+        const int packed = a.hp_tiles[a.hoff + j];
+        const int ap = packed >> 20, bp = (packed >> 10) & 1023, cp = packed & 1023;
+        const int dir = a.dir[e];
+        const bool sx = dir & 1, sz = (dir >> 1) & 1;
+        const int tri = f.ntr - 1 - ap;
+        const int txi = sx ? bp : f.ntx - 1 - bp;
+        const int tzi = sz ? cp : f.ntz - 1 - cp;
+        const int r0 = tri * TR, x0 = txi * TX, z0 = tzi * TZ;
+        R *Te = f.T + (size_t)e * N;
+        TL::load(box, Te, f, r0, x0, z0);
+        const int gx = x0 + tx, gz = z0 + tz;
+        const bool colv = gx < f.nnx && gz < f.nnz;
+        const int xs = sx ? tx : TX - 1 - tx;
+        const int zs = sz ? tz : TZ - 1 - tz;
+        const int cbase = (2 * TL::BX + (tx + 2)) * TL::BZ + (tz + 2);
+        __syncthreads();
+        // pipelined wavefront: layer rp (counted upward from the tile bottom)
+        // of column (xs, zs) is updated at step rp + xs + zs
+        for (int step = 0; step < TR + TX + TZ - 2; ++step) {
+            const int rp = step - xs - zs;
+            if (colv && rp >= 0 && rp < TR) {
+                const int r = TR - 1 - rp;
+                const int gr = r0 + r;
+                if (gr < f.nnr && !TL::frozen(f, e, gr, gx, gz)) {
+                    const int c = cbase + r * TL::SR;
+                    box[c] = TL::update(box, c, f, gr, gx, gz);
+                }
+            }
+            __syncthreads();
+        }
+        if (colv) {
+#pragma unroll
+            for (int r = 0; r < TR; ++r) {
+                const int gr = r0 + r;
+                if (gr < f.nnr) Te[((size_t)gr * f.nnx + gx) * f.nnz + gz] = box[cbase + r * TL::SR];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers (instantiated per precision in solver_f32.cu / solver_f64.cu)
+// ---------------------------------------------------------------------------
+template <typename R, int S>
+struct ShapeKernels {
+    static constexpr int TR = kShapes[S].tr, TX = kShapes[S].tx, TZ = kShapes[S].tz;
+    static constexpr size_t SMEM = Tile<R, TR, TX, TZ>::NBOX * sizeof(R);
+    static void setup()
+    {
+        static const bool once = [] {
+            cudaFuncSetAttribute(round_kernel<R, TR, TX, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+            cudaFuncSetAttribute(sweep_kernel<R, TR, TX, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+            return true;
+        }();
+        (void)once;
+    }
+    static void round(int grid, const RoundArgs<R> &a, cudaStream_t st)
+    {
+        setup();
+        round_kernel<R, TR, TX, TZ><<<grid, TX * TZ, SMEM, st>>>(a);
+    }
+    static void sweep(int grid, const SweepArgs<R> &a, cudaStream_t st)
+    {
+        setup();
+        sweep_kernel<R, TR, TX, TZ><<<grid, TX * TZ, SMEM, st>>>(a);
+    }
+    static int occ_round()
+    {
+        setup();
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, round_kernel<R, TR, TX, TZ>, TX * TZ, SMEM);
+        return nb;
+    }
+    static int occ_sweep()
+    {
+        setup();
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sweep_kernel<R, TR, TX, TZ>, TX * TZ, SMEM);
+        return nb;
+    }
+};
+
+#define FM_SHAPE_SWITCH(shape, CALL)      \
+    switch (shape) {                      \
+        case 0: CALL(0); break;           \
+        case 1: CALL(1); break;           \
+        case 2: CALL(2); break;           \
+        case 3: CALL(3); break;           \
+        case 4: CALL(4); break;           \
+        default: CALL(5); break;          \
+    }
+
+}  // namespace fm3dt

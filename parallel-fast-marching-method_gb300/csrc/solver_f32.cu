@@ -1,0 +1,39 @@
+// solver_f32.cu -- single-precision instantiations of the tile solver
+// kernels (sweep and rounds) for every tile shape.
+#include "solver.cuh"
+
+namespace fm3dt {
+
+void launch_round_f32(int shape, int grid, const RoundArgs<float> &a, cudaStream_t st)
+{
+#define C_(S) ShapeKernels<float, S>::round(grid, a, st)
+    FM_SHAPE_SWITCH(shape, C_)
+#undef C_
+}
+
+void launch_sweep_f32(int shape, int grid, const SweepArgs<float> &a, cudaStream_t st)
+{
+#define C_(S) ShapeKernels<float, S>::sweep(grid, a, st)
+    FM_SHAPE_SWITCH(shape, C_)
+#undef C_
+}
+
+int occupancy_round_f32(int shape)
+{
+    int r = 0;
+#define C_(S) r = ShapeKernels<float, S>::occ_round()
+    FM_SHAPE_SWITCH(shape, C_)
+#undef C_
+    return r;
+}
+
+int occupancy_sweep_f32(int shape)
+{
+    int r = 0;
+#define C_(S) r = ShapeKernels<float, S>::occ_sweep()
+    FM_SHAPE_SWITCH(shape, C_)
+#undef C_
+    return r;
+}
+
+}  // namespace fm3dt

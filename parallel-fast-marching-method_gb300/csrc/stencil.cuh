@@ -64,45 +64,66 @@ template <> FM_HD float fm_sqrt<float>(float x) {
 
 template <typename R> FM_HD R fm_min(R a, R b) { return b < a ? b : a; }
 
-// One upwind term in "first-order form": ((T - tau)/g)^2 with
-// tau = t1, g = h (first order) or tau = (4*t1 - t2)/3, g = 2h/3 (second).
-// Stored as tau relative to the octant's earliest neighbour (e), the
-// neighbour value t1 used for the causality test, and 1/g^2 (w).
-template <typename R> struct Term {
-    R t1;   // neighbour value used for the upwind test
-    R e;    // tau - reference time
-    R w;    // 1/g^2
-    R g;    // g
+// Explicit fused multiply-add.  The solver is compiled without automatic
+// contraction, so every kernel instantiation (and the host) evaluates the
+// stencil with exactly the same roundings; otherwise the compiler may fuse
+// differently per instantiation and the iteration map -- hence its fixed
+// point -- would differ in the last bits between tile shapes.
+template <typename R> FM_HD R fm_fma(R a, R b, R c);
+template <> FM_HD double fm_fma<double>(double a, double b, double c) { return __builtin_fma(a, b, c); }
+template <> FM_HD float fm_fma<float>(float a, float b, float c) { return __builtin_fmaf(a, b, c); }
+
+// Square root and quotient of the quadratic's root.  Single precision on the
+// device uses the hardware approximations (deterministic, <= 2 ulp on a
+// time increment of order 0.1-1 s, far below the float spacing of the
+// offset times themselves); double precision is IEEE-rounded.
+template <typename R> struct Fast;
+template <> struct Fast<double> {
+    static FM_HD double sqrt(double x) { return fm_sqrt<double>(x); }
+    static FM_HD double div(double a, double b) { return a / b; }
+};
+template <> struct Fast<float> {
+    static FM_HD float sqrt(float x) {
+#ifdef __CUDA_ARCH__
+        float r;
+        asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+        return r;
+#else
+        return __builtin_sqrtf(x);
+#endif
+    }
+    static FM_HD float div(float a, float b) {
+#ifdef __CUDA_ARCH__
+        return __fdividef(a, b);
+#else
+        return a / b;
+#endif
+    }
 };
 
-// solve sum_{i<n} ((x - e_i)^2 * w_i) = s2 for the larger root x
-template <typename R>
-FM_HD R solve_terms(const Term<R>* t, int n, R s, R s2)
-{
-    if (n == 1) return t[0].e + s * t[0].g;
-    R a = R(0), b = R(0), c = -s2;
-    for (int i = 0; i < n; ++i) {
-        a += t[i].w;
-        b += t[i].w * t[i].e;
-        c += t[i].w * t[i].e * t[i].e;
-    }
-    // a x^2 - 2 b x + c = 0
-    R disc = b * b - a * c;
-    if (disc < R(0)) disc = R(0);
-    return (b + fm_sqrt<R>(disc)) / a;
-}
+// Per-node grid spacings: h[a] and 1/h[a]^2 for axes r, theta, phi.
+template <typename R> struct Spacing {
+    R h[3];
+    R w[3];
+};
 
 // Neighbour directions: 0 = r-1 (up), 1 = r+1 (down), 2 = x-1, 3 = x+1,
 // 4 = z-1, 5 = z+1.
 //
 // t1[d]: neighbour value (+inf if unset; ignored when bit d of inb is clear)
 // t2[d]: second neighbour value (+inf if unset or outside the grid)
-// h[a]:  grid spacing of axis a (r, x, z) at the centre node, km
+// sp:    spacings at the centre node
 // s:     slowness at the centre node
 // order2: 1 for the mixed-order scheme (fom=1), 0 for first order (fom=0)
 // Returns the candidate time (+inf when no neighbour is set).
+//
+// Each direction is written in first-order form ((T - tau)/g)^2 with
+// tau = t1, g = h (first order) or tau = t1 + (t1 - t2)/3, g = 2h/3 (second
+// order, the same equation as the reference's (3T - 4 t1 + t2)/(2h) term),
+// relative to tmin, the earliest in-grid neighbour.  Every octant sorts its
+// three terms by t1 and adds them while t1 < T (the causal solve).
 template <typename R>
-FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const R h[3], int order2)
+FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing<R> &sp, int order2)
 {
     const R INF = Lim<R>::inf();
     R tmin = INF;
@@ -111,38 +132,47 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const R h[3],
         if ((inb >> d) & 1u) tmin = fm_min(tmin, t1[d]);
     if (!(tmin < INF)) return INF;
     const R s2 = s * s;
-    // per-direction terms relative to tmin
-    Term<R> dir[6];
+    R key[6], e[6], g[6], w[6];
 #pragma unroll
     for (int d = 0; d < 6; ++d) {
-        const R hh = h[d >> 1];
+        const int a = d >> 1;
         const bool o2 = order2 && (t2[d] < t1[d]);
-        dir[d].t1 = ((inb >> d) & 1u) ? t1[d] : INF;
-        if (o2) {
-            dir[d].e = (t1[d] - tmin) + (t1[d] - t2[d]) / R(3);
-            dir[d].g = hh * R(2) / R(3);
-        } else {
-            dir[d].e = t1[d] - tmin;
-            dir[d].g = hh;
-        }
-        dir[d].w = R(1) / (dir[d].g * dir[d].g);
+        const R dt = t1[d] - tmin;
+        key[d] = ((inb >> d) & 1u) ? dt : INF;
+        e[d] = o2 ? fm_fma<R>(t1[d] - t2[d], R(1.0 / 3.0), dt) : dt;
+        g[d] = o2 ? sp.h[a] * R(2.0 / 3.0) : sp.h[a];
+        w[d] = o2 ? sp.w[a] * R(2.25) : sp.w[a];
     }
     R best = INF;
 #pragma unroll
     for (int o = 0; o < 8; ++o) {
         const int dr = (o >> 2) & 1, dx = 2 + ((o >> 1) & 1), dz = 4 + (o & 1);
-        const bool inside = ((inb >> dr) & 1u) && ((inb >> dx) & 1u) && ((inb >> dz) & 1u);
-        if (!inside) continue;
-        Term<R> t[3] = {dir[dr], dir[dx], dir[dz]};
-        // ascending t1 (unset neighbours sort last)
-        if (t[1].t1 < t[0].t1) { Term<R> q = t[0]; t[0] = t[1]; t[1] = q; }
-        if (t[2].t1 < t[1].t1) { Term<R> q = t[1]; t[1] = t[2]; t[2] = q; }
-        if (t[1].t1 < t[0].t1) { Term<R> q = t[0]; t[0] = t[1]; t[1] = q; }
-        if (!(t[0].t1 < INF)) continue;
-        R x = solve_terms<R>(t, 1, s, s2);
-        if (t[1].t1 - tmin < x) {
-            x = solve_terms<R>(t, 2, s, s2);
-            if (t[2].t1 - tmin < x) x = solve_terms<R>(t, 3, s, s2);
+        if (!(((inb >> dr) & (inb >> dx) & (inb >> dz)) & 1u)) continue;
+        R k0 = key[dr], e0 = e[dr], g0 = g[dr], w0 = w[dr];
+        R k1 = key[dx], e1 = e[dx], g1 = g[dx], w1 = w[dx];
+        R k2 = key[dz], e2 = e[dz], g2 = g[dz], w2 = w[dz];
+#define FM_SWAP(a, b) { R q_ = a; a = b; b = q_; }
+        if (k1 < k0) { FM_SWAP(k0, k1) FM_SWAP(e0, e1) FM_SWAP(g0, g1) FM_SWAP(w0, w1) }
+        if (k2 < k1) { FM_SWAP(k1, k2) FM_SWAP(e1, e2) FM_SWAP(g1, g2) FM_SWAP(w1, w2) }
+        if (k1 < k0) { FM_SWAP(k0, k1) FM_SWAP(e0, e1) FM_SWAP(g0, g1) FM_SWAP(w0, w1) }
+#undef FM_SWAP
+        if (!(k0 < INF)) continue;
+        R x = fm_fma<R>(s, g0, e0);
+        if (k1 < x) {
+            R a = w0 + w1;
+            const R we0 = w0 * e0, we1 = w1 * e1;
+            R b = we0 + we1;
+            R c = fm_fma<R>(we0, e0, fm_fma<R>(we1, e1, -s2));
+            R disc = fm_fma<R>(b, b, -(a * c));
+            x = Fast<R>::div(b + Fast<R>::sqrt(disc > R(0) ? disc : R(0)), a);
+            if (k2 < x) {
+                const R we2 = w2 * e2;
+                a += w2;
+                b += we2;
+                c = fm_fma<R>(we2, e2, c);
+                disc = fm_fma<R>(b, b, -(a * c));
+                x = Fast<R>::div(b + Fast<R>::sqrt(disc > R(0) ? disc : R(0)), a);
+            }
         }
         best = fm_min(best, x);
     }

@@ -46,14 +46,16 @@ class GridDesc(C.Structure):
 class Status(C.Structure):
     _fields_ = [("rounds", C.c_int), ("converged", C.c_int), ("tile_updates", C.c_int64),
                 ("node_passes", C.c_int64), ("tile_nodes", C.c_int64), ("ms", C.c_double),
-                ("round_ms", C.c_double), ("round_launches", C.c_int)]
+                ("round_ms", C.c_double), ("round_launches", C.c_int), ("sweep_launches", C.c_int),
+                ("sweep_ms", C.c_double), ("sweep_nodes", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 EXPORTS = [
-    "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_planewave",
+    "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_resume",
+    "fm3dt_solve_planewave",
     "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
     "fm3dt_set_tuning", "fm3dt_tile_shapes", "fm3dt_tile_shape", "fm3dt_launch_count",
     "fm3dt_last_error", "fm3dt_ctx_destroy",
@@ -78,13 +80,14 @@ def load(path: str | None = None):
     L.fm3dt_solve.argtypes = [vp, C.c_int, dp, C.POINTER(Status)]
     L.fm3dt_solve_planewave.argtypes = [vp, C.c_int, dp, C.POINTER(Status)]
     L.fm3dt_solve_device.argtypes = [vp, C.c_int, C.c_void_p, C.POINTER(Status)]
+    L.fm3dt_solve_resume.argtypes = [vp, C.POINTER(Status)]
     L.fm3dt_receiver_times.argtypes = [vp, C.c_int, dp, dp, dp, C.POINTER(C.c_float)]
     L.fm3dt_rays_frechet.argtypes = [vp, C.c_int, dp, dp, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                      C.POINTER(C.c_float), C.c_int64, dp]
     L.fm3dt_get_times.argtypes = [vp, C.c_int, dp]
     L.fm3dt_set_times.argtypes = [vp, C.c_int, C.c_int, dp]
     L.fm3dt_get_velocity.argtypes = [vp, dp]
-    L.fm3dt_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    L.fm3dt_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
     L.fm3dt_tile_shapes.argtypes = [C.POINTER(C.c_int)]
     L.fm3dt_tile_shape.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.fm3dt_launch_count.argtypes = [vp]
@@ -188,8 +191,8 @@ class Solver:
     def launch_count(self) -> int:
         return int(self._L.fm3dt_launch_count(self._ctx))
 
-    def set_tuning(self, shape: int = 0, max_passes: int = 0, max_rounds: int = 0):
-        self._check(self._L.fm3dt_set_tuning(self._ctx, int(shape), int(max_passes), int(max_rounds)))
+    def set_tuning(self, shape: int = 0, max_passes: int = 0, max_rounds: int = 0, sweep: int = -1):
+        self._check(self._L.fm3dt_set_tuning(self._ctx, int(shape), int(max_passes), int(max_rounds), int(sweep)))
 
     def set_velocity(self, velv):
         velv = np.ascontiguousarray(velv, dtype=np.float64)
@@ -206,6 +209,13 @@ class Solver:
         st = Status()
         self._check(self._L.fm3dt_solve(self._ctx, nev, _d(frames), C.byref(st)))
         self.nev = nev
+        return st.as_dict()
+
+    def solve_resume(self) -> dict:
+        """Continue the rounds from the current fields (fixed-point check or
+        warm start)."""
+        st = Status()
+        self._check(self._L.fm3dt_solve_resume(self._ctx, C.byref(st)))
         return st.as_dict()
 
     def solve_ptr(self, nev: int, frames_ptr: int, device: bool) -> dict:

@@ -25,7 +25,8 @@ SOURCES = {
     "boundary.cu": ["-fmad=false"],
     "receivers.cu": ["-fmad=false"],
     "rays.cu": ["-fmad=false"],
-    "solver.cu": [],
+    "solver_f32.cu": ["-fmad=false"],
+    "solver_f64.cu": ["-fmad=false"],
     "capi.cu": [],
 }
 

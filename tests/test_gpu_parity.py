@@ -3,12 +3,15 @@
 Tolerances (stated per test):
 * gridder, plane-wave frames, receiver interpolation: bit-exact (same double
   precision operation order, no FMA contraction in those kernels);
+* solver vs the oracle's fixed point of the reference's octant formulas:
+  1e-9 s everywhere (any model, any boundary frame, both orders);
 * solver, first order: the iterative fixed point equals the fast-marching
   result to 1e-9 s;
 * solver, mixed order: receiver times within 1e-5 relative and 1 ms absolute
-  (the spec bar); field within 5 ms everywhere and 1e-6 s at 99.9% of
-  nodes (fast marching keeps a few sticky intermediate minima on rough
-  models that the fixed point does not);
+  (the spec bar); field within 5 ms everywhere and within 1e-6 s at 95%
+  of nodes (on rough models fast marching keeps a few sticky intermediate
+  minima that the fixed point does not: ~2% of nodes of the slab model by up
+  to 2.7 ms; smooth models agree to 1e-12 s);
 * single-precision offset mode vs double: receiver times within 1e-5 relative
   and 1 ms;
 * rays through an identical field: endpoints within 1e-9 rad / 1e-6 km and
@@ -93,7 +96,7 @@ def test_solve_fp64_matches_fast_marching(gpu_lib, orc, cfg, scale, event):
         trr = s.receiver_times(w.rec_elev, rcx, rcz)[0].astype(np.float64)
     d = np.abs(got - refs[0])
     assert d.max() < 5e-3
-    assert np.quantile(d, 0.999) < 1e-6
+    assert np.mean(d > 1e-6) < 0.05
     ref_trr = orc.srtimes(g, refs[0], w.rec_elev, rcx, rcz).astype(np.float64)
     assert np.max(np.abs(trr - ref_trr)) <= 1e-3
     assert np.max(np.abs(trr - ref_trr) / ref_trr) <= 1e-5
@@ -128,24 +131,32 @@ def test_host_frames_equal_planewave(gpu_lib, orc):
         assert np.array_equal(x, y)
 
 
-def test_unset_boundary_values(gpu_lib, orc):
-    """Boundary values <= 0 mean "no time" (F:6935-6936): those bottom nodes
-    are solved like any other node."""
+@pytest.mark.parametrize("cfg,scale,event,holes,fom", [
+    (0, 22, (60.0, 45.0), 0.0, 1), (2, 26, (50.0, 100.0), 0.0, 1), (3, 24, (45.0, 270.0), 0.0, 1),
+    (1, 27, (75.0, 10.0), 0.0, 0), (0, 22, (60.0, 45.0), 0.2, 1), (2, 30, (50.0, 100.0), 0.05, 0)])
+def test_solve_equals_fixed_point_of_reference_stencil(gpu_lib, orc, cfg, scale, event, holes, fom):
+    """Against the oracle's fixed point of the reference's own octant formulas
+    (order independent), the GPU field agrees to 1e-9 s everywhere, including
+    rough models, first order, and boundary frames with unset values (<= 0,
+    "no time", F:6935-6936) where the heap order of fast marching is not
+    causal."""
     import fm3dt
-    w = _setup(0, 22)
+    w = _setup(cfg, scale, events=[event])
     params = _params(w)
-    g, veln, _ = _oracle_solve(orc, w, params[:0])
+    g = _oracle_grid(orc, w.header)
+    veln, _ = orc.gridder(g, w.velv)
     fr = orc.planewave_frame(g, orc.PlaneWave(*params[0]))
     rng = np.random.default_rng(5)
-    fr[rng.uniform(size=fr.size) < 0.2] = 0.0
-    fr[:5] = -1.0
-    ref, _ = orc.fmm(g, veln, fr, 1)
-    with fm3dt.Solver(w.header) as s:
+    fr[rng.uniform(size=fr.size) < holes] = 0.0
+    if holes:
+        fr[:5] = -1.0
+    ref, _ = orc.fixed_point(g, veln, fr, fom)
+    with fm3dt.Solver(w.header, fom=fom) as s:
         s.set_velocity(w.velv)
-        s.solve(fr[None, :])
+        st = s.solve(fr[None, :])
+        assert st["converged"] == 1
         got = s.get_times(0)
-    assert np.max(np.abs(got - ref)) < 5e-3
-    assert np.quantile(np.abs(got - ref), 0.999) < 1e-6
+    assert np.max(np.abs(got - ref)) < 1e-9
 
 
 @pytest.mark.parametrize("prec", [0, 1])
@@ -164,23 +175,26 @@ def test_batch_equals_alone_bitwise(gpu_lib, prec):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-def test_tile_shapes_bitwise(gpu_lib, prec):
-    """The fixed point does not depend on the tile shape or schedule."""
+def test_tile_shapes_and_sweep_bitwise(gpu_lib, prec):
+    """The fixed point does not depend on the tile shape, the pass cap, the
+    directional sweep or the schedule."""
     import fm3dt
-    w = _setup(2, 30, nev=2)
+    w = _setup(2, 30, nev=3)
     params = _params(w)
     ref = None
-    with fm3dt.Solver(w.header, precision=prec, max_events=2) as s:
+    with fm3dt.Solver(w.header, precision=prec, max_events=3) as s:
         s.set_velocity(w.velv)
         for shape in range(len(fm3dt.tile_shapes())):
-            s.set_tuning(shape)
-            st = s.solve_planewave(params)
-            assert st["converged"] == 1
-            out = np.concatenate([s.get_times(e) for e in range(2)])
-            if ref is None:
-                ref = out
-            else:
-                assert np.array_equal(out, ref), f"shape {shape}"
+            for sweep, cap in ((1, 64), (0, 16), (1, 3)):
+                s.set_tuning(shape, cap, 0, sweep)
+                st = s.solve_planewave(params)
+                assert st["converged"] == 1
+                assert (st["sweep_launches"] > 0) == bool(sweep)
+                out = np.concatenate([s.get_times(e) for e in range(3)])
+                if ref is None:
+                    ref = out
+                else:
+                    assert np.array_equal(out, ref), f"shape {shape} sweep {sweep} cap {cap}"
 
 
 def test_fp32_offset_within_tolerance(gpu_lib):
