@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--prec", choices=["f32", "f64"], default="f32")
     ap.add_argument("--shape", type=int, default=-1, help="tile shape index (-1: autotune)")
     ap.add_argument("--passes", type=int, default=0)
+    ap.add_argument("--sweep-shape", type=int, default=-1, help="sweep tile shape index (-1: same as --shape)")
     ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline, FP64 check and e2e leg")
     return ap.parse_args()
 
@@ -257,11 +258,14 @@ def run_ours(a):
     fptr = d_frames.data_ptr()
 
     if a.shape >= 0:
-        solver.set_tuning(a.shape, a.passes or 64)
-        tuned = (a.shape, a.passes or 64, None)
+        sweep_shape = a.sweep_shape if a.sweep_shape >= 0 else a.shape
+        solver.set_tuning(a.shape, a.passes or 64, 0, 1)
+        solver.set_sweep_shape(sweep_shape)
+        tuned = (a.shape, a.passes or 64, sweep_shape, None)
     else:
         tuned = autotune.autotune(solver, fptr, nev, device=True)
     shape = fm3dt.tile_shapes()[tuned[0]]
+    sweep_shape_dims = fm3dt.tile_shapes()[tuned[2]]
 
     for _ in range(a.warmup):
         solver.solve_ptr(nev, fptr, True)
@@ -277,6 +281,8 @@ def run_ours(a):
     wall = time.perf_counter() - t0
     d.barrier()
     launches = solver.launch_count - l0
+    tt, tu = solver.round_trace()
+    trace_tiles, trace_updates = [int(x) for x in tt], [int(x) for x in tu]
     clk = clocks.stop() if clocks else None
     dev_ms = sum(s["ms"] for s in sts)
     step_s = max(wall, dev_ms / 1000.0)
@@ -350,6 +356,7 @@ def run_ours(a):
                                f"{len(rcr)} receivers, {'FP32 offset' if a.prec == 'f32' else 'FP64'} stencils",
                    "grid": [nnr, nnx, nnz], "events_per_gpu": nev, "receivers": len(rcr),
                    "tile_shape": list(shape), "max_passes": tuned[1],
+                   "sweep_tile_shape": list(sweep_shape_dims),
                    "l2": "inputs larger than L2 (traveltime fields %.1f GB per step)" %
                          (nev * nnr * nnx * nnz * (4 if a.prec == 'f32' else 8) / 1e9)},
         "p50_ms": p50, "p99_ms": p99,
@@ -365,7 +372,8 @@ def run_ours(a):
                    "staged_nodes_per_solve": staged / a.steps, "device_ms_per_step": dev_ms / a.steps,
                    "round_ms_per_step": round_ms / a.steps, "sweep_ms_per_step": sweep_ms / a.steps,
                    "sweep_launches_per_step": sweep_launches / a.steps,
-                   "kernel_shares": {k: v[0] / max(1e-9, dev_ms) for k, v in kernels.items()}},
+                   "kernel_shares": {k: v[0] / max(1e-9, dev_ms) for k, v in kernels.items()},
+                   "round_trace_tiles": trace_tiles, "round_trace_updates": trace_updates},
     }
     line.update(extras)
     if clk:

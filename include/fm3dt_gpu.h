@@ -155,6 +155,14 @@ int fm3dt_set_times(fm3dt_ctx *ctx, int event, int nev_total, const double *ttn)
  * -1 keep).  None of these changes the converged field. */
 int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rounds, int sweep);
 
+/* Tile shape of the directional sweep (independent of the rounds' shape). */
+int fm3dt_set_sweep_shape(fm3dt_ctx *ctx, int tile_shape);
+
+/* Per-round trace of the last solve: tiles processed and node updates of
+ * each round (up to cap rounds).  Returns the number of rounds, or a negative
+ * error. */
+int fm3dt_round_trace(fm3dt_ctx *ctx, int cap, int64_t *tiles, int64_t *updates);
+
 /* Number of available tile shapes and the shape (TR, TX, TZ) of one. */
 int fm3dt_tile_shapes(int *count);
 int fm3dt_tile_shape(int index, int *tr, int *tx, int *tz);

@@ -207,19 +207,31 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, bool resume = false)
     int sweep_launches = 0;
     CK(cudaEventRecord(sw0, s));
     if (do_sweep) {
-        int rc = ensure_planes(ctx, shape);
+        const int sshape = ctx->sweep_shape;
+        int rc = ensure_planes(ctx, sshape);
         if (rc) return rc;
-        const auto &P = ctx->planes[shape];
-        const int sgrid = std::max(1, sweep_blocks_per_sm(shape, ctx->prec)) * sm_count();
+        const auto &P = ctx->planes[sshape];
+        const int sgrid = std::max(1, sweep_blocks_per_sm(sshape, ctx->prec)) * sm_count();
+        // the sweep tiles the grid with its own shape
+        FieldArgs<double> s64 = f64;
+        FieldArgs<float> s32 = f32;
+        {
+            int a, b, c;
+            const int t = tiles_per_event(g, sshape, &a, &b, &c);
+            s64.ntr = s32.ntr = a;
+            s64.ntx = s32.ntx = b;
+            s64.ntz = s32.ntz = c;
+            s64.tiles_per_event = s32.tiles_per_event = t;
+        }
         for (size_t h = 0; h < P.off.size(); ++h) {
             const long long items = (long long)P.cnt[h] * nev;
             const int grid = (int)std::min<long long>(items, sgrid);
             if (ctx->prec == FM3DT_FP64) {
-                SweepArgs<double> a{f64, P.d_tiles, P.off[h], P.cnt[h], ctx->d_dir, nev};
-                launch_sweep_f64(shape, grid, a, s);
+                SweepArgs<double> a{s64, P.d_tiles, P.off[h], P.cnt[h], ctx->d_dir, nev};
+                launch_sweep_f64(sshape, grid, a, s);
             } else {
-                SweepArgs<float> a{f32, P.d_tiles, P.off[h], P.cnt[h], ctx->d_dir, nev};
-                launch_sweep_f32(shape, grid, a, s);
+                SweepArgs<float> a{s32, P.d_tiles, P.off[h], P.cnt[h], ctx->d_dir, nev};
+                launch_sweep_f32(sshape, grid, a, s);
             }
             ++sweep_launches;
         }
@@ -236,6 +248,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, bool resume = false)
     CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
     CK(cudaMemsetAsync(ctx->d_count[1], 0, sizeof(int), s));
     CK(cudaMemsetAsync(ctx->d_stats, 0, 3 * sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(ctx->d_trace, 0, 2 * sizeof(unsigned long long) * fm3dt_ctx::kTraceRounds, s));
     launch_initial_tiles(nev, tpe, first, cnt, ctx->d_list[0], ctx->d_count[0], ctx->d_flag, s);
     ctx->launches += 1;
     CKL();
@@ -268,10 +281,14 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, bool resume = false)
             CK(cudaMemsetAsync(ctx->d_count[nxt], 0, sizeof(int), s));
             CK(cudaEventRecord(ctx->round_events[2 * k], s));
             if (ctx->prec == FM3DT_FP64) {
+                a64.trace = rounds < fm3dt_ctx::kTraceRounds ? ctx->d_trace : nullptr;
+                a64.round = rounds;
                 a64.cur_list = ctx->d_list[cur]; a64.cur_count = ctx->d_count[cur];
                 a64.next_list = ctx->d_list[nxt]; a64.next_count = ctx->d_count[nxt];
                 launch_round_f64(shape, grid, a64, s);
             } else {
+                a32.trace = rounds < fm3dt_ctx::kTraceRounds ? ctx->d_trace : nullptr;
+                a32.round = rounds;
                 a32.cur_list = ctx->d_list[cur]; a32.cur_count = ctx->d_count[cur];
                 a32.next_list = ctx->d_list[nxt]; a32.next_count = ctx->d_count[nxt];
                 launch_round_f32(shape, grid, a32, s);
@@ -303,6 +320,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, bool resume = false)
     cudaEventDestroy(sw0);
     cudaEventDestroy(sw1);
     ctx->nev_solved = nev;
+    ctx->last_rounds = rounds;
     if (st) {
         st->rounds = rounds;
         st->converged = done ? 1 : 0;
@@ -403,6 +421,7 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMalloc(&ctx->d_count[0], sizeof(int)));
     CKC(cudaMalloc(&ctx->d_count[1], sizeof(int)));
     CKC(cudaMalloc(&ctx->d_stats, 3 * sizeof(unsigned long long)));
+    CKC(cudaMalloc(&ctx->d_trace, 2 * sizeof(unsigned long long) * fm3dt_ctx::kTraceRounds));
     CKC(cudaMalloc(&ctx->d_params, 4 * ctx->maxev * sizeof(double)));
     CKC(cudaMallocHost(&ctx->h_count, sizeof(int)));
     CKC(cudaMallocHost(&ctx->h_stats, 3 * sizeof(unsigned long long)));
@@ -684,6 +703,29 @@ int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rou
     return FM3DT_OK;
 }
 
+int fm3dt_set_sweep_shape(fm3dt_ctx *ctx, int tile_shape)
+{
+    if (!ctx) return FM3DT_EINVAL;
+    if (tile_shape < 0 || tile_shape >= kNumShapes) return fail(ctx, FM3DT_EINVAL, "tile shape out of range");
+    ctx->sweep_shape = tile_shape;
+    return FM3DT_OK;
+}
+
+int fm3dt_round_trace(fm3dt_ctx *ctx, int cap, int64_t *tiles, int64_t *updates)
+{
+    if (!ctx || cap < 0) return FM3DT_EINVAL;
+    const int n = std::min(std::min(cap, ctx->last_rounds), fm3dt_ctx::kTraceRounds);
+    if (n > 0 && tiles && updates) {
+        std::vector<unsigned long long> h(2 * (size_t)n);
+        CK(cudaMemcpy(h.data(), ctx->d_trace, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < n; ++i) {
+            tiles[i] = (int64_t)h[2 * i];
+            updates[i] = (int64_t)h[2 * i + 1];
+        }
+    }
+    return ctx->last_rounds;
+}
+
 int fm3dt_tile_shapes(int *count)
 {
     if (!count) return FM3DT_EINVAL;
@@ -729,6 +771,7 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_count[0]);
     cudaFree(ctx->d_count[1]);
     cudaFree(ctx->d_stats);
+    cudaFree(ctx->d_trace);
     cudaFree(ctx->d_params);
     if (ctx->h_count) cudaFreeHost(ctx->h_count);
     if (ctx->h_stats) cudaFreeHost(ctx->h_stats);

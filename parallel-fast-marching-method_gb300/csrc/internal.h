@@ -52,6 +52,8 @@ struct RoundArgs {
     int *next_count;
     int max_passes;
     unsigned long long *stats;  // [0] tiles processed, [1] node updates, [2] staged nodes
+    unsigned long long *trace;  // per round: [2*round] tiles, [2*round+1] node updates (or null)
+    int round;
 };
 
 // Arguments of one sweep launch (one tile hyperplane).
@@ -162,6 +164,10 @@ struct fm3dt_ctx {
     int max_passes = 64;
     int max_rounds = 0;           // 0 = automatic
     int sweep = 1;                // directional sweep before the rounds
+    int sweep_shape = 4;          // tile shape of the sweep (independent of the rounds')
+    unsigned long long *d_trace = nullptr;   // per-round tiles / node updates
+    static constexpr int kTraceRounds = 8192;
+    int last_rounds = 0;
     // tile hyperplanes of each shape (device list + host offsets)
     struct Planes { int shape = -1; int *d_tiles = nullptr; std::vector<int> off, cnt; };
     Planes planes[fm3dt::kNumShapes];

@@ -103,12 +103,15 @@ __global__ void __launch_bounds__(TX * TZ) round_kernel(RoundArgs<R> a)
     R *box = reinterpret_cast<R *>(smem_raw);
     __shared__ int s_face;
     __shared__ int s_w;
+    __shared__ unsigned s_chg[2][TX * TZ];        // per column: nodes changed in a pass
+    __shared__ unsigned long long s_upd;
     const FieldArgs<R> &f = a.f;
     const int tid = threadIdx.x;
     const int tz = tid % TZ, tx = tid / TZ;
     const int count = *((volatile const int *)a.cur_count);
     const size_t N = (size_t)f.nnx * f.nnz * (size_t)f.nnr;
-    unsigned long long my_tiles = 0, my_nodes = 0, my_staged = 0;
+    unsigned long long my_tiles = 0, my_staged = 0, my_upd = 0;
+    if (tid == 0) s_upd = 0;
 
     for (int item = blockIdx.x; item < count; item += gridDim.x) {
         if (tid == 0) {
@@ -139,29 +142,44 @@ __global__ void __launch_bounds__(TX * TZ) round_kernel(RoundArgs<R> a)
         }
         __syncthreads();
 
+        // Passes.  The first recomputes every node; later ones only the nodes
+        // with a stencil neighbour (+-1, +-2 along each axis) that changed in
+        // the previous pass -- a node's update never reads its own value, so
+        // nothing else can change.
         unsigned chm = 0;
-        int passes = 0;
         bool last_changed = false;
         const int cbase = (2 * TL::BX + (tx + 2)) * TL::BZ + (tz + 2);
-        auto node = [&](int r, bool &ch) {
-            if (!((updm >> r) & 1u)) return;
-            const int c = cbase + r * TL::SR;
-            const R nv = TL::update(box, c, f, r0 + r, gx, gz);
-            if (fbits(nv) != fbits(box[c])) {
-                box[c] = nv;
-                ch = true;
-                chm |= 1u << r;
-            }
-        };
+        unsigned dirty = updm;
         for (int p = 0; p < a.max_passes; ++p) {
-            bool ch = false;
+            unsigned pch = 0;
             // r changes only shared-memory offsets and mask bits: no unrolling
             const int k0 = (p & 1) ? 0 : TR - 1, dk = (p & 1) ? 1 : -1;
 #pragma unroll 1
-            for (int i = 0, k = k0; i < TR; ++i, k += dk) node(k, ch);
-            ++passes;
-            last_changed = __syncthreads_or(ch) != 0;
+            for (int i = 0, k = k0; i < TR; ++i, k += dk) {
+                if (!((dirty >> k) & 1u)) continue;
+                const int c = cbase + k * TL::SR;
+                const R nv = TL::update(box, c, f, r0 + k, gx, gz);
+                ++my_upd;
+                if (fbits(nv) != fbits(box[c])) {
+                    box[c] = nv;
+                    pch |= 1u << k;
+                }
+            }
+            chm |= pch;
+            s_chg[p & 1][tid] = pch;
+            last_changed = __syncthreads_or(pch != 0) != 0;
             if (!last_changed) break;
+            const unsigned *q = s_chg[p & 1];
+            unsigned lat = 0;
+            if (tx > 0) lat |= q[tid - TZ];
+            if (tx > 1) lat |= q[tid - 2 * TZ];
+            if (tx < TX - 1) lat |= q[tid + TZ];
+            if (tx < TX - 2) lat |= q[tid + 2 * TZ];
+            if (tz > 0) lat |= q[tid - 1];
+            if (tz > 1) lat |= q[tid - 2];
+            if (tz < TZ - 1) lat |= q[tid + 1];
+            if (tz < TZ - 2) lat |= q[tid + 2];
+            dirty = (lat | (pch << 1) | (pch >> 1) | (pch << 2) | (pch >> 2)) & updm;
         }
 
 #pragma unroll
@@ -203,15 +221,20 @@ __global__ void __launch_bounds__(TX * TZ) round_kernel(RoundArgs<R> a)
         if (tid == 0) {
             const int vr = min(TR, f.nnr - r0), vx = min(TX, f.nnx - x0), vz = min(TZ, f.nnz - z0);
             my_tiles += 1;
-            my_nodes += (unsigned long long)passes * (unsigned long long)(vr * vx * vz);
             my_staged += (unsigned long long)(vr * vx * vz);
         }
         __syncthreads();
     }
+    if (my_upd) atomicAdd(&s_upd, my_upd);
+    __syncthreads();
     if (tid == 0 && my_tiles) {
         atomicAdd(&a.stats[0], my_tiles);
-        atomicAdd(&a.stats[1], my_nodes);
+        atomicAdd(&a.stats[1], s_upd);
         atomicAdd(&a.stats[2], my_staged);
+        if (a.trace) {
+            atomicAdd(&a.trace[2 * a.round], my_tiles);
+            atomicAdd(&a.trace[2 * a.round + 1], s_upd);
+        }
     }
 }
 

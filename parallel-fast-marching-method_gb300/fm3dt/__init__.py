@@ -57,7 +57,8 @@ EXPORTS = [
     "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_resume",
     "fm3dt_solve_planewave",
     "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
-    "fm3dt_set_tuning", "fm3dt_tile_shapes", "fm3dt_tile_shape", "fm3dt_launch_count",
+    "fm3dt_set_tuning", "fm3dt_set_sweep_shape", "fm3dt_round_trace", "fm3dt_tile_shapes", "fm3dt_tile_shape",
+    "fm3dt_launch_count",
     "fm3dt_last_error", "fm3dt_ctx_destroy",
 ]
 
@@ -88,6 +89,8 @@ def load(path: str | None = None):
     L.fm3dt_set_times.argtypes = [vp, C.c_int, C.c_int, dp]
     L.fm3dt_get_velocity.argtypes = [vp, dp]
     L.fm3dt_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.fm3dt_set_sweep_shape.argtypes = [vp, C.c_int]
+    L.fm3dt_round_trace.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.fm3dt_tile_shapes.argtypes = [C.POINTER(C.c_int)]
     L.fm3dt_tile_shape.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.fm3dt_launch_count.argtypes = [vp]
@@ -193,6 +196,20 @@ class Solver:
 
     def set_tuning(self, shape: int = 0, max_passes: int = 0, max_rounds: int = 0, sweep: int = -1):
         self._check(self._L.fm3dt_set_tuning(self._ctx, int(shape), int(max_passes), int(max_rounds), int(sweep)))
+
+    def set_sweep_shape(self, shape: int):
+        self._check(self._L.fm3dt_set_sweep_shape(self._ctx, int(shape)))
+
+    def round_trace(self, cap: int = 8192):
+        """(tiles, node updates) per round of the last solve."""
+        t = np.zeros(cap, dtype=np.int64)
+        u = np.zeros(cap, dtype=np.int64)
+        n = self._L.fm3dt_round_trace(self._ctx, cap, t.ctypes.data_as(C.POINTER(C.c_int64)),
+                                      u.ctypes.data_as(C.POINTER(C.c_int64)))
+        if n < 0:
+            self._check(n)
+        n = min(n, cap)
+        return t[:n], u[:n]
 
     def set_velocity(self, velv):
         velv = np.ascontiguousarray(velv, dtype=np.float64)

@@ -1,13 +1,12 @@
-"""Autotuner of the tile-round solver.
+"""Autotuner of the tile solver.
 
-Times a sample batch for every tile shape (r x theta x phi extents, which
-also fixes the CTA size: one thread per column) and a few in-tile pass caps,
-then keeps the fastest on the solver.  The converged field does not depend on
-the choice (the fixed point is unique), so tuning never changes results.
+Tunes, on a sample batch, (1) the tile shape of the directional sweep and
+(2) the tile shape and in-tile pass cap of the fast-iterative rounds (the
+shape also fixes the CTA size: one thread per column), keeping the fastest
+device time.  The converged field does not depend on any of these choices
+(the fixed point is unique), so tuning never changes results.
 """
 from __future__ import annotations
-
-import time
 
 import numpy as np
 
@@ -16,19 +15,29 @@ from . import tile_shapes
 PASS_CAPS = (16, 64)
 
 
+def _time(solver, frames_ptr, nev, device, repeats):
+    solver.solve_ptr(nev, frames_ptr, device)       # warm
+    return float(np.median([solver.solve_ptr(nev, frames_ptr, device)["ms"] for _ in range(repeats)]))
+
+
 def autotune(solver, frames_ptr: int, nev: int, device: bool = True, repeats: int = 1):
-    """Returns (shape_index, max_passes, ms) and applies the best setting."""
+    """Returns (round_shape, max_passes, sweep_shape, ms) and applies it."""
+    nshapes = len(tile_shapes())
+    round_shape, cap = 0, PASS_CAPS[0]
+    solver.set_tuning(round_shape, cap, 0, 1)
+    best_sweep = None
+    for sshape in range(nshapes):
+        solver.set_sweep_shape(sshape)
+        ms = _time(solver, frames_ptr, nev, device, repeats)
+        if best_sweep is None or ms < best_sweep[1]:
+            best_sweep = (sshape, ms)
+    solver.set_sweep_shape(best_sweep[0])
     best = None
-    for shape in range(len(tile_shapes())):
-        for cap in PASS_CAPS:
-            solver.set_tuning(shape, cap)
-            solver.solve_ptr(nev, frames_ptr, device)       # warm
-            ms = []
-            for _ in range(repeats):
-                st = solver.solve_ptr(nev, frames_ptr, device)
-                ms.append(st["ms"])
-            m = float(np.median(ms))
-            if best is None or m < best[2]:
-                best = (shape, cap, m)
-    solver.set_tuning(best[0], best[1])
-    return best
+    for shape in range(nshapes):
+        for c in PASS_CAPS:
+            solver.set_tuning(shape, c, 0, 1)
+            ms = _time(solver, frames_ptr, nev, device, repeats)
+            if best is None or ms < best[2]:
+                best = (shape, c, ms)
+    solver.set_tuning(best[0], best[1], 0, 1)
+    return best[0], best[1], best_sweep[0], best[2]
