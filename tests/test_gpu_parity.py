@@ -197,6 +197,23 @@ def test_tile_shapes_and_sweep_bitwise(gpu_lib, prec):
                     assert np.array_equal(out, ref), f"shape {shape} sweep {sweep} cap {cap}"
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+def test_resume_changes_nothing(gpu_lib, prec):
+    """A finished solve is a true fixed point: running the rounds again from
+    it, every tile active, changes no bit."""
+    import fm3dt
+    w = _setup(2, 28, nev=2)
+    params = _params(w)
+    with fm3dt.Solver(w.header, precision=prec, max_events=2) as s:
+        s.set_velocity(w.velv)
+        s.solve_planewave(params)
+        a = np.concatenate([s.get_times(e) for e in range(2)])
+        st = s.solve_resume()
+        assert st["converged"] == 1 and st["sweep_launches"] == 0
+        b = np.concatenate([s.get_times(e) for e in range(2)])
+    assert np.array_equal(a, b)
+
+
 def test_fp32_offset_within_tolerance(gpu_lib):
     import fm3dt
     w = _setup(1, 40, nev=4)
