@@ -121,6 +121,21 @@ int fm3dt_solve_planewave(fm3dt_ctx *ctx, int nev, const double *params, fm3dt_s
 int fm3dt_receiver_times(fm3dt_ctx *ctx, int nrc, const double *rcr, const double *rcx,
                          const double *rcz, float *out);
 
+/* Same receiver times as fm3dt_receiver_times for callers that cannot
+ * allocate memory after start-up -- e.g. a serving loop or a Fortran driver
+ * that fixed its device footprint when it began and must keep it (an
+ * allocation can block, fragment a pre-sized pool or fail under a quota).
+ * This entry point has no counterpart in the reference.  It allocates
+ * nothing: its scratch is one fixed device array of about 1.1 MiB inside the
+ * library, held by every GPU that loads the library until the process ends.
+ * Limits: nrc <= 4096 and nev * nrc <= 262144 per call, else FM3DT_EINVAL.
+ * The first call on a device looks up that array's device address (once per
+ * device, with the device current); make that first call before capturing
+ * any stream.  All calls share the array: calls whose GPU work overlaps
+ * (other streams or contexts on the same device) race on it. */
+int fm3dt_receiver_times_noalloc(fm3dt_ctx *ctx, int nrc, const double *rcr, const double *rcx,
+                                 const double *rcz, float *out);
+
 /* Replaces parallel_rpaths and the Frechet writer merge (F:6456-6599,
  * F:7250-7777): one ray per (event, receiver), traced from the receiver down
  * the traveltime gradient with step dnr until it leaves the grid, and its
