@@ -1,0 +1,91 @@
+"""Golden fixtures (tests/golden/*.npz, written by tests/golden/make_golden.py
+from the oracle): the oracle must keep reproducing them, and the GPU path must
+match them through the C ABI.
+
+Tolerances: the gridder and the receiver interpolation use no transcendental
+functions and are compared bit for bit; fields and rays involve sin() (whose
+last bit may differ between the machine that wrote the fixtures and the one
+that runs the test), so fields compare to 1e-9 s, ray endpoints to 1e-9 rad,
+Frechet rows to 1e-5 of the row norm.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+
+
+class _H:
+    def __init__(self, z):
+        self.nv = tuple(int(x) for x in z["nv"])
+        self.vorig = tuple(float(x) for x in z["vorig"])
+        self.vstep = tuple(float(x) for x in z["vstep"])
+        self.nn = tuple(int(x) for x in z["nn"])
+        self.norig = tuple(float(x) for x in z["norig"])
+        self.nstep = tuple(float(x) for x in z["nstep"])
+        self.earth = float(z["earth"])
+
+
+def _load(path):
+    z = np.load(path)
+    return z, _H(z)
+
+
+def _dense_rows(ptr, cols, vals, nmp):
+    out = np.zeros((len(ptr) - 1, nmp))
+    for i in range(len(ptr) - 1):
+        out[i, cols[ptr[i]:ptr[i + 1]] - 1] = vals[ptr[i]:ptr[i + 1]]
+    return out
+
+
+def test_fixtures_present():
+    assert len(FIXTURES) >= 3
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p) for p in FIXTURES])
+def test_oracle_reproduces_fixture(orc, path):
+    z, h = _load(path)
+    g = orc.grid_from_header(h.nv, h.vorig, h.vstep, h.nn, h.norig, h.nstep, h.earth)
+    veln, _ = orc.gridder(g, z["velv"])
+    assert np.array_equal(veln, z["veln"])
+    fmm, _ = orc.fmm(g, veln, z["frame"], 1)
+    assert np.max(np.abs(fmm - z["fmm"])) < 1e-9
+    fp, _ = orc.fixed_point(g, veln, z["frame"], 1)
+    assert np.max(np.abs(fp - z["fixed_point"])) < 1e-9
+    trr = orc.srtimes(g, z["fmm"], z["rec_elev"], z["rec_colat"], z["rec_lon"])
+    assert np.array_equal(trr, z["trr"])
+    fdm, ends, steps = orc.rays(g, z["fmm"], veln, z["rec_elev"], z["rec_colat"], z["rec_lon"])
+    assert np.max(np.abs(ends - z["ray_ends"])) < 1e-9
+    ref = _dense_rows(z["frechet_ptr"], z["frechet_cols"], z["frechet_vals"], fdm.shape[1])
+    got = np.where(np.abs(fdm) >= np.float32(1e-6), fdm, 0).astype(np.float64)
+    assert np.max(np.abs(got - ref)) <= 1e-5 * max(1e-30, np.max(np.abs(ref)))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p) for p in FIXTURES])
+def test_gpu_matches_fixture(gpu_lib, path):
+    import fm3dt
+    z, h = _load(path)
+    with fm3dt.Solver(h, fom=1, precision=fm3dt.FP64) as s:
+        s.set_velocity(z["velv"])
+        assert np.array_equal(s.get_velocity(), z["veln"])
+        st = s.solve(z["frame"][None, :])
+        assert st["converged"] == 1
+        got = s.get_times(0)
+        assert np.max(np.abs(got - z["fixed_point"])) < 1e-9
+        trr = s.receiver_times(z["rec_elev"], z["rec_colat"], z["rec_lon"])[0].astype(np.float64)
+        ref_trr = z["trr"].astype(np.float64)
+        assert np.max(np.abs(trr - ref_trr)) <= 1e-3
+        assert np.max(np.abs(trr - ref_trr) / ref_trr) <= 1e-5
+        # receivers and rays through the fixture's own (fast-marching) field
+        s.set_times(0, 1, z["fmm"])
+        assert np.array_equal(s.receiver_times(z["rec_elev"], z["rec_colat"], z["rec_lon"])[0], z["trr"])
+        ptr, cols, vals, ends = s.rays_frechet(z["rec_elev"], z["rec_colat"], z["rec_lon"])
+    assert np.max(np.abs(ends - z["ray_ends"])) < 1e-9
+    nmp = (h.nv[0] + 2) * (h.nv[1] + 2) * (h.nv[2] + 2)
+    got_rows = _dense_rows(ptr, cols, vals, nmp)
+    ref_rows = _dense_rows(z["frechet_ptr"], z["frechet_cols"], z["frechet_vals"], nmp)
+    assert np.max(np.abs(got_rows - ref_rows)) <= 1e-5 * np.max(np.abs(ref_rows))
