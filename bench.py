@@ -233,7 +233,7 @@ def run_ours(a):
     import numpy as np
     import torch
     import fm3dt
-    from fm3dt import autotune, synth
+    from fm3dt import autotune, shard, synth
     from fm3dt import build as fb
 
     d = Dist(ws, rank)
@@ -242,9 +242,15 @@ def run_ours(a):
     h = w.header
     nev = len(w.events)
     nnr, nnx, nnz = h.nn
-    # shard: each rank solves its own batch of nev events (weak scaling)
-    rng = np.random.default_rng(1000 * a.config + 17 + rank)
-    events = w.events if rank == 0 else np.stack([rng.uniform(30, 90, nev), rng.uniform(0, 360, nev)], 1)
+    # shard: the job holds ws x nev events; each rank solves its own share of
+    # them (weak scaling), with no collective until the final gather
+    mine = list(range(nev))
+    events = w.events
+    if ws > 1:
+        wg = synth.config(a.config, scale=a.scale or None, nev=nev * ws)
+        costs = [shard.event_cost(h.nn)] * len(wg.events)
+        mine = shard.rank_events(costs, ws, rank, "balanced")
+        events = wg.events[mine]
     params = np.array([synth.planewave_params(h, *ev) for ev in events])
     frames = synth.planewave_frames(h, params)
     rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat, w.rec_lon)
@@ -328,6 +334,11 @@ def run_ours(a):
                          "h2d_bytes_per_step": int(frames.nbytes + 3 * rcr.nbytes),
                          "d2h_bytes_per_step": int(h_out.numel() * 4)}
         trr32 = h_out.numpy().astype(np.float64).copy()
+        # the job's one collective: receiver times of every rank's events to
+        # rank 0 (host gather, after the timed region)
+        got = shard.gather_to_root((mine, h_out.numpy().copy()), getattr(d, "dist", None))
+        if rank == 0:
+            extras["gathered_events"] = int(shard.merge_times(ws * nev, got).shape[0])
         # error against the plain FP64 GPU path on a subset of events (untimed)
         k = min(nev, 8)
         with fm3dt.Solver(h, fom=1, precision=fm3dt.FP64, max_events=k) as s64:

@@ -119,7 +119,7 @@ __global__ void initial_tiles_kernel(int nev, int tiles_per_event, int first, in
         const int e = q / cnt, j = q - e * cnt;
         const int w = e * tiles_per_event + first + j;
         list[q] = w;
-        flag[w] = 1;
+        flag[w] = kFull | kQueued;   // new to the solve: recompute every node
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *count = total;
 }

@@ -41,6 +41,12 @@ struct FieldArgs {
     int order2;
 };
 
+// Per-tile flag of the rounds: the halo faces changed since the tile's last
+// pass (up = r-1 side, down = r+1 side, then -/+ theta and -/+ phi), "recompute
+// every node", and "in the next round's list".
+constexpr int kFaceUp = 1, kFaceDown = 2, kFaceXm = 4, kFaceXp = 8, kFaceZm = 16, kFaceZp = 32;
+constexpr int kFaceMask = 63, kFull = 64, kQueued = 128;
+
 // Arguments of one solver round.
 template <typename R>
 struct RoundArgs {

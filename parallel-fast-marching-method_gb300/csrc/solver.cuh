@@ -43,10 +43,18 @@ struct Tile {
     static constexpr int BR = TR + 4, BX = TX + 4, BZ = TZ + 4;
     static constexpr int SR = BX * BZ;     // shared stride of one r layer
     static constexpr int NBOX = BR * BX * BZ;
+    // shared-memory layout after the box: slowness of the tile's nodes, then
+    // the spacing tables of its (r, theta) rows and r layers
+    static constexpr int OFF_S = NBOX;
+    static constexpr int OFF_HZ = OFF_S + TR * TX * TZ;
+    static constexpr int OFF_WZ = OFF_HZ + TR * TX;
+    static constexpr int OFF_HX = OFF_WZ + TR * TX;
+    static constexpr int OFF_WX = OFF_HX + TR;
+    static constexpr int NSMEM = OFF_WX + TR;
 
-    // stage tile + face halos (edges/corners are never read by the stencil);
-    // outside the grid reads as unset
-    static __device__ void load(R *box, const R *Te, const FieldArgs<R> &a, int r0, int x0, int z0)
+    // stage tile + face halos (edges/corners are never read by the stencil;
+    // outside the grid reads as unset)
+    static __device__ void load(R *sm, const R *Te, const FieldArgs<R> &a, int r0, int x0, int z0)
     {
         const R INF = Lim<R>::inf();
         for (int q = threadIdx.x; q < NBOX; q += NT) {
@@ -58,32 +66,87 @@ struct Tile {
                 if (gr >= 0 && gr < a.nnr && gx >= 0 && gx < a.nnx && gz >= 0 && gz < a.nnz)
                     v = __ldcg(Te + ((size_t)gr * a.nnx + gx) * a.nnz + gz);
             }
-            box[q] = v;
+            sm[q] = v;
         }
     }
 
-    // one node update from the shared box; returns the new value
-    static __device__ __forceinline__ R update(const R *box, int c, const FieldArgs<R> &a, int gr, int gx, int gz)
+    // stage the slowness of the tile's nodes and the spacings its rows use
+    // (the rounds reuse them over several passes)
+    static __device__ void load_params(R *sm, const FieldArgs<R> &a, int r0, int x0, int z0)
+    {
+        for (int q = threadIdx.x; q < TR * TX * TZ; q += NT) {
+            const int lz = q % TZ, lx = (q / TZ) % TX, lr = q / (TZ * TX);
+            const int gr = r0 + lr, gx = x0 + lx, gz = z0 + lz;
+            sm[OFF_S + q] = (gr < a.nnr && gx < a.nnx && gz < a.nnz)
+                                ? __ldg(a.s + ((size_t)gr * a.nnx + gx) * a.nnz + gz) : R(1);
+        }
+        for (int q = threadIdx.x; q < TR * TX; q += NT) {
+            const int lx = q % TX, lr = q / TX;
+            const int gr = r0 + lr, gx = x0 + lx;
+            const bool ok = gr < a.nnr && gx < a.nnx;
+            sm[OFF_HZ + q] = ok ? __ldg(a.hz + (size_t)gr * a.nnx + gx) : R(1);
+            sm[OFF_WZ + q] = ok ? __ldg(a.wz + (size_t)gr * a.nnx + gx) : R(1);
+        }
+        for (int q = threadIdx.x; q < TR; q += NT) {
+            const bool ok = r0 + q < a.nnr;
+            sm[OFF_HX + q] = ok ? __ldg(a.hx + r0 + q) : R(1);
+            sm[OFF_WX + q] = ok ? __ldg(a.wx + r0 + q) : R(1);
+        }
+    }
+
+    // node parameters (slowness and spacings) of one node
+    struct Params {
+        R s;
+        Spacing<R> sp;
+    };
+    static __device__ __forceinline__ Params params_global(const FieldArgs<R> &a, int gr, int gx, int gz)
+    {
+        Params p;
+        p.sp.h[0] = a.hr;
+        p.sp.w[0] = a.wr;
+        p.sp.h[1] = __ldg(a.hx + gr);
+        p.sp.w[1] = __ldg(a.wx + gr);
+        const size_t q = (size_t)gr * a.nnx + gx;
+        p.sp.h[2] = __ldg(a.hz + q);
+        p.sp.w[2] = __ldg(a.wz + q);
+        p.s = __ldg(a.s + q * a.nnz + gz);
+        return p;
+    }
+    static __device__ __forceinline__ Params params_shared(const R *sm, const FieldArgs<R> &a, int r, int tx, int tz)
+    {
+        Params p;
+        p.sp.h[0] = a.hr;
+        p.sp.w[0] = a.wr;
+        p.sp.h[1] = sm[OFF_HX + r];
+        p.sp.w[1] = sm[OFF_WX + r];
+        p.sp.h[2] = sm[OFF_HZ + r * TX + tx];
+        p.sp.w[2] = sm[OFF_WZ + r * TX + tx];
+        p.s = sm[OFF_S + (r * TX + tx) * TZ + tz];
+        return p;
+    }
+
+    // one node update from the shared box with the node's parameters
+    static __device__ __forceinline__ R update_with(const R *sm, int c, const FieldArgs<R> &a, int gr, int gx, int gz,
+                                                    const Params &p)
     {
         R t1[6], t2[6];
-        t1[0] = box[c - SR];     t2[0] = box[c - 2 * SR];
-        t1[1] = box[c + SR];     t2[1] = box[c + 2 * SR];
-        t1[2] = box[c - BZ];     t2[2] = box[c - 2 * BZ];
-        t1[3] = box[c + BZ];     t2[3] = box[c + 2 * BZ];
-        t1[4] = box[c - 1];      t2[4] = box[c - 2];
-        t1[5] = box[c + 1];      t2[5] = box[c + 2];
+        t1[0] = sm[c - SR];     t2[0] = sm[c - 2 * SR];
+        t1[1] = sm[c + SR];     t2[1] = sm[c + 2 * SR];
+        t1[2] = sm[c - BZ];     t2[2] = sm[c - 2 * BZ];
+        t1[3] = sm[c + BZ];     t2[3] = sm[c + 2 * BZ];
+        t1[4] = sm[c - 1];      t2[4] = sm[c - 2];
+        t1[5] = sm[c + 1];      t2[5] = sm[c + 2];
         const unsigned inb = (gr > 0 ? 1u : 0u) | (gr < a.nnr - 1 ? 2u : 0u) | (gx > 0 ? 4u : 0u) |
                              (gx < a.nnx - 1 ? 8u : 0u) | (gz > 0 ? 16u : 0u) | (gz < a.nnz - 1 ? 32u : 0u);
-        Spacing<R> sp;
-        sp.h[0] = a.hr;
-        sp.w[0] = a.wr;
-        sp.h[1] = __ldg(a.hx + gr);
-        sp.w[1] = __ldg(a.wx + gr);
-        const size_t q = (size_t)gr * a.nnx + gx;
-        sp.h[2] = __ldg(a.hz + q);
-        sp.w[2] = __ldg(a.wz + q);
-        const R sv = __ldg(a.s + q * a.nnz + gz);
-        return fm_update<R>(sv, t1, t2, inb, sp, a.order2);
+        return fm_update<R>(p.s, t1, t2, inb, p.sp, a.order2);
+    }
+
+    // one node update (tile-local r, tx, tz) from shared memory; returns the
+    // new value
+    static __device__ __forceinline__ R update(const R *sm, int c, const FieldArgs<R> &a, int r, int tx, int tz,
+                                               int gr, int gx, int gz)
+    {
+        return update_with(sm, c, a, gr, gx, gz, params_shared(sm, a, r, tx, tz));
     }
 
     static __device__ __forceinline__ bool frozen(const FieldArgs<R> &a, int e, int gr, int gx, int gz)
@@ -113,12 +176,15 @@ __global__ void __launch_bounds__(TX * TZ) round_kernel(RoundArgs<R> a)
     unsigned long long my_tiles = 0, my_staged = 0, my_upd = 0;
     if (tid == 0) s_upd = 0;
 
+    __shared__ int s_dirty_faces;
     for (int item = blockIdx.x; item < count; item += gridDim.x) {
         if (tid == 0) {
             const int w = a.cur_list[item];
             s_w = w;
             s_face = 0;
-            atomicExch(&a.flag[w], 0);   // later activations re-queue this tile
+            // take the halo faces changed since this tile's last pass; later
+            // activations re-queue it
+            s_dirty_faces = atomicExch(&a.flag[w], 0) & (kFaceMask | kFull);
             __threadfence();
         }
         __syncthreads();
@@ -131,6 +197,7 @@ __global__ void __launch_bounds__(TX * TZ) round_kernel(RoundArgs<R> a)
         const int r0 = tri * TR, x0 = txi * TX, z0 = tzi * TZ;
         R *Te = f.T + (size_t)e * N;
         TL::load(box, Te, f, r0, x0, z0);
+        TL::load_params(box, f, r0, x0, z0);
 
         const int gx = x0 + tx, gz = z0 + tz;
         const bool colv = gx < f.nnx && gz < f.nnz;
@@ -142,14 +209,30 @@ __global__ void __launch_bounds__(TX * TZ) round_kernel(RoundArgs<R> a)
         }
         __syncthreads();
 
-        // Passes.  The first recomputes every node; later ones only the nodes
-        // with a stencil neighbour (+-1, +-2 along each axis) that changed in
-        // the previous pass -- a node's update never reads its own value, so
-        // nothing else can change.
+        // Passes.  The tile was at its fixed point for the halo it last saw, so
+        // the first pass recomputes only the nodes within two nodes of a halo
+        // face that changed since (every node when the tile is new to the
+        // solve); later passes only the nodes with a stencil neighbour (+-1,
+        // +-2 along each axis) that changed in the previous pass -- a node's
+        // update never reads its own value, so nothing else can change.
         unsigned chm = 0;
         bool last_changed = false;
         const int cbase = (2 * TL::BX + (tx + 2)) * TL::BZ + (tz + 2);
-        unsigned dirty = updm;
+        const int df = s_dirty_faces;
+        unsigned dirty;
+        if (df & kFull) {
+            dirty = updm;
+        } else {
+            constexpr unsigned all = (TR >= 32) ? 0xffffffffu : ((1u << TR) - 1u);
+            dirty = 0;
+            if (df & kFaceUp) dirty |= 3u;
+            if (df & kFaceDown) dirty |= 3u << (TR - 2);
+            if ((df & kFaceXm) && tx < 2) dirty = all;
+            if ((df & kFaceXp) && tx >= TX - 2) dirty = all;
+            if ((df & kFaceZm) && tz < 2) dirty = all;
+            if ((df & kFaceZp) && tz >= TZ - 2) dirty = all;
+            dirty &= updm;
+        }
         for (int p = 0; p < a.max_passes; ++p) {
             unsigned pch = 0;
             // r changes only shared-memory offsets and mask bits: no unrolling
@@ -158,7 +241,7 @@ __global__ void __launch_bounds__(TX * TZ) round_kernel(RoundArgs<R> a)
             for (int i = 0, k = k0; i < TR; ++i, k += dk) {
                 if (!((dirty >> k) & 1u)) continue;
                 const int c = cbase + k * TL::SR;
-                const R nv = TL::update(box, c, f, r0 + k, gx, gz);
+                const R nv = TL::update(box, c, f, k, tx, tz, r0 + k, gx, gz);
                 ++my_upd;
                 if (fbits(nv) != fbits(box[c])) {
                     box[c] = nv;
@@ -201,18 +284,19 @@ __global__ void __launch_bounds__(TX * TZ) round_kernel(RoundArgs<R> a)
             int fl = s_face;
             if (tid == 6 && last_changed) fl |= 64;   // pass cap hit: run again
             if ((fl >> tid) & 1) {
-                int nb = -1;
+                int nb = -1, bit = kFull;
                 const int sl = f.ntx * f.ntz;
+                // the neighbour's halo face opposite to the face that changed
                 switch (tid) {
-                    case 0: nb = tri > 0 ? w - sl : -1; break;
-                    case 1: nb = tri < f.ntr - 1 ? w + sl : -1; break;
-                    case 2: nb = txi > 0 ? w - f.ntz : -1; break;
-                    case 3: nb = txi < f.ntx - 1 ? w + f.ntz : -1; break;
-                    case 4: nb = tzi > 0 ? w - 1 : -1; break;
-                    case 5: nb = tzi < f.ntz - 1 ? w + 1 : -1; break;
-                    default: nb = w; break;
+                    case 0: nb = tri > 0 ? w - sl : -1; bit = kFaceDown; break;
+                    case 1: nb = tri < f.ntr - 1 ? w + sl : -1; bit = kFaceUp; break;
+                    case 2: nb = txi > 0 ? w - f.ntz : -1; bit = kFaceXp; break;
+                    case 3: nb = txi < f.ntx - 1 ? w + f.ntz : -1; bit = kFaceXm; break;
+                    case 4: nb = tzi > 0 ? w - 1 : -1; bit = kFaceZp; break;
+                    case 5: nb = tzi < f.ntz - 1 ? w + 1 : -1; bit = kFaceZm; break;
+                    default: nb = w; bit = kFull; break;
                 }
-                if (nb >= 0 && atomicExch(&a.flag[nb], 1) == 0) {
+                if (nb >= 0 && !(atomicOr(&a.flag[nb], bit | kQueued) & kQueued)) {
                     const int pos = atomicAdd(a.next_count, 1);
                     a.next_list[pos] = nb;
                 }
@@ -273,14 +357,21 @@ __global__ void __launch_bounds__(TX * TZ) sweep_kernel(SweepArgs<R> a)
         __syncthreads();
         // pipelined wavefront: layer rp (counted upward from the tile bottom)
         // of column (xs, zs) is updated at step rp + xs + zs
+        // The next node's slowness and spacings are fetched one step ahead,
+        // so their latency hides behind the barrier.
+        typename TL::Params pnext{};
+        if (colv && xs + zs == 0 && r0 + TR - 1 < f.nnr) pnext = TL::params_global(f, r0 + TR - 1, gx, gz);
         for (int step = 0; step < TR + TX + TZ - 2; ++step) {
             const int rp = step - xs - zs;
+            const typename TL::Params pcur = pnext;
+            if (colv && rp + 1 >= 0 && rp + 1 < TR && r0 + TR - 2 - rp < f.nnr)
+                pnext = TL::params_global(f, r0 + TR - 2 - rp, gx, gz);
             if (colv && rp >= 0 && rp < TR) {
                 const int r = TR - 1 - rp;
                 const int gr = r0 + r;
                 if (gr < f.nnr && !TL::frozen(f, e, gr, gx, gz)) {
                     const int c = cbase + r * TL::SR;
-                    box[c] = TL::update(box, c, f, gr, gx, gz);
+                    box[c] = TL::update_with(box, c, f, gr, gx, gz, pcur);
                 }
             }
             __syncthreads();
@@ -302,12 +393,16 @@ __global__ void __launch_bounds__(TX * TZ) sweep_kernel(SweepArgs<R> a)
 template <typename R, int S>
 struct ShapeKernels {
     static constexpr int TR = kShapes[S].tr, TX = kShapes[S].tx, TZ = kShapes[S].tz;
-    static constexpr size_t SMEM = Tile<R, TR, TX, TZ>::NBOX * sizeof(R);
+    // rounds stage the node parameters too; the sweep only the box
+    static constexpr size_t SMEM_ROUND = Tile<R, TR, TX, TZ>::NSMEM * sizeof(R);
+    static constexpr size_t SMEM_SWEEP = Tile<R, TR, TX, TZ>::NBOX * sizeof(R);
     static void setup()
     {
         static const bool once = [] {
-            cudaFuncSetAttribute(round_kernel<R, TR, TX, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
-            cudaFuncSetAttribute(sweep_kernel<R, TR, TX, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+            cudaFuncSetAttribute(round_kernel<R, TR, TX, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)SMEM_ROUND);
+            cudaFuncSetAttribute(sweep_kernel<R, TR, TX, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)SMEM_SWEEP);
             return true;
         }();
         (void)once;
@@ -315,25 +410,25 @@ struct ShapeKernels {
     static void round(int grid, const RoundArgs<R> &a, cudaStream_t st)
     {
         setup();
-        round_kernel<R, TR, TX, TZ><<<grid, TX * TZ, SMEM, st>>>(a);
+        round_kernel<R, TR, TX, TZ><<<grid, TX * TZ, SMEM_ROUND, st>>>(a);
     }
     static void sweep(int grid, const SweepArgs<R> &a, cudaStream_t st)
     {
         setup();
-        sweep_kernel<R, TR, TX, TZ><<<grid, TX * TZ, SMEM, st>>>(a);
+        sweep_kernel<R, TR, TX, TZ><<<grid, TX * TZ, SMEM_SWEEP, st>>>(a);
     }
     static int occ_round()
     {
         setup();
         int nb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, round_kernel<R, TR, TX, TZ>, TX * TZ, SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, round_kernel<R, TR, TX, TZ>, TX * TZ, SMEM_ROUND);
         return nb;
     }
     static int occ_sweep()
     {
         setup();
         int nb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sweep_kernel<R, TR, TX, TZ>, TX * TZ, SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sweep_kernel<R, TR, TX, TZ>, TX * TZ, SMEM_SWEEP);
         return nb;
     }
 };

@@ -47,6 +47,7 @@ def make(name, cfg, n, event, holes):
     nrc = min(20, len(colat))
     rec = (w.rec_elev[:nrc], colat[:nrc], lonr[:nrc])
     trr = O.srtimes(g, fmm, *rec)
+    trr_fp = O.srtimes(g, fp, *rec)
     fdm, ends, steps = O.rays(g, fmm, veln, *rec)
     cols, vals, ptr = [], [], [0]
     for i in range(nrc):
@@ -60,7 +61,7 @@ def make(name, cfg, n, event, holes):
         nn=np.array(h.nn), norig=np.array(h.norig), nstep=np.array(h.nstep), earth=np.array(h.earth),
         velv=w.velv, veln=veln, frame=frame, params=params,
         fmm=fmm, fmm_first_order=fmm1, fixed_point=fp,
-        rec_elev=rec[0], rec_colat=rec[1], rec_lon=rec[2], trr=trr,
+        rec_elev=rec[0], rec_colat=rec[1], rec_lon=rec[2], trr=trr, trr_fixed_point=trr_fp,
         ray_ends=ends, ray_steps=steps,
         frechet_ptr=np.array(ptr, dtype=np.int64),
         frechet_cols=np.concatenate(cols).astype(np.int32),

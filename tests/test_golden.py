@@ -57,6 +57,8 @@ def test_oracle_reproduces_fixture(orc, path):
     assert np.max(np.abs(fp - z["fixed_point"])) < 1e-9
     trr = orc.srtimes(g, z["fmm"], z["rec_elev"], z["rec_colat"], z["rec_lon"])
     assert np.array_equal(trr, z["trr"])
+    trr = orc.srtimes(g, z["fixed_point"], z["rec_elev"], z["rec_colat"], z["rec_lon"])
+    assert np.max(np.abs(trr.astype(np.float64) - z["trr_fixed_point"])) <= 1e-3
     fdm, ends, steps = orc.rays(g, z["fmm"], veln, z["rec_elev"], z["rec_colat"], z["rec_lon"])
     assert np.max(np.abs(ends - z["ray_ends"])) < 1e-9
     ref = _dense_rows(z["frechet_ptr"], z["frechet_cols"], z["frechet_vals"], fdm.shape[1])
@@ -76,8 +78,11 @@ def test_gpu_matches_fixture(gpu_lib, path):
         assert st["converged"] == 1
         got = s.get_times(0)
         assert np.max(np.abs(got - z["fixed_point"])) < 1e-9
+        # the solve converges to the fixed point; with unset boundary values
+        # that differs from the fast-marching field (its heap is not causal
+        # there), so the receivers compare with the fixed point's times
         trr = s.receiver_times(z["rec_elev"], z["rec_colat"], z["rec_lon"])[0].astype(np.float64)
-        ref_trr = z["trr"].astype(np.float64)
+        ref_trr = z["trr_fixed_point"].astype(np.float64)
         assert np.max(np.abs(trr - ref_trr)) <= 1e-3
         assert np.max(np.abs(trr - ref_trr) / ref_trr) <= 1e-5
         # receivers and rays through the fixture's own (fast-marching) field
