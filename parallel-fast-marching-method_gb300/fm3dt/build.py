@@ -17,6 +17,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(ROOT, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(ROOT, "libfm3dt_gpu.so")
+DRIVER_DIR = os.path.join(ROOT, "driver")
+DRIVER = os.path.join(ROOT, "fm3dt_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
@@ -38,10 +40,11 @@ def nvcc() -> str:
     return cand
 
 
-def _deps_mtime() -> float:
+def _deps_mtime(dirs=(CSRC,)) -> float:
     m = 0.0
-    for f in os.listdir(CSRC):
-        m = max(m, os.path.getmtime(os.path.join(CSRC, f)))
+    for d in dirs:
+        for f in os.listdir(d):
+            m = max(m, os.path.getmtime(os.path.join(d, f)))
     hdr = os.path.join(os.path.dirname(ROOT), "include", "fm3dt_gpu.h")
     if os.path.exists(hdr):
         m = max(m, os.path.getmtime(hdr))
@@ -78,6 +81,25 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
     return LIB
+
+
+def build_driver(force: bool = False) -> str:
+    """Builds the host driver fm3dt_run (the reference's file contract over
+    the C ABI) with g++, linked to libfm3dt_gpu.so in the same directory."""
+    lib = build(force=force)
+    if not force and os.path.exists(DRIVER) and \
+            os.path.getmtime(DRIVER) >= max(_deps_mtime((DRIVER_DIR,)), os.path.getmtime(lib)):
+        return DRIVER
+    cxx = shutil.which("g++") or "g++"
+    tmp = DRIVER + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", os.path.join(DRIVER_DIR, "fm3dt_run.cpp"),
+           os.path.join(DRIVER_DIR, "fm3dt_files.cpp"), "-o", tmp, "-L" + ROOT, "-lfm3dt_gpu",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":
