@@ -33,6 +33,17 @@ bool parse_double(const std::string &tok, double &v)
     return errno == 0 && end && *end == '\0' && !t.empty();
 }
 
+bool parse_float(const std::string &tok, float &v)
+{
+    std::string t = tok;
+    for (char &c : t)
+        if (c == 'd' || c == 'D') c = 'e';
+    errno = 0;
+    char *end = nullptr;
+    v = std::strtof(t.c_str(), &end);
+    return errno == 0 && end && *end == '\0' && !t.empty();
+}
+
 bool parse_int(const std::string &tok, int &v)
 {
     errno = 0;
@@ -97,6 +108,15 @@ bool ListReader::doubles(double *v, int n)
     if (!tokens(t, n)) return false;
     for (int i = 0; i < n; ++i)
         if (!parse_double(t[i], v[i])) return false;
+    return true;
+}
+
+bool ListReader::floats(float *v, int n)
+{
+    std::vector<std::string> t;
+    if (!tokens(t, n)) return false;
+    for (int i = 0; i < n; ++i)
+        if (!parse_float(t[i], v[i])) return false;
     return true;
 }
 
@@ -263,6 +283,45 @@ std::string format_real4(float v)
         std::snprintf(buf, sizeof buf, "%16s", (m + ex).c_str());
     }
     return " " + std::string(buf);
+}
+
+bool read_frechet(const std::string &path, int64_t nrows, std::vector<int64_t> &row_ptr, std::vector<int32_t> &cols,
+                  std::vector<float> &vals, std::string &err)
+{
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) { err = "cannot open " + path; return false; }
+    auto rec = [&](int32_t &a, float &b) {
+        int32_t l0 = 0, l1 = 0;
+        if (std::fread(&l0, 4, 1, f) != 1 || l0 != 8 || std::fread(&a, 4, 1, f) != 1 || std::fread(&b, 4, 1, f) != 1 ||
+            std::fread(&l1, 4, 1, f) != 1 || l1 != 8)
+            return false;
+        return true;
+    };
+    if (row_ptr.empty()) row_ptr.push_back((int64_t)cols.size());
+    bool good = true;
+    for (int64_t r = 0; r < nrows && good; ++r) {
+        int32_t n = 0;
+        float recid = 0.0f;
+        if (!rec(n, recid) || n < 0) { good = false; break; }
+        for (int32_t k = 0; k < n; ++k) {
+            int32_t c = 0;
+            float v = 0.0f;
+            if (!rec(c, v)) { good = false; break; }
+            cols.push_back(c);
+            vals.push_back(v);
+        }
+        row_ptr.push_back((int64_t)cols.size());
+    }
+    std::fclose(f);
+    if (!good) err = path + ": truncated or malformed record";
+    return good;
+}
+
+std::string format_real8(double v)
+{
+    char buf[64];
+    std::snprintf(buf, sizeof buf, " %24.17E", v);
+    return buf;
 }
 
 FrechetWriter::FrechetWriter(const std::string &path) { f_ = std::fopen(path.c_str(), "wb"); }

@@ -55,6 +55,8 @@ public:
     // or on a value that does not parse.
     bool doubles(double *out, int n);
     bool ints(int *out, int n);
+    // REAL(4) items: each value converted from its decimal text to float
+    bool floats(float *out, int n);
     // Reads one whole record (without its newline).
     bool record(std::string &line);
     long line_number() const { return line_no_; }
@@ -84,6 +86,14 @@ private:
     FILE *f_ = nullptr;
     size_t frame_ = 0;
 };
+
+// Reads nrows rows of frechet.out (format below): per row its entries
+// (1-based column, value) appended to cols/vals and row_ptr extended.
+bool read_frechet(const std::string &path, int64_t nrows, std::vector<int64_t> &row_ptr, std::vector<int32_t> &cols,
+                  std::vector<float> &vals, std::string &err);
+
+// gfortran list-directed output of one REAL(8) value (17 significant digits).
+std::string format_real8(double v);
 
 // gfortran list-directed output of one REAL(4) value, one per record
 // (WRITE(10,*) trr at F:7174-7176), e.g. "   357.198395    ".

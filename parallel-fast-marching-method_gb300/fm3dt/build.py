@@ -102,6 +102,35 @@ def build_driver(force: bool = False) -> str:
     return DRIVER
 
 
+SUBINV_DIR = os.path.join(ROOT, "subinv")
+SUBINV_LIB = os.path.join(ROOT, "libfm3dt_subinv.so")
+SUBINV = os.path.join(ROOT, "fm3dt_subinv")
+HOST_FLAGS = ["-O2", "-std=c++17", "-Wall", "-ffp-contract=off"]
+
+
+def build_subinv(force: bool = False) -> str:
+    """Builds the host-side subspace inversion (libfm3dt_subinv.so and the
+    fm3dt_subinv program) with g++; no CUDA involved."""
+    deps = max(_deps_mtime((SUBINV_DIR, DRIVER_DIR)), os.path.getmtime(
+        os.path.join(os.path.dirname(ROOT), "include", "fm3dt_subinv.h")))
+    if not force and all(os.path.exists(p) and os.path.getmtime(p) >= deps for p in (SUBINV_LIB, SUBINV)):
+        return SUBINV_LIB
+    cxx = shutil.which("g++") or "g++"
+    steps = [
+        [cxx, *HOST_FLAGS, "-fPIC", "-shared", os.path.join(SUBINV_DIR, "subinv.cpp"), "-o", SUBINV_LIB + ".tmp"],
+        [cxx, *HOST_FLAGS, os.path.join(SUBINV_DIR, "subinv_main.cpp"), os.path.join(DRIVER_DIR, "fm3dt_files.cpp"),
+         "-o", SUBINV + ".tmp", "-L" + ROOT, "-lfm3dt_subinv", "-Wl,-rpath,$ORIGIN"],
+    ]
+    for i, cmd in enumerate(steps):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"subinv build failed:\n{r.stdout}\n{r.stderr}")
+        if i == 0:
+            os.replace(SUBINV_LIB + ".tmp", SUBINV_LIB)
+    os.replace(SUBINV + ".tmp", SUBINV)
+    return SUBINV_LIB
+
+
 if __name__ == "__main__":
     import sys
     print(build(force=True, verbose=True, ptxas_info="-v" in sys.argv))
