@@ -295,6 +295,40 @@ def read_frechet(path) -> FrechetRows:
                        np.array(recid, np.float64))
 
 
+SUBINV_KEYS = [("gridi", "a"), ("gridc", "a"), ("otimes", "a"), ("rtimes", "a"), ("mtimes", "a"),
+               ("rmtr", "i"), ("frechet", "a"), ("sources", "a"), ("receivers", "a"), ("subiter", "a"),
+               ("epsilon", "f"), ("subdim", "i"), ("asds", "i"), ("eta", "f"), ("invst", "i"),
+               ("stfile", "a"), ("stdf", "f"), ("fracg", "f"), ("earth", "f")]
+
+
+def write_subinv_in(path, **kw):
+    """subinv.in: three comment records, then one item per
+    record; file names are read (a25)."""
+    defaults = dict(gridi="gridi.vtx", gridc="gridc.vtx", otimes="otimes.dat", rtimes="rtimes.dat",
+                    mtimes="rtravel.out", rmtr=1, frechet="frechet.out", sources="sources.dat",
+                    receivers="receivers.dat", subiter="subiter.in", epsilon=10.0, subdim=10, asds=1, eta=10.0,
+                    invst=0, stfile="stationres.dat", stdf=10.0, fracg=0.1, earth=6371.0)
+    defaults.update(kw)
+    c = "c" * 70
+    with open(path, "w") as fh:
+        fh.write(c + "\nc INPUT PARAMETERS\n" + c + "\n")
+        for k, _ in SUBINV_KEYS:
+            fh.write(f"{str(defaults[k]):<26}c: {k}\n")
+
+
+def read_subinv_in(path) -> dict:
+    lines = open(path).read().splitlines()
+    out, pos = {}, 3
+    for k, t in SUBINV_KEYS:
+        if t == "a":
+            out[k] = lines[pos][:25].strip()
+            pos += 1
+        else:
+            (v,), pos = _list_values(lines, 1, pos, int if t == "i" else float)
+            out[k] = v
+    return out
+
+
 def write_otimes(path, tstat, resid, unc):
     with open(path, "w") as fh:
         for s, r, u in zip(tstat, resid, unc):

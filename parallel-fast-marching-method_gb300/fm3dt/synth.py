@@ -204,3 +204,36 @@ def planewave_frames(h: Header, params) -> np.ndarray:
     for e, (t0, p, ca, sa) in enumerate(params):
         out[e] = t0 + p * (dn[:, None] * ca + de[None, :] * sa)
     return out.reshape(len(params), nnx * nnz)
+
+
+@dataclass
+class TomographyProblem:
+    """A teleseismic tomography run: the starting model (a 1-D gradient, as
+    gridi.vtx holds it: 8 decimals, a priori standard deviation 0.3), the
+    true model (the config-3 checkerboard), and a survey of plane-wave
+    sources and surface receivers, array by array."""
+    header: Header
+    velv_start: np.ndarray
+    velv_true: np.ndarray
+    cm_sd: np.ndarray
+    frames: list                  # per array (nsrc, nnx*nnz)
+    receivers: list               # per array (nrc, 3): elev km, lat, lon
+    events: list                  # per array (nsrc, 2): distance, back-azimuth
+
+
+def tomography_problem(scale: int | None = None, arrays=((500, 300),), seed: int = 3001) -> TomographyProblem:
+    w = config(3, nev=1, scale=scale)
+    h = w.header
+    # as the solver reads gridi.vtx written with 8 decimals
+    start = np.array([float("%.8f" % v) for v in velocity_model(h, "plain", seed)])
+    true = velocity_model(h, "checker", seed)
+    rng = np.random.default_rng(seed)
+    frames, recs, evs = [], [], []
+    for a, (ns, nr) in enumerate(arrays):
+        ev = np.stack([rng.uniform(30.0, 90.0, ns), rng.uniform(0.0, 360.0, ns)], axis=1)
+        params = np.array([planewave_params(h, *e) for e in ev])
+        frames.append(planewave_frames(h, params))
+        elev, lat, lon = receivers(h, nr, seed + 11 + a)
+        recs.append(np.stack([elev, lat, lon], axis=1))
+        evs.append(ev)
+    return TomographyProblem(h, start, true, np.full(start.size, 0.3, np.float32), frames, recs, evs)
