@@ -199,7 +199,7 @@ def write_receivers(path, arrays):
         for a, arr in enumerate(arrays):
             fh.write(f"{len(arr)}         ARRAY {a + 1}\n")
             for el, lat, lon, name in arr:
-                fh.write(f"{el!r}     {lat!r}    {lon!r}     {name}\n")
+                fh.write(f"{float(el)!r}     {float(lat)!r}    {float(lon)!r}     {name}\n")
 
 
 def read_receivers(path):
