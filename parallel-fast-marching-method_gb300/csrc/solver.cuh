@@ -155,11 +155,32 @@ struct Tile {
     }
 };
 
+// Resident 128-thread CTAs per SM that the register allocation must allow.
+// The kernels are issue-bound with long dependent chains, so occupancy pays
+// until registers spill.
+#ifndef FM_ROUND_MINB_F32
+#define FM_ROUND_MINB_F32 8
+#endif
+#ifndef FM_ROUND_MINB_F64
+#define FM_ROUND_MINB_F64 4
+#endif
+#ifndef FM_SWEEP_MINB_F32
+#define FM_SWEEP_MINB_F32 6
+#endif
+#ifndef FM_SWEEP_MINB_F64
+#define FM_SWEEP_MINB_F64 4
+#endif
+template <typename R, int THREADS>
+struct MinBlocks {
+    static constexpr int round = (sizeof(R) == 4 ? FM_ROUND_MINB_F32 : FM_ROUND_MINB_F64) * 128 / THREADS;
+    static constexpr int sweep = (sizeof(R) == 4 ? FM_SWEEP_MINB_F32 : FM_SWEEP_MINB_F64) * 128 / THREADS;
+};
+
 // ---------------------------------------------------------------------------
 // Rounds (fast-iterative cleanup until the fixed point)
 // ---------------------------------------------------------------------------
 template <typename R, int TR, int TX, int TZ>
-__global__ void __launch_bounds__(TX * TZ) round_kernel(RoundArgs<R> a)
+__global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round)) round_kernel(RoundArgs<R> a)
 {
     using TL = Tile<R, TR, TX, TZ>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -326,7 +347,7 @@ __global__ void __launch_bounds__(TX * TZ) round_kernel(RoundArgs<R> a)
 // Sweep (one launch per tile hyperplane of the event's dominant direction)
 // ---------------------------------------------------------------------------
 template <typename R, int TR, int TX, int TZ>
-__global__ void __launch_bounds__(TX * TZ) sweep_kernel(SweepArgs<R> a)
+__global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::sweep)) sweep_kernel(SweepArgs<R> a)
 {
     using TL = Tile<R, TR, TX, TZ>;
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -1,14 +1,15 @@
 """Builds libfm3dt_gpu.so in-tree with nvcc for sm_103a (GB300).
 
-Translation units compile in parallel; the kernels whose double-precision
-results must round exactly like the reference's left-to-right Fortran
-arithmetic (gridder, boundary frames, receivers, rays) are compiled without
-FMA contraction.  The solver keeps contraction on.
+Translation units compile in parallel, all without automatic FMA
+contraction: the gridder, boundary frames, receivers and rays round like the
+reference's left-to-right Fortran arithmetic, and the solver's explicit FMAs
+make every kernel instantiation compute the same bits.
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import shlex
 import shutil
 import subprocess
 
@@ -60,7 +61,9 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     def one(item):
         src, extra = item
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-        cmd = [nv, *ARCH, *COMMON, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+        # FM3DT_NVCC_FLAGS: extra flags for tuning builds (e.g. -DFM_ROUND_MINB_F32=8)
+        cmd = [nv, *ARCH, *COMMON, *extra, *shlex.split(os.environ.get("FM3DT_NVCC_FLAGS", "")),
+               "-c", os.path.join(CSRC, src), "-o", obj]
         if ptxas_info:
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)
