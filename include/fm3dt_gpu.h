@@ -113,6 +113,24 @@ int fm3dt_solve_resume(fm3dt_ctx *ctx, fm3dt_status *st);
  * in the tangent plane of the bottom surface. */
 int fm3dt_solve_planewave(fm3dt_ctx *ctx, int nev, const double *params, fm3dt_status *st);
 
+/* Point sources (local events).  No counterpart in the reference, whose
+ * sources are teleseismic boundary frames; the serving workload's local
+ * events need it.  src: nev x 3 doubles (height km -- negative below the
+ * surface --, colatitude rad, longitude rad; the receiver convention).
+ * Around each source a box of 2*extent nodes per axis centred on the source
+ * cell is started before the rounds run:
+ *   refine = 0:  straight-ray times (Cartesian chord times the mean of the
+ *                source's trilinear slowness and the node's), the whole box
+ *                fixed;  extent 1..16;
+ *   refine = k:  (2..16) a k-times finer grid over the box, started with
+ *                straight-ray times within two fine cells of the source and
+ *                solved to its fixed point, sampled at the coarse nodes; the
+ *                box without its outer layer fixed;  extent 2..16.
+ * Times are seconds after the origin time.  Receiver times work as after
+ * fm3dt_solve; rays and Frechet rows are teleseismic only (FM3DT_ESTATE).
+ * FM3DT_ERANGE if a source lies outside the grid. */
+int fm3dt_solve_point(fm3dt_ctx *ctx, int nev, const double *src, int refine, int extent, fm3dt_status *st);
+
 /* Replaces srtimes (F:7040-7248): trilinear receiver times of every solved
  * event, accumulated in single precision like REAL(4) trr (F:47, 7098-7106).
  * rcr: receiver height km; rcx: colatitude rad; rcz: longitude rad

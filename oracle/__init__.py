@@ -61,6 +61,10 @@ def lib():
         L.orc_gridder.argtypes = [C.POINTER(Grid), dp, dp, C.POINTER(C.c_int)]
         L.orc_fmm.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.POINTER(C.c_longlong)]
         L.orc_fixed_point.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.c_int, C.POINTER(C.c_int)]
+        ub = C.POINTER(C.c_ubyte)
+        L.orc_fixed_point_field.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, ub, dp, C.c_int, C.POINTER(C.c_int)]
+        L.orc_point_start.argtypes = [C.POINTER(Grid), dp, dp, C.c_int, C.c_double, C.c_double, C.c_double,
+                                      C.c_int, C.c_int, dp, ub]
         L.orc_srtimes.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, dp, C.POINTER(C.c_float)]
         L.orc_rays.argtypes = [C.POINTER(Grid), dp, dp, C.c_int, dp, dp, dp, C.POINTER(C.c_float),
                                dp, C.POINTER(C.c_int)]
@@ -136,6 +140,42 @@ def fixed_point(g: Grid, veln: np.ndarray, bottom: np.ndarray, fom: int = 1, max
     if rc != 0:
         raise RuntimeError(f"orc_fixed_point failed: {rc}")
     return ttn, sweeps.value
+
+
+def fixed_point_field(g: Grid, veln: np.ndarray, init: np.ndarray, fixed: np.ndarray, fom: int = 1,
+                      max_sweeps: int = 100000):
+    """Fixed point from an arbitrary start (init: inf = unset; fixed: keep)."""
+    veln = np.ascontiguousarray(veln, dtype=np.float64)
+    init = np.ascontiguousarray(init, dtype=np.float64)
+    fixed = np.ascontiguousarray(fixed, dtype=np.uint8)
+    ttn = np.zeros(g.nnr * g.nnx * g.nnz, dtype=np.float64)
+    sweeps = C.c_int(0)
+    rc = lib().orc_fixed_point_field(C.byref(g), _d(veln), int(fom), _d(init),
+                                     fixed.ctypes.data_as(C.POINTER(C.c_ubyte)), _d(ttn), int(max_sweeps),
+                                     C.byref(sweeps))
+    if rc != 0:
+        raise RuntimeError(f"orc_fixed_point_field failed: {rc}")
+    return ttn, sweeps.value
+
+
+def point_start(g: Grid, velv, veln, src, refine: int = 5, extent: int = 3, fom: int = 1):
+    """(init, fixed) of a point-source solve; src = (height km, colat, lon)."""
+    velv = np.ascontiguousarray(velv, dtype=np.float64)
+    veln = np.ascontiguousarray(veln, dtype=np.float64)
+    n = g.nnr * g.nnx * g.nnz
+    init = np.zeros(n, dtype=np.float64)
+    fixed = np.zeros(n, dtype=np.uint8)
+    rc = lib().orc_point_start(C.byref(g), _d(velv), _d(veln), int(fom), float(src[0]), float(src[1]),
+                               float(src[2]), int(refine), int(extent), _d(init),
+                               fixed.ctypes.data_as(C.POINTER(C.c_ubyte)))
+    if rc != 0:
+        raise RuntimeError(f"orc_point_start failed: {rc}")
+    return init, fixed
+
+
+def point_solve(g: Grid, velv, veln, src, refine: int = 5, extent: int = 3, fom: int = 1):
+    init, fixed = point_start(g, velv, veln, src, refine, extent, fom)
+    return fixed_point_field(g, veln, init, fixed, fom)[0]
 
 
 def srtimes(g: Grid, ttn: np.ndarray, rcr, rcx, rcz):

@@ -647,6 +647,9 @@ static double fp_update(fmm_state *s, int fom, int iz, int ix, int ir)
     return best;
 }
 
+static int fixed_point_run(fmm_state *s, unsigned char *fixed, int fom, double *ttn, int max_sweeps,
+                           int *sweeps);
+
 int orc_fixed_point(const orc_grid *g, const double *veln, int fom, const double *bottom, double *ttn,
                     int max_sweeps, int *sweeps)
 {
@@ -669,6 +672,38 @@ int orc_fixed_point(const orc_grid *g, const double *veln, int fom, const double
                 fixed[TI(&s, j, i, rn)] = 1;
             }
         }
+    return fixed_point_run(&s, fixed, fom, ttn, max_sweeps, sweeps);
+}
+
+int orc_fixed_point_field(const orc_grid *g, const double *veln, int fom, const double *init,
+                          const unsigned char *fixed_in, double *ttn, int max_sweeps, int *sweeps)
+{
+    fmm_state s;
+    memset(&s, 0, sizeof s);
+    s.g = g; s.veln = veln;
+    s.nnr = g->nnr; s.nnx = g->nnx; s.nnz = g->nnz;
+    s.NZ2 = g->nnz + 2; s.NX2 = g->nnx + 2;
+    const size_t npad = (size_t)s.NZ2 * (size_t)s.NX2 * (size_t)(g->nnr + 2);
+    s.ttn = (double *)malloc(npad * sizeof(double));
+    unsigned char *fixed = (unsigned char *)calloc(npad, 1);
+    if (!s.ttn || !fixed) { free(s.ttn); free(fixed); return -3; }
+    for (size_t q = 0; q < npad; ++q) s.ttn[q] = INFINITY;
+    for (int ir = 1; ir <= g->nnr; ++ir)
+        for (int ix = 1; ix <= g->nnx; ++ix)
+            for (int iz = 1; iz <= g->nnz; ++iz) {
+                const size_t q = (size_t)(iz - 1) + (size_t)g->nnz * ((size_t)(ix - 1) + (size_t)g->nnx * (size_t)(ir - 1));
+                TT(&s, iz, ix, ir) = init[q];
+                fixed[TI(&s, iz, ix, ir)] = fixed_in[q];
+            }
+    return fixed_point_run(&s, fixed, fom, ttn, max_sweeps, sweeps);
+}
+
+/* Gauss-Seidel sweeps in the eight alternating orders until no value
+ * changes; fixed nodes keep their values.  Frees s->ttn and fixed. */
+static int fixed_point_run(fmm_state *s_, unsigned char *fixed, int fom, double *ttn, int max_sweeps, int *sweeps)
+{
+    fmm_state s = *s_;
+    const orc_grid *g = s.g;
     int it;
     int converged = 0;
     for (it = 0; it < max_sweeps; ++it) {
@@ -1158,4 +1193,126 @@ void orc_planewave_frame(const orc_grid *g, const orc_planewave *pw, double *fra
             frame[(size_t)(iz - 1) + (size_t)g->nnz * (size_t)(ix - 1)] = pw->t0 + pw->p * d;
         }
     }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Point sources (no reference counterpart; restates the GPU library's      */
+/* start of a local-event solve, csrc/point.cu and fm3dt_solve_point)       */
+/* ------------------------------------------------------------------------ */
+static double node_slow(const orc_grid *g, const double *veln, int ir, int ix, int iz)
+{
+    /* 0-based node (ir, ix, iz) -> padded veln with 1-based indices */
+    return 1.0 / veln[VELN(g, iz + 1, ix + 1, ir + 1)];
+}
+
+static void to_cart(double r, double th, double ph, double *x, double *y, double *z)
+{
+    const double st = sin(th);
+    *x = r * st * cos(ph);
+    *y = r * st * sin(ph);
+    *z = r * cos(th);
+}
+
+/* straight-ray times on box nodes b (0-based, inclusive) of a field */
+static void point_analytic(const orc_grid *g, const double *veln, double h, double th, double ph, const int b[6],
+                           double *field)
+{
+    const double fr = (g->rgor - h) / g->dnr, fx = (th - g->rgox) / g->dnx, fz = (ph - g->rgoz) / g->dnz;
+    int ir = (int)floor(fr), ix = (int)floor(fx), iz = (int)floor(fz);
+    if (ir < 0) ir = 0;
+    if (ir > g->nnr - 2) ir = g->nnr - 2;
+    if (ix < 0) ix = 0;
+    if (ix > g->nnx - 2) ix = g->nnx - 2;
+    if (iz < 0) iz = 0;
+    if (iz > g->nnz - 2) iz = g->nnz - 2;
+    const double ar = fr - ir, ax = fx - ix, az = fz - iz;
+    double ss = 0.0;
+    for (int c = 0; c < 8; ++c) {
+        const int dr = (c >> 2) & 1, dx = (c >> 1) & 1, dz = c & 1;
+        const double w = (dr ? ar : 1.0 - ar) * (dx ? ax : 1.0 - ax) * (dz ? az : 1.0 - az);
+        ss = ss + w * node_slow(g, veln, ir + dr, ix + dx, iz + dz);
+    }
+    double xs, ys, zs;
+    to_cart(g->earth + h, th, ph, &xs, &ys, &zs);
+    for (int kr = b[0]; kr <= b[1]; ++kr)
+        for (int kx = b[2]; kx <= b[3]; ++kx)
+            for (int kz = b[4]; kz <= b[5]; ++kz) {
+                double xn, yn, zn;
+                to_cart(g->earth + (g->rgor - (double)kr * g->dnr), g->rgox + (double)kx * g->dnx,
+                        g->rgoz + (double)kz * g->dnz, &xn, &yn, &zn);
+                const double d = sqrt((xn - xs) * (xn - xs) + (yn - ys) * (yn - ys) + (zn - zs) * (zn - zs));
+                field[((size_t)kr * g->nnx + kx) * g->nnz + kz] = d * (0.5 * (ss + node_slow(g, veln, kr, kx, kz)));
+            }
+}
+
+int orc_point_start(const orc_grid *g, const double *velv, const double *veln, int fom, double h, double th,
+                    double ph, int refine, int extent, double *init, unsigned char *fixed)
+{
+    const int n[3] = {g->nnr, g->nnx, g->nnz};
+    const double f[3] = {(g->rgor - h) / g->dnr, (th - g->rgox) / g->dnx, (ph - g->rgoz) / g->dnz};
+    int box[6], fix[6];
+    for (int a = 0; a < 3; ++a) {
+        if (!(f[a] >= 0.0 && f[a] < (double)(n[a] - 1))) return -5;
+        const int c = (int)floor(f[a]);
+        const int lo = c - extent + 1 > 0 ? c - extent + 1 : 0;
+        const int hi = c + extent < n[a] - 1 ? c + extent : n[a] - 1;
+        box[2 * a] = lo;
+        box[2 * a + 1] = hi;
+        fix[2 * a] = (refine && lo > 0) ? lo + 1 : lo;
+        fix[2 * a + 1] = (refine && hi < n[a] - 1) ? hi - 1 : hi;
+    }
+    const size_t N = (size_t)g->nnr * g->nnx * g->nnz;
+    for (size_t q = 0; q < N; ++q) { init[q] = INFINITY; fixed[q] = 0; }
+    if (!refine) {
+        point_analytic(g, veln, h, th, ph, box, init);
+    } else {
+        orc_grid fg = *g;
+        fg.nnr = (box[1] - box[0]) * refine + 1;
+        fg.nnx = (box[3] - box[2]) * refine + 1;
+        fg.nnz = (box[5] - box[4]) * refine + 1;
+        fg.rgor = g->rgor - (double)box[0] * g->dnr;
+        fg.rgox = g->rgox + (double)box[2] * g->dnx;
+        fg.rgoz = g->rgoz + (double)box[4] * g->dnz;
+        fg.dnr = g->dnr / refine;
+        fg.dnx = g->dnx / refine;
+        fg.dnz = g->dnz / refine;
+        const size_t Nf = (size_t)fg.nnr * fg.nnx * fg.nnz;
+        const size_t npf = (size_t)(fg.nnr + 3) * (fg.nnx + 3) * (fg.nnz + 3);
+        double *vf = (double *)malloc(npf * sizeof(double));
+        double *tf = (double *)malloc(Nf * sizeof(double));
+        double *of = (double *)malloc(Nf * sizeof(double));
+        unsigned char *xf = (unsigned char *)calloc(Nf, 1);
+        if (!vf || !tf || !of || !xf) { free(vf); free(tf); free(of); free(xf); return -3; }
+        orc_gridder(&fg, velv, vf, NULL);
+        const int nf[3] = {fg.nnr, fg.nnx, fg.nnz};
+        const double ff[3] = {(fg.rgor - h) / fg.dnr, (th - fg.rgox) / fg.dnx, (ph - fg.rgoz) / fg.dnz};
+        int fb[6];
+        for (int a = 0; a < 3; ++a) {
+            int c = (int)floor(ff[a]);
+            if (c < 0) c = 0;
+            if (c > nf[a] - 2) c = nf[a] - 2;
+            fb[2 * a] = c - 1 > 0 ? c - 1 : 0;
+            fb[2 * a + 1] = c + 2 < nf[a] - 1 ? c + 2 : nf[a] - 1;
+        }
+        for (size_t q = 0; q < Nf; ++q) tf[q] = INFINITY;
+        point_analytic(&fg, vf, h, th, ph, fb, tf);
+        for (int kr = fb[0]; kr <= fb[1]; ++kr)
+            for (int kx = fb[2]; kx <= fb[3]; ++kx)
+                for (int kz = fb[4]; kz <= fb[5]; ++kz) xf[((size_t)kr * fg.nnx + kx) * fg.nnz + kz] = 1;
+        const int rc = orc_fixed_point_field(&fg, vf, fom, tf, xf, of, 100000, NULL);
+        if (rc == 0)
+            for (int kr = box[0]; kr <= box[1]; ++kr)
+                for (int kx = box[2]; kx <= box[3]; ++kx)
+                    for (int kz = box[4]; kz <= box[5]; ++kz) {
+                        const size_t q = ((size_t)((kr - box[0]) * refine) * fg.nnx + (size_t)((kx - box[2]) * refine)) *
+                                             fg.nnz + (size_t)((kz - box[4]) * refine);
+                        init[((size_t)kr * g->nnx + kx) * g->nnz + kz] = of[q];
+                    }
+        free(vf); free(tf); free(of); free(xf);
+        if (rc != 0) return rc;
+    }
+    for (int kr = fix[0]; kr <= fix[1]; ++kr)
+        for (int kx = fix[2]; kx <= fix[3]; ++kx)
+            for (int kz = fix[4]; kz <= fix[5]; ++kz) fixed[((size_t)kr * g->nnx + kx) * g->nnz + kz] = 1;
+    return 0;
 }

@@ -85,6 +85,21 @@ int orc_fmm(const orc_grid *g, const double *veln, int fom, const double *bottom
 int orc_fixed_point(const orc_grid *g, const double *veln, int fom, const double *bottom,
                     double *ttn, int max_sweeps, int *sweeps);
 
+/* The same fixed point from an arbitrary start: init (ttn layout, INFINITY =
+ * unset) and fixed (one byte per node, 1 = keep the init value). */
+int orc_fixed_point_field(const orc_grid *g, const double *veln, int fom, const double *init,
+                          const unsigned char *fixed, double *ttn, int max_sweeps, int *sweeps);
+
+/* Start of a point-source solve (no reference counterpart: a restatement of
+ * the GPU library's fm3dt_solve_point): a box of 2*extent nodes per axis
+ * around the source cell with straight-ray times (refine = 0, all fixed) or
+ * the times of a refine-times finer grid over the box solved from a
+ * straight-ray start (the box without its outer layer fixed).  Source at
+ * height h km, colatitude th, longitude ph (radians).  Returns -5 if the
+ * source lies outside the grid. */
+int orc_point_start(const orc_grid *g, const double *velv, const double *veln, int fom, double h, double th,
+                    double ph, int refine, int extent, double *init, unsigned char *fixed);
+
 /* Receiver traveltimes (F:7040-7248): trilinear interpolation accumulated
  * in single precision.  Returns 0, or -(1+k) if receiver k lies outside the
  * propagation grid. */

@@ -154,10 +154,15 @@ int ensure_planes(fm3dt_ctx *ctx, int shape)
     return FM3DT_OK;
 }
 
-// resume: keep the current fields (no initialisation, no sweep) and run the
-// rounds with every tile active.
-int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, bool resume = false)
+// How a solve starts: from boundary frames (initialisation, sweep, rounds),
+// from the current fields (resume: rounds with every tile active), or from
+// point-source boxes the caller already wrote (rounds from the boxes' tiles).
+enum SolveMode { kFrames = 0, kResume = 1, kPoint = 2 };
+
+int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
 {
+    const bool resume = mode == kResume;
+    const bool point = mode == kPoint || (resume && ctx->last_point);
     cudaStream_t s = ctx->stream;
     const Geom &g = ctx->g;
     cudaEvent_t ev0, ev1, sw0, sw1;
@@ -166,9 +171,9 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, bool resume = false)
     CK(cudaEventCreate(&sw0));
     CK(cudaEventCreate(&sw1));
     CK(cudaEventRecord(ev0, s));
-    const bool do_sweep = ctx->sweep && !resume;
+    const bool do_sweep = ctx->sweep && mode == kFrames;
 
-    if (!resume) {
+    if (mode == kFrames) {
         launch_fill_inf(ctx->d_T, (size_t)nev * ctx->N, ctx->prec, s);
         launch_finalize_frames(g, nev, ctx->prec, ctx->d_frames, ctx->d_T, ctx->d_frozen, ctx->d_base, s);
         launch_sweep_directions(g, nev, ctx->d_frames, ctx->d_dir, s);
@@ -186,6 +191,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, bool resume = false)
     auto fill_field = [&](auto &f, auto *T, auto *sl, auto *hx, auto *hz, auto *wx, auto *wz) {
         f.T = T; f.s = sl; f.hx = hx; f.hz = hz; f.wx = wx; f.wz = wz;
         f.frozen = ctx->d_frozen;
+        f.box = point ? ctx->d_box : nullptr;
         f.nnr = g.nnr; f.nnx = g.nnx; f.nnz = g.nnz;
         f.ntr = ntr; f.ntx = ntx; f.ntz = ntz;
         f.tiles_per_event = tpe;
@@ -249,7 +255,11 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, bool resume = false)
     CK(cudaMemsetAsync(ctx->d_count[1], 0, sizeof(int), s));
     CK(cudaMemsetAsync(ctx->d_stats, 0, 3 * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->d_trace, 0, 2 * sizeof(unsigned long long) * fm3dt_ctx::kTraceRounds, s));
-    launch_initial_tiles(nev, tpe, first, cnt, ctx->d_list[0], ctx->d_count[0], ctx->d_flag, s);
+    if (mode == kPoint)
+        launch_initial_tiles_box(nev, tpe, ntx, ntz, ts.tr, ts.tx, ts.tz, ctx->d_box_init, ctx->d_list[0],
+                                 ctx->d_count[0], ctx->d_flag, s);
+    else
+        launch_initial_tiles(nev, tpe, first, cnt, ctx->d_list[0], ctx->d_count[0], ctx->d_flag, s);
     ctx->launches += 1;
     CKL();
 
@@ -321,6 +331,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, bool resume = false)
     cudaEventDestroy(sw1);
     ctx->nev_solved = nev;
     ctx->last_rounds = rounds;
+    ctx->last_point = point ? 1 : 0;
     if (st) {
         st->rounds = rounds;
         st->converged = done ? 1 : 0;
@@ -336,6 +347,24 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, bool resume = false)
     }
     if (!done) return fail(ctx, FM3DT_ENOCONV, "solver round limit reached before convergence");
     return FM3DT_OK;
+}
+
+// Replaces a context's grid geometry (same node counts): the refined source
+// grids move with each source.
+int set_geometry(fm3dt_ctx *ctx, const Geom &g)
+{
+    ctx->g = g;
+    ctx->hr = g.dnr;
+    ctx->have_velocity = 0;
+    return ctx->prec == FM3DT_FP64 ? upload_geometry<double>(ctx) : upload_geometry<float>(ctx);
+}
+
+// A refined source grid solves with its parent's tuning, without the sweep.
+void inherit_tuning(fm3dt_ctx *fc, const fm3dt_ctx *parent)
+{
+    fc->shape = parent->shape;
+    fc->max_passes = parent->max_passes;
+    fc->sweep = 0;
 }
 
 int check_ready(fm3dt_ctx *ctx, int nev)
@@ -423,6 +452,8 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMalloc(&ctx->d_stats, 3 * sizeof(unsigned long long)));
     CKC(cudaMalloc(&ctx->d_trace, 2 * sizeof(unsigned long long) * fm3dt_ctx::kTraceRounds));
     CKC(cudaMalloc(&ctx->d_params, 4 * ctx->maxev * sizeof(double)));
+    CKC(cudaMalloc(&ctx->d_box, 6 * ctx->maxev * sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_box_init, 6 * ctx->maxev * sizeof(int)));
     CKC(cudaMallocHost(&ctx->h_count, sizeof(int)));
     CKC(cudaMallocHost(&ctx->h_stats, 3 * sizeof(unsigned long long)));
     CKC(cudaMemset(ctx->d_base, 0, ctx->maxev * sizeof(double)));
@@ -475,7 +506,7 @@ int fm3dt_solve_resume(fm3dt_ctx *ctx, fm3dt_status *st)
 {
     if (!ctx) return FM3DT_EINVAL;
     if (ctx->nev_solved < 1) return fail(ctx, FM3DT_ESTATE, "no solved events to resume");
-    return solve_common(ctx, ctx->nev_solved, st, true);
+    return solve_common(ctx, ctx->nev_solved, st, kResume);
 }
 
 int fm3dt_solve_planewave(fm3dt_ctx *ctx, int nev, const double *params, fm3dt_status *st)
@@ -495,6 +526,126 @@ int fm3dt_solve_planewave(fm3dt_ctx *ctx, int nev, const double *params, fm3dt_s
     ctx->launches += 1;
     CKL();
     return solve_common(ctx, nev, st);
+}
+
+int fm3dt_solve_point(fm3dt_ctx *ctx, int nev, const double *src, int refine, int extent, fm3dt_status *st)
+{
+    int rc = check_ready(ctx, nev);
+    if (rc) return rc;
+    if (!src) return fail(ctx, FM3DT_EINVAL, "null sources");
+    if (refine != 0 && (refine < 2 || refine > 16)) return fail(ctx, FM3DT_EINVAL, "refine must be 0 or 2..16");
+    if (extent < (refine ? 2 : 1) || extent > 16)
+        return fail(ctx, FM3DT_EINVAL, refine ? "extent must be 2..16 with a refined grid" : "extent must be 1..16");
+    const Geom &g = ctx->g;
+    cudaStream_t s = ctx->stream;
+    std::vector<PointSource> ps(nev);
+    std::vector<int> box(6 * (size_t)nev), fixed(6 * (size_t)nev);
+    for (int e = 0; e < nev; ++e) {
+        const PointSource p{src[3 * e], src[3 * e + 1], src[3 * e + 2]};
+        const double f[3] = {(g.rgor - p.h) / g.dnr, (p.th - g.rgox) / g.dnx, (p.ph - g.rgoz) / g.dnz};
+        const int n[3] = {g.nnr, g.nnx, g.nnz};
+        for (int a = 0; a < 3; ++a) {
+            if (!(f[a] >= 0.0 && f[a] < (double)(n[a] - 1)))
+                return fail(ctx, FM3DT_ERANGE, "source " + std::to_string(e + 1) + " lies outside the grid");
+            const int c = (int)std::floor(f[a]);
+            const int lo = std::max(0, c - extent + 1), hi = std::min(n[a] - 1, c + extent);
+            box[6 * e + 2 * a] = lo;
+            box[6 * e + 2 * a + 1] = hi;
+            // with a refined grid the box's outer layer is left to the coarse
+            // solve (the fine solve saw nothing outside the box), except on
+            // the faces of the grid itself
+            fixed[6 * e + 2 * a] = (refine && lo > 0) ? lo + 1 : lo;
+            fixed[6 * e + 2 * a + 1] = (refine && hi < n[a] - 1) ? hi - 1 : hi;
+        }
+        ps[e] = p;
+    }
+    const size_t rs = rsize(ctx->prec);
+    launch_fill_inf(ctx->d_T, (size_t)nev * ctx->N, ctx->prec, s);
+    CK(cudaMemsetAsync(ctx->d_base, 0, (size_t)nev * sizeof(double), s));
+    ctx->launches += 1;
+    if (!refine) {
+        PointSource *d_src = nullptr;
+        CK(cudaMallocAsync(&d_src, nev * sizeof(PointSource), s));
+        CK(cudaMemcpyAsync(d_src, ps.data(), nev * sizeof(PointSource), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->d_box, box.data(), box.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->d_box_init, box.data(), box.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        launch_point_analytic(g, ctx->prec, ctx->d_veln, nev, d_src, ctx->d_box, ctx->d_T, s);
+        ctx->launches += 1;
+        CKL();
+        CK(cudaFreeAsync(d_src, s));
+    } else {
+        CK(cudaStreamSynchronize(s));
+        for (int e = 0; e < nev; ++e) {
+            const int *b = &box[6 * e];
+            const int fn[3] = {(b[1] - b[0]) * refine + 1, (b[3] - b[2]) * refine + 1, (b[5] - b[4]) * refine + 1};
+            fm3dt_ctx *fc = nullptr;
+            for (auto &fe : ctx->fine)
+                if (fe.nnr == fn[0] && fe.nnx == fn[1] && fe.nnz == fn[2]) fc = fe.ctx;
+            if (!fc) {
+                fm3dt_grid_desc fd = ctx->desc;
+                fd.nnr = fn[0];
+                fd.nnx = fn[1];
+                fd.nnz = fn[2];
+                fd.max_events = 1;
+                rc = fm3dt_ctx_create(&fd, &fc);
+                if (rc != FM3DT_OK) return fail(ctx, rc, std::string("refined grid: ") + fm3dt_last_error(nullptr));
+                inherit_tuning(fc, ctx);
+                ctx->fine.push_back({fn[0], fn[1], fn[2], fc});
+            }
+            // the refined grid: node (0,0,0) on the box corner, 1/refine spacing
+            Geom fg = g;
+            fg.nnr = fn[0];
+            fg.nnx = fn[1];
+            fg.nnz = fn[2];
+            fg.rgor = g.rgor - (double)b[0] * g.dnr;
+            fg.rgox = g.rgox + (double)b[2] * g.dnx;
+            fg.rgoz = g.rgoz + (double)b[4] * g.dnz;
+            fg.dnr = g.dnr / refine;
+            fg.dnx = g.dnx / refine;
+            fg.dnz = g.dnz / refine;
+            rc = set_geometry(fc, fg);
+            if (rc != FM3DT_OK) return fail(ctx, rc, std::string("refined grid: ") + fc->err);
+            CK(cudaMemcpyAsync(fc->d_velv, ctx->d_velv,
+                               (size_t)(g.nvr + 2) * (g.nvx + 2) * (g.nvz + 2) * sizeof(double),
+                               cudaMemcpyDeviceToDevice, fc->stream));
+            launch_gridder(fg, fc->d_velv, fc->d_veln, fc->stream);
+            launch_slowness(fg, fc->d_veln, fc->d_s, fc->prec, fc->stream);
+            fc->have_velocity = 1;
+            // straight-ray start within two fine cells of the source
+            int fb[6];
+            const double ff[3] = {(fg.rgor - ps[e].h) / fg.dnr, (ps[e].th - fg.rgox) / fg.dnx,
+                                  (ps[e].ph - fg.rgoz) / fg.dnz};
+            for (int a = 0; a < 3; ++a) {
+                const int c = std::min(std::max((int)std::floor(ff[a]), 0), fn[a] - 2);
+                fb[2 * a] = std::max(0, c - 1);
+                fb[2 * a + 1] = std::min(fn[a] - 1, c + 2);
+            }
+            launch_fill_inf(fc->d_T, fc->N, fc->prec, fc->stream);
+            CK(cudaMemsetAsync(fc->d_base, 0, sizeof(double), fc->stream));
+            CK(cudaMemcpyAsync(fc->d_box, fb, sizeof fb, cudaMemcpyHostToDevice, fc->stream));
+            CK(cudaMemcpyAsync(fc->d_box_init, fb, sizeof fb, cudaMemcpyHostToDevice, fc->stream));
+            PointSource *d_src = nullptr;
+            CK(cudaMallocAsync(&d_src, sizeof(PointSource), fc->stream));
+            CK(cudaMemcpyAsync(d_src, &ps[e], sizeof(PointSource), cudaMemcpyHostToDevice, fc->stream));
+            launch_point_analytic(fg, fc->prec, fc->d_veln, 1, d_src, fc->d_box, fc->d_T, fc->stream);
+            fc->launches += 4;
+            CK(cudaFreeAsync(d_src, fc->stream));
+            fm3dt_status fst{};
+            rc = solve_common(fc, 1, &fst, kPoint);
+            ctx->launches += fc->launches;
+            fc->launches = 0;
+            if (rc != FM3DT_OK) return fail(ctx, rc, std::string("refined grid solve: ") + fc->err);
+            launch_point_sample(ctx->prec, fc->d_T, fn[1], fn[2], refine, b, g.nnx, g.nnz,
+                                (char *)ctx->d_T + (size_t)e * ctx->N * rs, s);
+            ctx->launches += 1;
+            CKL();
+        }
+        // fixed: the box without its outer layer; active at the start: every
+        // tile the sampled box touches
+        CK(cudaMemcpyAsync(ctx->d_box, fixed.data(), fixed.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->d_box_init, box.data(), box.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    }
+    return solve_common(ctx, nev, st, kPoint);
 }
 
 int fm3dt_receiver_times(fm3dt_ctx *ctx, int nrc, const double *rcr, const double *rcx, const double *rcz,
@@ -543,6 +694,8 @@ int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double 
     if (!ctx || nrc < 0 || (nrc > 0 && (!rcr || !rcx || !rcz))) return FM3DT_EINVAL;
     if (ctx->nev_solved < 1) return fail(ctx, FM3DT_ESTATE, "no solved events");
     if (!ctx->have_velocity) return fail(ctx, FM3DT_ESTATE, "no velocity model");
+    if (ctx->last_point)
+        return fail(ctx, FM3DT_ESTATE, "rays are traced through teleseismic (boundary-frame) solves only");
     const bool want_rows = cols != nullptr && vals != nullptr;
     if (want_rows && !row_ptr) return FM3DT_EINVAL;
     if (nrc == 0) return FM3DT_OK;
@@ -773,6 +926,9 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_stats);
     cudaFree(ctx->d_trace);
     cudaFree(ctx->d_params);
+    cudaFree(ctx->d_box);
+    cudaFree(ctx->d_box_init);
+    for (auto &f : ctx->fine) fm3dt_ctx_destroy(f.ctx);
     if (ctx->h_count) cudaFreeHost(ctx->h_count);
     if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

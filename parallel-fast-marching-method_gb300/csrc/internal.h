@@ -35,6 +35,8 @@ struct FieldArgs {
     const R *hz, *wz;           // [nnr*nnx]  r*sin(theta)*dphi and its inverse square
     R hr, wr;                   // dr and 1/dr^2
     const uint8_t *frozen;      // [E][nnx*nnz] fixed bottom-layer nodes
+    const int *box;             // [E][6] fixed node box r0,r1,x0,x1,z0,z1 (inclusive) of point
+                                // sources, or null
     int nnr, nnx, nnz;
     int ntr, ntx, ntz;          // tiles per axis
     int tiles_per_event;
@@ -103,10 +105,19 @@ void launch_fill_inf(void *T, size_t n, int prec, cudaStream_t st);
 void launch_sweep_directions(const Geom &g, int nev, const double *frames, int *dir, cudaStream_t st);
 void launch_initial_tiles(int nev, int tiles_per_event, int first_tile, int count_per_event,
                           int *list, int *count, int *flag, cudaStream_t st);
+void launch_initial_tiles_box(int nev, int tiles_per_event, int ntx, int ntz, int tr, int tx, int tz,
+                              const int *box, int *list, int *count, int *flag, cudaStream_t st);
 void launch_to_absolute(const Geom &g, int prec, const void *T, size_t offset, double base, double *out,
                         cudaStream_t st);
 void launch_from_absolute(const Geom &g, int prec, const double *in, double base, void *T, size_t offset,
                           cudaStream_t st);
+
+// point.cu -- point sources
+struct PointSource { double h, th, ph; };   // height km, colatitude rad, longitude rad
+void launch_point_analytic(const Geom &g, int prec, const double *veln, int nev, const PointSource *src,
+                           const int *box, void *T, cudaStream_t st);
+void launch_point_sample(int prec, const void *Tf, int nnx_f, int nnz_f, int refine, const int box[6], int nnx,
+                         int nnz, void *T_event, cudaStream_t st);
 
 // receivers.cu
 struct RecCell { int irr, irx, irz, pad; double drr, drx, drz; };
@@ -184,4 +195,10 @@ struct fm3dt_ctx {
     struct Graph { int shape, nev, rounds; cudaGraphExec_t exec; };
     std::vector<Graph> graphs;
     std::vector<cudaEvent_t> round_events;   // start/stop pairs of round kernels
+    // point sources: fixed node boxes, and the refined source grids' contexts
+    int *d_box = nullptr;         // [maxev][6] fixed nodes
+    int *d_box_init = nullptr;    // [maxev][6] nodes whose tiles start active
+    int last_point = 0;           // the last solve started from point sources
+    struct Fine { int nnr, nnx, nnz; fm3dt_ctx *ctx; };
+    std::vector<Fine> fine;
 };

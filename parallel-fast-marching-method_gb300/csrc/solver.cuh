@@ -151,6 +151,10 @@ struct Tile {
 
     static __device__ __forceinline__ bool frozen(const FieldArgs<R> &a, int e, int gr, int gx, int gz)
     {
+        if (a.box) {
+            const int *b = a.box + 6 * e;
+            return gr >= b[0] && gr <= b[1] && gx >= b[2] && gx <= b[3] && gz >= b[4] && gz <= b[5];
+        }
         return gr == a.nnr - 1 && a.frozen[(size_t)e * a.nnx * a.nnz + (size_t)gx * a.nnz + gz] != 0;
     }
 };

@@ -55,7 +55,7 @@ class Status(C.Structure):
 
 EXPORTS = [
     "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_resume",
-    "fm3dt_solve_planewave",
+    "fm3dt_solve_planewave", "fm3dt_solve_point",
     "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
     "fm3dt_set_tuning", "fm3dt_set_sweep_shape", "fm3dt_round_trace", "fm3dt_tile_shapes", "fm3dt_tile_shape",
     "fm3dt_launch_count",
@@ -80,6 +80,7 @@ def load(path: str | None = None):
     L.fm3dt_set_velocity.argtypes = [vp, dp]
     L.fm3dt_solve.argtypes = [vp, C.c_int, dp, C.POINTER(Status)]
     L.fm3dt_solve_planewave.argtypes = [vp, C.c_int, dp, C.POINTER(Status)]
+    L.fm3dt_solve_point.argtypes = [vp, C.c_int, dp, C.c_int, C.c_int, C.POINTER(Status)]
     L.fm3dt_solve_device.argtypes = [vp, C.c_int, C.c_void_p, C.POINTER(Status)]
     L.fm3dt_solve_resume.argtypes = [vp, C.POINTER(Status)]
     L.fm3dt_receiver_times.argtypes = [vp, C.c_int, dp, dp, dp, C.POINTER(C.c_float)]
@@ -257,6 +258,15 @@ class Solver:
         st = Status()
         self._check(self._L.fm3dt_solve_planewave(self._ctx, len(params), _d(params), C.byref(st)))
         self.nev = len(params)
+        return st.as_dict()
+
+    def solve_point(self, src, refine: int = 5, extent: int = 3) -> dict:
+        """Point sources: src is (nev, 3) of (height km, colatitude rad,
+        longitude rad); see fm3dt_solve_point."""
+        src = np.ascontiguousarray(src, dtype=np.float64).reshape(-1, 3)
+        st = Status()
+        self._check(self._L.fm3dt_solve_point(self._ctx, len(src), _d(src), int(refine), int(extent), C.byref(st)))
+        self.nev = len(src)
         return st.as_dict()
 
     def receiver_times(self, rcr, rcx, rcz) -> np.ndarray:

@@ -28,6 +28,7 @@ SOURCES = {
     "boundary.cu": ["-fmad=false"],
     "receivers.cu": ["-fmad=false"],
     "rays.cu": ["-fmad=false"],
+    "point.cu": ["-fmad=false"],
     "solver_f32.cu": ["-fmad=false"],
     "solver_f64.cu": ["-fmad=false"],
     "capi.cu": [],
