@@ -272,7 +272,7 @@ def run_ours(a):
     else:
         tuned = autotune.autotune(solver, fptr, nev, device=True)
     shape = fm3dt.tile_shapes()[tuned[0]]
-    sweep_shape_dims = fm3dt.tile_shapes()[tuned[2]]
+    sweep_shape_dims = fm3dt.sweep_shapes()[tuned[2]]
 
     for _ in range(a.warmup):
         solver.solve_ptr(nev, fptr, True)

@@ -185,10 +185,16 @@ int fm3dt_set_times(fm3dt_ctx *ctx, int event, int nev_total, const double *ttn)
 
 /* Solver tuning: tile shape index, in-tile pass cap and round cap (0 keeps
  * the current value), directional sweep before the rounds (1 on, 0 off,
- * -1 keep).  None of these changes the converged field. */
+ * -1 keep; 2 on, and a streaming sweep is followed by a second, verifying
+ * sweep that queues only the tiles still changing instead of starting the
+ * rounds with every tile).  None of these changes the converged field. */
 int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rounds, int sweep);
 
-/* Tile shape of the directional sweep (independent of the rounds' shape). */
+/* Shape of the directional sweep (independent of the rounds' shape): a tile
+ * shape index 0..count-1 of fm3dt_tile_shapes (tile sweep), or count +
+ * 0 / 1 for the streaming sweep, one warp per 4x8 / 2x16 block of
+ * (theta, phi) columns streamed over the whole height.  None of these
+ * changes the converged field. */
 int fm3dt_set_sweep_shape(fm3dt_ctx *ctx, int tile_shape);
 
 /* Per-round trace of the last solve: tiles processed and node updates of

@@ -154,6 +154,30 @@ int ensure_planes(fm3dt_ctx *ctx, int shape)
     return FM3DT_OK;
 }
 
+// Column-block hyperplanes x' + z' = h of a streaming sweep shape (swept
+// block coordinates), packed x'<<16 | z'.
+int ensure_block_planes(fm3dt_ctx *ctx, int sweep_shape)
+{
+    auto &P = ctx->planes[sweep_shape];
+    if (P.shape == sweep_shape) return FM3DT_OK;
+    const StreamShape ss = kStreamShapes[sweep_shape - kNumShapes];
+    const int nbx = (ctx->g.nnx + ss.sx - 1) / ss.sx, nbz = (ctx->g.nnz + ss.sz - 1) / ss.sz;
+    if (nbx > 32767 || nbz > 65535) return fail(ctx, FM3DT_EINVAL, "too many column blocks along one axis");
+    const int H = nbx + nbz - 1;
+    std::vector<int> flat;
+    P.off.assign(H, 0);
+    P.cnt.assign(H, 0);
+    for (int h = 0; h < H; ++h) {
+        P.off[h] = (int)flat.size();
+        for (int b = std::max(0, h - nbz + 1); b <= std::min(h, nbx - 1); ++b) flat.push_back((b << 16) | (h - b));
+        P.cnt[h] = (int)flat.size() - P.off[h];
+    }
+    CK(cudaMalloc(&P.d_tiles, flat.size() * sizeof(int)));
+    CK(cudaMemcpy(P.d_tiles, flat.data(), flat.size() * sizeof(int), cudaMemcpyHostToDevice));
+    P.shape = sweep_shape;
+    return FM3DT_OK;
+}
+
 // How a solve starts: from boundary frames (initialisation, sweep, rounds),
 // from the current fields (resume: rounds with every tile active), or from
 // point-source boxes the caller already wrote (rounds from the boxes' tiles).
@@ -211,8 +235,54 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
 
     // 1. directional sweep, one launch per tile hyperplane
     int sweep_launches = 0;
+    bool verified = false;
     CK(cudaEventRecord(sw0, s));
-    if (do_sweep) {
+    if (do_sweep && ctx->sweep_shape >= kNumShapes) {
+        // streaming sweep: one launch per column-block hyperplane
+        const int idx = ctx->sweep_shape - kNumShapes;
+        int rc = ensure_block_planes(ctx, ctx->sweep_shape);
+        if (rc) return rc;
+        const auto &P = ctx->planes[ctx->sweep_shape];
+        const StreamShape ss = kStreamShapes[idx];
+        const int nbx = (g.nnx + ss.sx - 1) / ss.sx, nbz = (g.nnz + ss.sz - 1) / ss.sz;
+        const int occ = ctx->prec == FM3DT_FP64 ? occupancy_stream_f64(idx) : occupancy_stream_f32(idx);
+        const int sgrid = std::max(1, occ) * sm_count();
+        // pass 0 sweeps from the boundary; pass 1 (verification) sweeps again
+        // and queues the rounds' tiles where a node still changed
+        const int passes = ctx->verify ? 2 : 1;
+        if (ctx->verify) {
+            CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
+            CK(cudaMemsetAsync(ctx->d_count[0], 0, sizeof(int), s));
+        }
+        for (int pass = 0; pass < passes; ++pass)
+            for (size_t h = 0; h < P.off.size(); ++h) {
+                const long long items = (long long)P.cnt[h] * nev;
+                const int grid = (int)std::min<long long>(items, sgrid);
+                auto fill = [&](auto &a) {
+                    a.hp_blocks = P.d_tiles; a.hoff = P.off[h]; a.hcount = P.cnt[h];
+                    a.dir = ctx->d_dir; a.nev = nev; a.nbx = nbx; a.nbz = nbz;
+                    a.flag = pass ? ctx->d_flag : nullptr;
+                    a.list = ctx->d_list[0]; a.count = ctx->d_count[0];
+                    a.tr = ts.tr; a.tx = ts.tx; a.tz = ts.tz;
+                    a.ntr = ntr; a.ntx = ntx; a.ntz = ntz; a.tiles_per_event = tpe;
+                };
+                if (ctx->prec == FM3DT_FP64) {
+                    StreamArgs<double> a{};
+                    a.f = f64;
+                    fill(a);
+                    launch_stream_f64(idx, grid, a, s);
+                } else {
+                    StreamArgs<float> a{};
+                    a.f = f32;
+                    fill(a);
+                    launch_stream_f32(idx, grid, a, s);
+                }
+                ++sweep_launches;
+            }
+        ctx->launches += sweep_launches;
+        CKL();
+        verified = ctx->verify != 0;
+    } else if (do_sweep) {
         const int sshape = ctx->sweep_shape;
         int rc = ensure_planes(ctx, sshape);
         if (rc) return rc;
@@ -248,20 +318,23 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
 
     // 2. rounds until no tile changes: all tiles after a sweep, else the
     //    tiles whose nodes or 2-deep halos include the bottom layer
+    //    (or, after a verification sweep, the tiles it queued)
     const int tlo = (do_sweep || resume) ? 0 : std::max(0, (g.nnr - 3) / ts.tr);
     const int first = tlo * ntx * ntz;
     const int cnt = (ntr - tlo) * ntx * ntz;
-    CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
     CK(cudaMemsetAsync(ctx->d_count[1], 0, sizeof(int), s));
     CK(cudaMemsetAsync(ctx->d_stats, 0, 3 * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->d_trace, 0, 2 * sizeof(unsigned long long) * fm3dt_ctx::kTraceRounds, s));
-    if (mode == kPoint)
-        launch_initial_tiles_box(nev, tpe, ntx, ntz, ts.tr, ts.tx, ts.tz, ctx->d_box_init, ctx->d_list[0],
-                                 ctx->d_count[0], ctx->d_flag, s);
-    else
-        launch_initial_tiles(nev, tpe, first, cnt, ctx->d_list[0], ctx->d_count[0], ctx->d_flag, s);
-    ctx->launches += 1;
-    CKL();
+    if (!verified) {
+        CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
+        if (mode == kPoint)
+            launch_initial_tiles_box(nev, tpe, ntx, ntz, ts.tr, ts.tx, ts.tz, ctx->d_box_init, ctx->d_list[0],
+                                     ctx->d_count[0], ctx->d_flag, s);
+        else
+            launch_initial_tiles(nev, tpe, first, cnt, ctx->d_list[0], ctx->d_count[0], ctx->d_flag, s);
+        ctx->launches += 1;
+        CKL();
+    }
 
     const int bps = std::max(1, round_blocks_per_sm(shape, ctx->prec));
     const int grid = bps * sm_count();
@@ -343,7 +416,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         st->round_launches = rounds;
         st->sweep_ms = do_sweep ? sms : 0.0;
         st->sweep_launches = sweep_launches;
-        st->sweep_nodes = do_sweep ? (int64_t)nev * (int64_t)ctx->N : 0;
+        st->sweep_nodes = do_sweep ? (int64_t)nev * (int64_t)ctx->N * (verified ? 2 : 1) : 0;
     }
     if (!done) return fail(ctx, FM3DT_ENOCONV, "solver round limit reached before convergence");
     return FM3DT_OK;
@@ -852,14 +925,18 @@ int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rou
     ctx->shape = tile_shape;
     if (max_passes > 0) ctx->max_passes = max_passes;
     if (max_rounds > 0) ctx->max_rounds = max_rounds;
-    if (sweep >= 0) ctx->sweep = sweep ? 1 : 0;
+    if (sweep >= 0) {
+        ctx->sweep = sweep ? 1 : 0;
+        ctx->verify = sweep == 2 ? 1 : 0;
+    }
     return FM3DT_OK;
 }
 
 int fm3dt_set_sweep_shape(fm3dt_ctx *ctx, int tile_shape)
 {
     if (!ctx) return FM3DT_EINVAL;
-    if (tile_shape < 0 || tile_shape >= kNumShapes) return fail(ctx, FM3DT_EINVAL, "tile shape out of range");
+    if (tile_shape < 0 || tile_shape >= kNumSweepShapes)
+        return fail(ctx, FM3DT_EINVAL, "sweep shape out of range");
     ctx->sweep_shape = tile_shape;
     return FM3DT_OK;
 }

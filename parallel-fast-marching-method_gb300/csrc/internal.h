@@ -74,6 +74,35 @@ struct SweepArgs {
     int nev;
 };
 
+// Streaming sweep (stream.cuh): one warp per column block of SX x SZ
+// columns streamed over the whole height; sweep shape indices kNumShapes and
+// up select these blocks.
+struct StreamShape { int sx, sz; };
+constexpr int kNumStream = 2;
+constexpr StreamShape kStreamShapes[kNumStream] = {{4, 8}, {2, 16}};
+constexpr int kNumSweepShapes = kNumShapes + kNumStream;
+
+template <typename R>
+struct StreamArgs {
+    FieldArgs<R> f;
+    const int *hp_blocks;       // swept column-block coordinates (x' << 16 | z'), by hyperplane
+    int hoff, hcount;
+    const int *dir;             // [E] bit 0: sweep +theta, bit 1: sweep +phi
+    int nev;
+    int nbx, nbz;               // column blocks per axis
+    // verification sweep: when flag is set, every node whose value changes
+    // queues its round tile (recompute all) and, near a tile face, the face
+    // neighbour (that face changed) -- the first round's work list
+    int *flag, *list, *count;
+    int tr, tx, tz;             // the rounds' tile shape and tile counts
+    int ntr, ntx, ntz, tiles_per_event;
+};
+
+void launch_stream_f32(int idx, int grid, const StreamArgs<float> &a, cudaStream_t st);
+void launch_stream_f64(int idx, int grid, const StreamArgs<double> &a, cudaStream_t st);
+int occupancy_stream_f32(int idx);
+int occupancy_stream_f64(int idx);
+
 void launch_round_f64(int shape, int grid, const RoundArgs<double> &a, cudaStream_t st);
 void launch_round_f32(int shape, int grid, const RoundArgs<float> &a, cudaStream_t st);
 void launch_sweep_f64(int shape, int grid, const SweepArgs<double> &a, cudaStream_t st);
@@ -181,13 +210,14 @@ struct fm3dt_ctx {
     int max_passes = 64;
     int max_rounds = 0;           // 0 = automatic
     int sweep = 1;                // directional sweep before the rounds
-    int sweep_shape = 4;          // tile shape of the sweep (independent of the rounds')
+    int sweep_shape = fm3dt::kNumShapes;   // the sweep's shape: streaming 4x8 column blocks
+    int verify = 0;               // follow a streaming sweep by a verifying sweep (off: slower)
     unsigned long long *d_trace = nullptr;   // per-round tiles / node updates
     static constexpr int kTraceRounds = 8192;
     int last_rounds = 0;
     // tile hyperplanes of each shape (device list + host offsets)
     struct Planes { int shape = -1; int *d_tiles = nullptr; std::vector<int> off, cnt; };
-    Planes planes[fm3dt::kNumShapes];
+    Planes planes[fm3dt::kNumSweepShapes];   // tile hyperplanes, then column-block hyperplanes
     size_t flag_capacity = 0;     // tiles allocated for flags/lists
     int64_t launches = 0;
     std::string err;

@@ -37,3 +37,26 @@ int occupancy_sweep_f64(int shape)
 }
 
 }  // namespace fm3dt
+
+// streaming sweep
+#include "stream.cuh"
+
+namespace fm3dt {
+
+void launch_stream_f64(int idx, int grid, const StreamArgs<double> &a, cudaStream_t st)
+{
+#define C_(X, Z) StreamKernels<double, X, Z>::sweep(grid, a, st)
+    FM_STREAM_SWITCH(idx, C_)
+#undef C_
+}
+
+int occupancy_stream_f64(int idx)
+{
+    int r = 0;
+#define C_(X, Z) r = StreamKernels<double, X, Z>::occ()
+    FM_STREAM_SWITCH(idx, C_)
+#undef C_
+    return r;
+}
+
+}  // namespace fm3dt

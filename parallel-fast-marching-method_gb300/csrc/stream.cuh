@@ -1,0 +1,160 @@
+// stream.cuh -- streaming directional sweep (an alternative to the tile sweep
+// of solver.cuh).
+//
+// One warp owns a block of SX x SZ (theta, phi) columns and streams through
+// the whole height of the grid from the bottom face upward.  Lane (x', z')
+// updates layer r' at step r' + x' + z' (swept coordinates, as in the tile
+// sweep), so each node sees its upwind neighbours' new values; the ramp of
+// that wavefront (SX + SZ - 2 steps) is paid once per column block instead
+// of once per tile.  The layers the lanes are working on, plus the two
+// layers above and below and a two-column halo, sit in a shared-memory ring
+// of RING layers.  Column blocks go in hyperplanes of the event's sweep
+// direction (one launch per hyperplane); a block's upwind neighbours are in
+// earlier launches.  The sweep is only a good start for the rounds, which
+// reach the same fixed point from any start.
+#pragma once
+#include "solver.cuh"
+
+namespace fm3dt {
+
+template <int SX, int SZ>
+struct StreamRing {
+    static constexpr int need = SX + SZ + 4;
+    static constexpr int value = need <= 16 ? 16 : (need <= 32 ? 32 : 64);
+};
+
+template <typename R>
+__device__ __forceinline__ void stream_queue(const StreamArgs<R> &a, int w, int bits)
+{
+    if (!(atomicOr(&a.flag[w], bits | kQueued) & kQueued)) a.list[atomicAdd(a.count, 1)] = w;
+}
+
+// A node changed in the verification sweep: its tile recomputes every node,
+// and each face neighbour whose 2-deep halo holds the node recomputes the
+// nodes next to that face (the flag bits of the rounds).
+template <typename R>
+__device__ void stream_mark(const StreamArgs<R> &a, int e, int gr, int gx, int gz)
+{
+    const int ti = gr / a.tr, tj = gx / a.tx, tk = gz / a.tz;
+    const int ri = gr - ti * a.tr, xi = gx - tj * a.tx, zi = gz - tk * a.tz;
+    const int sl = a.ntx * a.ntz;
+    const int w = e * a.tiles_per_event + (ti * a.ntx + tj) * a.ntz + tk;
+    stream_queue(a, w, kFull);
+    if (ri < 2 && ti > 0) stream_queue(a, w - sl, kFaceDown);
+    if (ri >= a.tr - 2 && ti < a.ntr - 1) stream_queue(a, w + sl, kFaceUp);
+    if (xi < 2 && tj > 0) stream_queue(a, w - a.ntz, kFaceXp);
+    if (xi >= a.tx - 2 && tj < a.ntx - 1) stream_queue(a, w + a.ntz, kFaceXm);
+    if (zi < 2 && tk > 0) stream_queue(a, w - 1, kFaceZp);
+    if (zi >= a.tz - 2 && tk < a.ntz - 1) stream_queue(a, w + 1, kFaceZm);
+}
+
+template <typename R, int SX, int SZ>
+__global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
+{
+    static_assert(SX * SZ == 32, "one warp per column block");
+    constexpr int LX = SX + 4, LZ = SZ + 4, LAYER = LX * LZ;
+    constexpr int RING = StreamRing<SX, SZ>::value;
+    __shared__ R ring[RING * LAYER];
+    using TL = Tile<R, 1, SX, SZ>;
+    const FieldArgs<R> &f = a.f;
+    const int lane = threadIdx.x;
+    const int lx = lane / SZ, lz = lane % SZ;
+    const R INF = Lim<R>::inf();
+    const size_t N = (size_t)f.nnx * f.nnz * (size_t)f.nnr;
+    const long long count = (long long)a.hcount * a.nev;
+    for (long long item = blockIdx.x; item < count; item += gridDim.x) {
+        const int e = (int)(item / a.hcount);
+        const int j = (int)(item - (long long)e * a.hcount);
+        const int packed = a.hp_blocks[a.hoff + j];
+        const int bxp = packed >> 16, bzp = packed & 0xffff;
+        const int dir = a.dir[e];
+        const bool sx = dir & 1, sz = (dir >> 1) & 1;
+        const int x0 = (sx ? bxp : a.nbx - 1 - bxp) * SX;
+        const int z0 = (sz ? bzp : a.nbz - 1 - bzp) * SZ;
+        const int xs = sx ? lx : SX - 1 - lx;
+        const int zs = sz ? lz : SZ - 1 - lz;
+        const int gx = x0 + lx, gz = z0 + lz;
+        const bool colv = gx < f.nnx && gz < f.nnz;
+        R *Te = f.T + (size_t)e * N;
+        // layer rp (counted upward from the bottom) into its ring slot; unset
+        // outside the grid
+        auto load_layer = [&](int rp) {
+            R *dst = ring + ((rp + RING) & (RING - 1)) * LAYER;
+            const int gr = f.nnr - 1 - rp;
+            for (int q = lane; q < LAYER; q += 32) {
+                const int qx = x0 + q / LZ - 2, qz = z0 + q % LZ - 2;
+                R v = INF;
+                if (rp >= 0 && rp < f.nnr && qx >= 0 && qx < f.nnx && qz >= 0 && qz < f.nnz)
+                    v = __ldcg(Te + ((size_t)gr * f.nnx + qx) * f.nnz + qz);
+                dst[q] = v;
+            }
+        };
+        __syncwarp();
+        load_layer(-2);
+        load_layer(-1);
+        load_layer(0);
+        load_layer(1);
+        const int c = (lx + 2) * LZ + (lz + 2);
+        typename TL::Params pnext{};
+        if (colv && xs + zs == 0) pnext = TL::params_global(f, f.nnr - 1, gx, gz);
+        const int steps = f.nnr + SX + SZ - 2;
+        for (int step = 0; step < steps; ++step) {
+            load_layer(step + 2);
+            __syncwarp();
+            const int rp = step - xs - zs;
+            const typename TL::Params pcur = pnext;
+            // the next node's slowness and spacings, one step ahead
+            if (colv && rp + 1 >= 0 && rp + 1 < f.nnr) pnext = TL::params_global(f, f.nnr - 2 - rp, gx, gz);
+            if (colv && rp >= 0 && rp < f.nnr) {
+                const int gr = f.nnr - 1 - rp;
+                if (!TL::frozen(f, e, gr, gx, gz)) {
+                    const R *L0 = ring + ((rp + RING) & (RING - 1)) * LAYER;
+                    const R *Lu1 = ring + ((rp + 1 + RING) & (RING - 1)) * LAYER;
+                    const R *Lu2 = ring + ((rp + 2 + RING) & (RING - 1)) * LAYER;
+                    const R *Ld1 = ring + ((rp - 1 + RING) & (RING - 1)) * LAYER;
+                    const R *Ld2 = ring + ((rp - 2 + RING) & (RING - 1)) * LAYER;
+                    R t1[6], t2[6];
+                    t1[0] = Lu1[c];       t2[0] = Lu2[c];          // r-1 (up)
+                    t1[1] = Ld1[c];       t2[1] = Ld2[c];          // r+1 (down)
+                    t1[2] = L0[c - LZ];   t2[2] = L0[c - 2 * LZ];
+                    t1[3] = L0[c + LZ];   t2[3] = L0[c + 2 * LZ];
+                    t1[4] = L0[c - 1];    t2[4] = L0[c - 2];
+                    t1[5] = L0[c + 1];    t2[5] = L0[c + 2];
+                    const unsigned inb = (gr > 0 ? 1u : 0u) | (gr < f.nnr - 1 ? 2u : 0u) | (gx > 0 ? 4u : 0u) |
+                                         (gx < f.nnx - 1 ? 8u : 0u) | (gz > 0 ? 16u : 0u) |
+                                         (gz < f.nnz - 1 ? 32u : 0u);
+                    const R v = fm_update<R>(pcur.s, t1, t2, inb, pcur.sp, f.order2);
+                    const R old = L0[c];
+                    if (fbits(v) != fbits(old)) {
+                        ring[((rp + RING) & (RING - 1)) * LAYER + c] = v;
+                        Te[((size_t)gr * f.nnx + gx) * f.nnz + gz] = v;
+                        if (a.flag) stream_mark(a, e, gr, gx, gz);
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+template <typename R, int SX, int SZ>
+struct StreamKernels {
+    static void sweep(int grid, const StreamArgs<R> &a, cudaStream_t st)
+    {
+        stream_sweep_kernel<R, SX, SZ><<<grid, 32, 0, st>>>(a);
+    }
+    static int occ()
+    {
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stream_sweep_kernel<R, SX, SZ>, 32, 0);
+        return nb;
+    }
+};
+
+#define FM_STREAM_SWITCH(idx, CALL)       \
+    switch (idx) {                        \
+        case 0: CALL(4, 8); break;        \
+        default: CALL(2, 16); break;      \
+    }
+
+}  // namespace fm3dt

@@ -135,6 +135,15 @@ def tile_shapes():
     return out
 
 
+STREAM_SWEEPS = (("stream", 4, 8), ("stream", 2, 16))
+
+
+def sweep_shapes():
+    """Shapes fm3dt_set_sweep_shape accepts: the tile shapes (tile sweep),
+    then the streaming sweep's column blocks."""
+    return [tuple(s) for s in tile_shapes()] + list(STREAM_SWEEPS)
+
+
 class Solver:
     """One solver context: a grid, a velocity model and up to max_events
     device-resident traveltime fields."""

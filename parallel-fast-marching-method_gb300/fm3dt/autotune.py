@@ -1,6 +1,7 @@
 """Autotuner of the tile solver.
 
-Tunes, on a sample batch, (1) the tile shape of the directional sweep and
+Tunes, on a sample batch, (1) the shape of the directional sweep (tile or
+streaming) and
 (2) the tile shape and in-tile pass cap of the fast-iterative rounds (the
 shape also fixes the CTA size: one thread per column), keeping the fastest
 device time.  The converged field does not depend on any of these choices
@@ -10,7 +11,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from . import tile_shapes
+from . import sweep_shapes, tile_shapes
 
 PASS_CAPS = (16, 64)
 
@@ -26,7 +27,7 @@ def autotune(solver, frames_ptr: int, nev: int, device: bool = True, repeats: in
     round_shape, cap = 0, PASS_CAPS[0]
     solver.set_tuning(round_shape, cap, 0, 1)
     best_sweep = None
-    for sshape in range(nshapes):
+    for sshape in range(len(sweep_shapes())):
         solver.set_sweep_shape(sshape)
         ms = _time(solver, frames_ptr, nev, device, repeats)
         if best_sweep is None or ms < best_sweep[1]:

@@ -195,6 +195,16 @@ def test_tile_shapes_and_sweep_bitwise(gpu_lib, prec):
                     ref = out
                 else:
                     assert np.array_equal(out, ref), f"shape {shape} sweep {sweep} cap {cap}"
+        # every sweep shape, the streaming column blocks with and without
+        # their verification sweep included
+        for sweep in (1, 2):
+            s.set_tuning(3, 16, 0, sweep)
+            for sshape in range(len(fm3dt.sweep_shapes())):
+                s.set_sweep_shape(sshape)
+                st = s.solve_planewave(params)
+                assert st["converged"] == 1 and st["sweep_launches"] > 0
+                out = np.concatenate([s.get_times(e) for e in range(3)])
+                assert np.array_equal(out, ref), f"sweep shape {fm3dt.sweep_shapes()[sshape]}, mode {sweep}"
 
 
 @pytest.mark.parametrize("prec", [0, 1])
