@@ -17,6 +17,9 @@
 
 namespace fm3dt {
 
+// Ring of layers: at step s the lanes read layers s - (SX+SZ) .. s+2 and the
+// warp stores layer s+3 (loaded into registers during step s-1), so the
+// ring must hold SX + SZ + 4 layers.
 template <int SX, int SZ>
 struct StreamRing {
     static constexpr int need = SX + SZ + 4;
@@ -76,30 +79,44 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
         const int gx = x0 + lx, gz = z0 + lz;
         const bool colv = gx < f.nnx && gz < f.nnz;
         R *Te = f.T + (size_t)e * N;
-        // layer rp (counted upward from the bottom) into its ring slot; unset
-        // outside the grid
-        auto load_layer = [&](int rp) {
-            R *dst = ring + ((rp + RING) & (RING - 1)) * LAYER;
+        // layer rp (counted upward from the bottom) into registers (this
+        // lane's share of the layer), unset outside the grid; then into its
+        // ring slot
+        constexpr int PER = (LAYER + 31) / 32;
+        R buf[PER];
+        auto fetch_layer = [&](int rp) {
             const int gr = f.nnr - 1 - rp;
-            for (int q = lane; q < LAYER; q += 32) {
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int q = lane + 32 * k;
                 const int qx = x0 + q / LZ - 2, qz = z0 + q % LZ - 2;
                 R v = INF;
-                if (rp >= 0 && rp < f.nnr && qx >= 0 && qx < f.nnx && qz >= 0 && qz < f.nnz)
+                if (q < LAYER && rp >= 0 && rp < f.nnr && qx >= 0 && qx < f.nnx && qz >= 0 && qz < f.nnz)
                     v = __ldcg(Te + ((size_t)gr * f.nnx + qx) * f.nnz + qz);
-                dst[q] = v;
+                buf[k] = v;
             }
         };
+        auto store_layer = [&](int rp) {
+            R *dst = ring + ((rp + RING) & (RING - 1)) * LAYER;
+#pragma unroll
+            for (int k = 0; k < PER; ++k)
+                if (lane + 32 * k < LAYER) dst[lane + 32 * k] = buf[k];
+        };
         __syncwarp();
-        load_layer(-2);
-        load_layer(-1);
-        load_layer(0);
-        load_layer(1);
+        for (int rp = -2; rp <= 2; ++rp) {
+            fetch_layer(rp);
+            store_layer(rp);
+        }
+        fetch_layer(3);
         const int c = (lx + 2) * LZ + (lz + 2);
         typename TL::Params pnext{};
         if (colv && xs + zs == 0) pnext = TL::params_global(f, f.nnr - 1, gx, gz);
         const int steps = f.nnr + SX + SZ - 2;
         for (int step = 0; step < steps; ++step) {
-            load_layer(step + 2);
+            // layer step+3 was fetched during the previous step; fetch the
+            // next one now, used a step later
+            store_layer(step + 3);
+            fetch_layer(step + 4);
             __syncwarp();
             const int rp = step - xs - zs;
             const typename TL::Params pcur = pnext;
