@@ -197,6 +197,13 @@ int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rou
  * changes the converged field. */
 int fm3dt_set_sweep_shape(fm3dt_ctx *ctx, int tile_shape);
 
+/* Height segments of the streaming sweep (its work items are column blocks
+ * of one segment; more segments give more parallel items per launch and a
+ * longer pipeline ramp), for the sweep of every event and for the second,
+ * reversed sweep of the events whose lateral direction is a near tie
+ * (within ~6 degrees of an axis).  0 = chosen from the batch size. */
+int fm3dt_set_sweep_segments(fm3dt_ctx *ctx, int segments, int tie_segments);
+
 /* Per-round trace of the last solve: tiles processed and node updates of
  * each round (up to cap rounds).  Returns the number of rounds, or a negative
  * error. */

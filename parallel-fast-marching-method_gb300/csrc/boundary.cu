@@ -76,7 +76,8 @@ __global__ void finalize_kernel(Geom g, const double *__restrict__ frames, R *__
 // One block per event: the dominant lateral propagation direction of the
 // boundary frame (sign of its summed theta and phi differences over pairs of
 // fixed nodes), which orders the solver's sweep.  bit 0: times grow with
-// theta (sweep +theta), bit 1: times grow with phi.
+// theta (sweep +theta), bit 1: times grow with phi; bits 2 and 3: theta /
+// phi is a near tie (sweep it both ways).
 __global__ void directions_kernel(Geom g, const double *__restrict__ frames, int *__restrict__ dir)
 {
     const int e = blockIdx.x;
@@ -100,7 +101,11 @@ __global__ void directions_kernel(Geom g, const double *__restrict__ frames, int
     if (threadIdx.x == 0) {
         double ax = 0.0, az = 0.0;
         for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) { ax += rx[w]; az += rz[w]; }
-        dir[e] = (ax >= 0.0 ? 1 : 0) | (az >= 0.0 ? 2 : 0);
+        // bits 2 / 3: the wave runs within ~6 degrees of the phi / theta
+        // axis, so its theta / phi direction is ambiguous under heterogeneity
+        // and a second sweep with that direction reversed is worth its cost
+        const double mx = fabs(ax), mz = fabs(az);
+        dir[e] = (ax >= 0.0 ? 1 : 0) | (az >= 0.0 ? 2 : 0) | (mx < 0.1 * mz ? 4 : 0) | (mz < 0.1 * mx ? 8 : 0);
     }
 }
 

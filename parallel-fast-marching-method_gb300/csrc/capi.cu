@@ -154,28 +154,48 @@ int ensure_planes(fm3dt_ctx *ctx, int shape)
     return FM3DT_OK;
 }
 
-// Column-block hyperplanes x' + z' = h of a streaming sweep shape (swept
-// block coordinates), packed x'<<16 | z'.
-int ensure_block_planes(fm3dt_ctx *ctx, int sweep_shape)
+// Hyperplanes s' + x' + z' = h of a streaming sweep's work items: height
+// segment s' (counted upward), column blocks x', z' in swept coordinates,
+// packed s'<<24 | x'<<12 | z'.
+int ensure_block_planes(fm3dt_ctx *ctx, int sweep_shape, int nseg, const fm3dt_ctx::Planes **out)
 {
-    auto &P = ctx->planes[sweep_shape];
-    if (P.shape == sweep_shape) return FM3DT_OK;
+    for (const auto &P : ctx->block_planes)
+        if (P.shape == sweep_shape && P.nseg == nseg) {
+            *out = &P;
+            return FM3DT_OK;
+        }
     const StreamShape ss = kStreamShapes[sweep_shape - kNumShapes];
     const int nbx = (ctx->g.nnx + ss.sx - 1) / ss.sx, nbz = (ctx->g.nnz + ss.sz - 1) / ss.sz;
-    if (nbx > 32767 || nbz > 65535) return fail(ctx, FM3DT_EINVAL, "too many column blocks along one axis");
-    const int H = nbx + nbz - 1;
+    if (nbx > 4095 || nbz > 4095 || nseg > 127) return fail(ctx, FM3DT_EINVAL, "too many column blocks or segments");
+    fm3dt_ctx::Planes P;
+    P.shape = sweep_shape;
+    P.nseg = nseg;
+    const int H = nseg + nbx + nbz - 2;
     std::vector<int> flat;
     P.off.assign(H, 0);
     P.cnt.assign(H, 0);
     for (int h = 0; h < H; ++h) {
         P.off[h] = (int)flat.size();
-        for (int b = std::max(0, h - nbz + 1); b <= std::min(h, nbx - 1); ++b) flat.push_back((b << 16) | (h - b));
+        for (int s = 0; s < nseg && s <= h; ++s)
+            for (int b = std::max(0, h - s - nbz + 1); b <= std::min(h - s, nbx - 1); ++b)
+                flat.push_back((s << 24) | (b << 12) | (h - s - b));
         P.cnt[h] = (int)flat.size() - P.off[h];
     }
     CK(cudaMalloc(&P.d_tiles, flat.size() * sizeof(int)));
     CK(cudaMemcpy(P.d_tiles, flat.data(), flat.size() * sizeof(int), cudaMemcpyHostToDevice));
-    P.shape = sweep_shape;
+    ctx->block_planes.push_back(std::move(P));
+    *out = &ctx->block_planes.back();
     return FM3DT_OK;
+}
+
+// Height segments for a streaming sweep over nitems events: enough work
+// items per launch to fill the GPU once, each segment at least 16 layers.
+int stream_segments(const fm3dt_ctx *ctx, int nitems, int nbx, int nbz, int sgrid)
+{
+    const double per_plane = (double)nbx * nbz / (double)(nbx + nbz - 1);
+    int nseg = 1;
+    while (nseg * 2 <= std::max(1, ctx->g.nnr / 16) && nitems * per_plane * nseg < (double)sgrid) nseg *= 2;
+    return nseg;
 }
 
 // How a solve starts: from boundary frames (initialisation, sweep, rounds),
@@ -240,28 +260,47 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     if (do_sweep && ctx->sweep_shape >= kNumShapes) {
         // streaming sweep: one launch per column-block hyperplane
         const int idx = ctx->sweep_shape - kNumShapes;
-        int rc = ensure_block_planes(ctx, ctx->sweep_shape);
-        if (rc) return rc;
-        const auto &P = ctx->planes[ctx->sweep_shape];
         const StreamShape ss = kStreamShapes[idx];
         const int nbx = (g.nnx + ss.sx - 1) / ss.sx, nbz = (g.nnz + ss.sz - 1) / ss.sz;
         const int occ = ctx->prec == FM3DT_FP64 ? occupancy_stream_f64(idx) : occupancy_stream_f32(idx);
         const int sgrid = std::max(1, occ) * sm_count();
-        // pass 0 sweeps from the boundary; pass 1 (verification) sweeps again
+        // the events whose lateral direction is a near tie get a second
+        // sweep with it reversed
+        CK(cudaMemcpyAsync(ctx->h_dir, ctx->d_dir, nev * sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        std::vector<int> ties;
+        for (int e = 0; e < nev; ++e)
+            if (ctx->h_dir[e] & 12) ties.push_back(e);
+        if (!ties.empty())
+            CK(cudaMemcpyAsync(ctx->d_events, ties.data(), ties.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        // pass 0 sweeps every event from the boundary, pass 1 the near-tie
+        // events reversed; pass 2 (verification, optional) sweeps once more
         // and queues the rounds' tiles where a node still changed
-        const int passes = ctx->verify ? 2 : 1;
         if (ctx->verify) {
             CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
             CK(cudaMemsetAsync(ctx->d_count[0], 0, sizeof(int), s));
         }
-        for (int pass = 0; pass < passes; ++pass)
+        for (int pass = 0; pass < 3; ++pass) {
+            if ((pass == 1 && ties.empty()) || (pass == 2 && !ctx->verify)) continue;
+            const int nitems = pass == 1 ? (int)ties.size() : nev;
+            int nseg = pass == 1 ? ctx->tie_segments : ctx->sweep_segments;
+            if (nseg <= 0) nseg = stream_segments(ctx, nitems, nbx, nbz, sgrid);
+            nseg = std::min(nseg, g.nnr);
+            const fm3dt_ctx::Planes *PP = nullptr;
+            int rc = ensure_block_planes(ctx, ctx->sweep_shape, nseg, &PP);
+            if (rc) return rc;
+            const auto &P = *PP;
+            const int seg_len = (g.nnr + nseg - 1) / nseg;
             for (size_t h = 0; h < P.off.size(); ++h) {
-                const long long items = (long long)P.cnt[h] * nev;
+                const long long items = (long long)P.cnt[h] * nitems;
                 const int grid = (int)std::min<long long>(items, sgrid);
                 auto fill = [&](auto &a) {
                     a.hp_blocks = P.d_tiles; a.hoff = P.off[h]; a.hcount = P.cnt[h];
-                    a.dir = ctx->d_dir; a.nev = nev; a.nbx = nbx; a.nbz = nbz;
-                    a.flag = pass ? ctx->d_flag : nullptr;
+                    a.dir = ctx->d_dir; a.nev = nitems; a.nbx = nbx; a.nbz = nbz;
+                    a.events = pass == 1 ? ctx->d_events : nullptr;
+                    a.flip = pass == 1;
+                    a.seg_len = seg_len;
+                    a.flag = pass == 2 ? ctx->d_flag : nullptr;
                     a.list = ctx->d_list[0]; a.count = ctx->d_count[0];
                     a.tr = ts.tr; a.tx = ts.tx; a.tz = ts.tz;
                     a.ntr = ntr; a.ntx = ntx; a.ntz = ntz; a.tiles_per_event = tpe;
@@ -279,6 +318,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                 }
                 ++sweep_launches;
             }
+        }
         ctx->launches += sweep_launches;
         CKL();
         verified = ctx->verify != 0;
@@ -528,6 +568,8 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMalloc(&ctx->d_box, 6 * ctx->maxev * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_box_init, 6 * ctx->maxev * sizeof(int)));
     CKC(cudaMallocHost(&ctx->h_count, sizeof(int)));
+    CKC(cudaMallocHost(&ctx->h_dir, ctx->maxev * sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_events, ctx->maxev * sizeof(int)));
     CKC(cudaMallocHost(&ctx->h_stats, 3 * sizeof(unsigned long long)));
     CKC(cudaMemset(ctx->d_base, 0, ctx->maxev * sizeof(double)));
     int rc = ctx->prec == FM3DT_FP64 ? upload_geometry<double>(ctx) : upload_geometry<float>(ctx);
@@ -941,6 +983,16 @@ int fm3dt_set_sweep_shape(fm3dt_ctx *ctx, int tile_shape)
     return FM3DT_OK;
 }
 
+int fm3dt_set_sweep_segments(fm3dt_ctx *ctx, int segments, int tie_segments)
+{
+    if (!ctx) return FM3DT_EINVAL;
+    if (segments < 0 || tie_segments < 0 || segments > 127 || tie_segments > 127)
+        return fail(ctx, FM3DT_EINVAL, "segments outside 0..127");
+    ctx->sweep_segments = segments;
+    ctx->tie_segments = tie_segments;
+    return FM3DT_OK;
+}
+
 int fm3dt_round_trace(fm3dt_ctx *ctx, int cap, int64_t *tiles, int64_t *updates)
 {
     if (!ctx || cap < 0) return FM3DT_EINVAL;
@@ -991,6 +1043,9 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_wz);
     cudaFree(ctx->d_dir);
     for (auto &P : ctx->planes) cudaFree(P.d_tiles);
+    for (auto &P : ctx->block_planes) cudaFree(P.d_tiles);
+    cudaFree(ctx->d_events);
+    if (ctx->h_dir) cudaFreeHost(ctx->h_dir);
     cudaFree(ctx->d_T);
     cudaFree(ctx->d_frames);
     cudaFree(ctx->d_base);

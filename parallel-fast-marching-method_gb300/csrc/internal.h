@@ -85,11 +85,14 @@ constexpr int kNumSweepShapes = kNumShapes + kNumStream;
 template <typename R>
 struct StreamArgs {
     FieldArgs<R> f;
-    const int *hp_blocks;       // swept column-block coordinates (x' << 16 | z'), by hyperplane
+    const int *hp_blocks;       // swept (segment, x block, z block): s << 24 | x' << 12 | z', by hyperplane
     int hoff, hcount;
-    const int *dir;             // [E] bit 0: sweep +theta, bit 1: sweep +phi
+    const int *dir;             // [E] bit 0: sweep +theta, bit 1: sweep +phi, bits 2/3: near ties
+    const int *events;          // the events swept (indices), or null for events 0..nev-1
     int nev;
+    int flip;                   // reverse each near-tie lateral direction
     int nbx, nbz;               // column blocks per axis
+    int seg_len;                // layers per height segment
     // verification sweep: when flag is set, every node whose value changes
     // queues its round tile (recompute all) and, near a tile face, the face
     // neighbour (that face changed) -- the first round's work list
@@ -216,7 +219,12 @@ struct fm3dt_ctx {
     static constexpr int kTraceRounds = 8192;
     int last_rounds = 0;
     // tile hyperplanes of each shape (device list + host offsets)
-    struct Planes { int shape = -1; int *d_tiles = nullptr; std::vector<int> off, cnt; };
+    struct Planes { int shape = -1; int nseg = 1; int *d_tiles = nullptr; std::vector<int> off, cnt; };
+    std::vector<Planes> block_planes;   // streaming sweeps, by (shape, height segments)
+    int sweep_segments = 0;       // height segments of the streaming sweep (0: automatic)
+    int tie_segments = 0;         // the same for the reversed sweep of near-tie events
+    int *h_dir = nullptr;         // pinned [maxev] sweep directions of the last solve
+    int *d_events = nullptr;      // [maxev] the near-tie events of the last solve
     Planes planes[fm3dt::kNumSweepShapes];   // tile hyperplanes, then column-block hyperplanes
     size_t flag_capacity = 0;     // tiles allocated for flags/lists
     int64_t launches = 0;

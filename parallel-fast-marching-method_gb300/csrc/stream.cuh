@@ -2,16 +2,19 @@
 // of solver.cuh).
 //
 // One warp owns a block of SX x SZ (theta, phi) columns and streams through
-// the whole height of the grid from the bottom face upward.  Lane (x', z')
+// one height segment of the grid (the whole height, or a few tens of layers
+// when more parallel work is needed) from the bottom upward.  Lane (x', z')
 // updates layer r' at step r' + x' + z' (swept coordinates, as in the tile
 // sweep), so each node sees its upwind neighbours' new values; the ramp of
-// that wavefront (SX + SZ - 2 steps) is paid once per column block instead
-// of once per tile.  The layers the lanes are working on, plus the two
-// layers above and below and a two-column halo, sit in a shared-memory ring
-// of RING layers.  Column blocks go in hyperplanes of the event's sweep
-// direction (one launch per hyperplane); a block's upwind neighbours are in
-// earlier launches.  The sweep is only a good start for the rounds, which
-// reach the same fixed point from any start.
+// that wavefront (SX + SZ - 2 steps) is paid once per segment instead of
+// once per tile.  The layers the lanes are working on, plus the two layers
+// above and below and a two-column halo, sit in a shared-memory ring of RING
+// layers.  Work items (segment, column block) go in hyperplanes of the
+// event's sweep direction (one launch per hyperplane); an item's upwind
+// neighbours are in earlier launches.  Events whose lateral direction is a
+// near tie are swept a second time with that direction reversed.  The sweep
+// is only a good start for the rounds, which reach the same fixed point from
+// any start.
 #pragma once
 #include "solver.cuh"
 
@@ -66,12 +69,16 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
     const size_t N = (size_t)f.nnx * f.nnz * (size_t)f.nnr;
     const long long count = (long long)a.hcount * a.nev;
     for (long long item = blockIdx.x; item < count; item += gridDim.x) {
-        const int e = (int)(item / a.hcount);
-        const int j = (int)(item - (long long)e * a.hcount);
+        const int k = (int)(item / a.hcount);
+        const int j = (int)(item - (long long)k * a.hcount);
+        const int e = a.events ? a.events[k] : k;
         const int packed = a.hp_blocks[a.hoff + j];
-        const int bxp = packed >> 16, bzp = packed & 0xffff;
-        const int dir = a.dir[e];
+        const int seg = packed >> 24, bxp = (packed >> 12) & 0xfff, bzp = packed & 0xfff;
+        int dir = a.dir[e];
+        if (a.flip) dir ^= ((dir >> 2) & 1) | (((dir >> 3) & 1) << 1);
         const bool sx = dir & 1, sz = (dir >> 1) & 1;
+        // this item's layers, counted upward from the bottom: [lo, hi)
+        const int lo = seg * a.seg_len, hi = min(f.nnr, lo + a.seg_len);
         const int x0 = (sx ? bxp : a.nbx - 1 - bxp) * SX;
         const int z0 = (sz ? bzp : a.nbz - 1 - bzp) * SZ;
         const int xs = sx ? lx : SX - 1 - lx;
@@ -103,26 +110,26 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
                 if (lane + 32 * k < LAYER) dst[lane + 32 * k] = buf[k];
         };
         __syncwarp();
-        for (int rp = -2; rp <= 2; ++rp) {
+        for (int rp = lo - 2; rp <= lo + 2; ++rp) {
             fetch_layer(rp);
             store_layer(rp);
         }
-        fetch_layer(3);
+        fetch_layer(lo + 3);
         const int c = (lx + 2) * LZ + (lz + 2);
         typename TL::Params pnext{};
-        if (colv && xs + zs == 0) pnext = TL::params_global(f, f.nnr - 1, gx, gz);
-        const int steps = f.nnr + SX + SZ - 2;
+        if (colv && xs + zs == 0) pnext = TL::params_global(f, f.nnr - 1 - lo, gx, gz);
+        const int steps = (hi - lo) + SX + SZ - 2;
         for (int step = 0; step < steps; ++step) {
-            // layer step+3 was fetched during the previous step; fetch the
-            // next one now, used a step later
-            store_layer(step + 3);
-            fetch_layer(step + 4);
+            // layer lo+step+3 was fetched during the previous step; fetch
+            // the next one now, used a step later
+            store_layer(lo + step + 3);
+            fetch_layer(lo + step + 4);
             __syncwarp();
-            const int rp = step - xs - zs;
+            const int rp = lo + step - xs - zs;
             const typename TL::Params pcur = pnext;
             // the next node's slowness and spacings, one step ahead
-            if (colv && rp + 1 >= 0 && rp + 1 < f.nnr) pnext = TL::params_global(f, f.nnr - 2 - rp, gx, gz);
-            if (colv && rp >= 0 && rp < f.nnr) {
+            if (colv && rp + 1 >= lo && rp + 1 < hi) pnext = TL::params_global(f, f.nnr - 2 - rp, gx, gz);
+            if (colv && rp >= lo && rp < hi) {
                 const int gr = f.nnr - 1 - rp;
                 if (!TL::frozen(f, e, gr, gx, gz)) {
                     const R *L0 = ring + ((rp + RING) & (RING - 1)) * LAYER;

@@ -57,7 +57,7 @@ EXPORTS = [
     "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_resume",
     "fm3dt_solve_planewave", "fm3dt_solve_point",
     "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
-    "fm3dt_set_tuning", "fm3dt_set_sweep_shape", "fm3dt_round_trace", "fm3dt_tile_shapes", "fm3dt_tile_shape",
+    "fm3dt_set_tuning", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_tile_shapes", "fm3dt_tile_shape",
     "fm3dt_launch_count",
     "fm3dt_last_error", "fm3dt_ctx_destroy",
 ]
@@ -91,6 +91,7 @@ def load(path: str | None = None):
     L.fm3dt_get_velocity.argtypes = [vp, dp]
     L.fm3dt_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
     L.fm3dt_set_sweep_shape.argtypes = [vp, C.c_int]
+    L.fm3dt_set_sweep_segments.argtypes = [vp, C.c_int, C.c_int]
     L.fm3dt_round_trace.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.fm3dt_tile_shapes.argtypes = [C.POINTER(C.c_int)]
     L.fm3dt_tile_shape.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -209,6 +210,9 @@ class Solver:
 
     def set_sweep_shape(self, shape: int):
         self._check(self._L.fm3dt_set_sweep_shape(self._ctx, int(shape)))
+
+    def set_sweep_segments(self, segments: int = 0, tie_segments: int = 0):
+        self._check(self._L.fm3dt_set_sweep_segments(self._ctx, int(segments), int(tie_segments)))
 
     def round_trace(self, cap: int = 8192):
         """(tiles, node updates) per round of the last solve."""
