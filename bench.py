@@ -156,10 +156,12 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-# Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of
-# each solver kernel from one ncu capture, scaled to the bench workload; see
-# the summaries under profiles/.  Absent until a capture exists.
-KERNEL_TRAFFIC_BYTES = {}
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per node of
+# each single-precision solver kernel, from one ncu capture of a smaller case
+# of the same kernels (96^3, 64 events): the first round's launch (every tile
+# staged) and one mid-sweep launch; the bench scales it to its own launches
+# by the nodes they process.
+KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.25, "stream_sweep_kernel": 28.6}
 
 
 def _oracle_event(args):
@@ -310,16 +312,21 @@ def run_ours(a):
     sweep_ms = sum(s["sweep_ms"] for s in sts)
     sweep_launches = sum(s["sweep_launches"] for s in sts)
     sweep_nodes = sum(s["sweep_nodes"] for s in sts)
+    sweep_name = "stream_sweep_kernel" if sweep_shape_dims[0] == "stream" else "sweep_kernel"
     kernels = {
-        "round_kernel": (round_ms, round_launches, staged * B_NODE[a.prec]),
-        "sweep_kernel": (sweep_ms, sweep_launches, sweep_nodes * B_NODE[a.prec]),
+        "round_kernel": (round_ms, round_launches, staged * B_NODE[a.prec], staged),
+        sweep_name: (sweep_ms, sweep_launches, sweep_nodes * B_NODE[a.prec], sweep_nodes),
     }
     top = max(kernels, key=lambda k: kernels[k][0])
-    k_ms, k_launches, alg_bytes = kernels[top]
+    k_ms, k_launches, alg_bytes, k_nodes = kernels[top]
     achieved = alg_bytes / (k_ms / 1000.0) / 1e9 if k_ms > 0 else 0.0
     peak, peak_kind = measured_peak_hbm()
     per_launch = alg_bytes / max(1, k_launches)
-    traffic = KERNEL_TRAFFIC_BYTES.get(top)
+    # DRAM bytes per node processed, from the ncu capture of the small case
+    # (profiles/solver_kernels_small_case.md), times the nodes one launch
+    # processes here on average
+    traffic = (KERNEL_DRAM_BYTES_PER_NODE[top] * k_nodes / max(1, k_launches)
+               if top in KERNEL_DRAM_BYTES_PER_NODE and a.prec == "f32" else None)
 
     extras = {}
     if not a.no_extras:

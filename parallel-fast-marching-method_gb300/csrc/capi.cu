@@ -255,6 +255,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
 
     // 1. directional sweep, one launch per tile hyperplane
     int sweep_launches = 0;
+    int64_t sweep_nodes = 0;      // nodes visited by all sweep passes
     bool verified = false;
     CK(cudaEventRecord(sw0, s));
     if (do_sweep && ctx->sweep_shape >= kNumShapes) {
@@ -283,6 +284,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         for (int pass = 0; pass < 3; ++pass) {
             if ((pass == 1 && ties.empty()) || (pass == 2 && !ctx->verify)) continue;
             const int nitems = pass == 1 ? (int)ties.size() : nev;
+            sweep_nodes += (int64_t)nitems * (int64_t)ctx->N;
             int nseg = pass == 1 ? ctx->tie_segments : ctx->sweep_segments;
             if (nseg <= 0) nseg = stream_segments(ctx, nitems, nbx, nbz, sgrid);
             nseg = std::min(nseg, g.nnr);
@@ -323,6 +325,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         CKL();
         verified = ctx->verify != 0;
     } else if (do_sweep) {
+        sweep_nodes = (int64_t)nev * (int64_t)ctx->N;
         const int sshape = ctx->sweep_shape;
         int rc = ensure_planes(ctx, sshape);
         if (rc) return rc;
@@ -456,7 +459,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         st->round_launches = rounds;
         st->sweep_ms = do_sweep ? sms : 0.0;
         st->sweep_launches = sweep_launches;
-        st->sweep_nodes = do_sweep ? (int64_t)nev * (int64_t)ctx->N * (verified ? 2 : 1) : 0;
+        st->sweep_nodes = sweep_nodes;
     }
     if (!done) return fail(ctx, FM3DT_ENOCONV, "solver round limit reached before convergence");
     return FM3DT_OK;
