@@ -109,7 +109,7 @@ def build_driver(force: bool = False) -> str:
 SUBINV_DIR = os.path.join(ROOT, "subinv")
 SUBINV_LIB = os.path.join(ROOT, "libfm3dt_subinv.so")
 SUBINV = os.path.join(ROOT, "fm3dt_subinv")
-HOST_FLAGS = ["-O2", "-std=c++17", "-Wall", "-ffp-contract=off"]
+HOST_FLAGS = ["-O2", "-std=c++17", "-Wall", "-ffp-contract=off", "-pthread"]
 
 
 def build_subinv(force: bool = False) -> str:

@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -148,16 +149,35 @@ System<R> assemble(const fm3dt_subinv_desc &d, int nra, const int *nsrc, const i
     return S;
 }
 
+// fn(i) for i in [0, n) on the host's cores.  Each i is computed whole by
+// one thread, so results do not depend on the number of threads.
+template <typename F>
+void parallel_for(int n, F fn)
+{
+    const int nt = std::max(1, std::min((int)std::thread::hardware_concurrency(), std::min(32, n / 256)));
+    if (nt <= 1) {
+        for (int i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back([&, t] {
+            const int a = (int)((int64_t)n * t / nt), b = (int)((int64_t)n * (t + 1) / nt);
+            for (int i = a; i < b; ++i) fn(i);
+        });
+    for (auto &x : th) x.join();
+}
+
 // y = G x / cd over the picked rows (the ga of S:764-773)
 template <typename R>
 void g_times(const System<R> &S, const R *x, std::vector<R> &ga)
 {
     ga.resize(S.ntr);
-    for (int j = 0; j < S.ntr; ++j) {
+    parallel_for(S.ntr, [&](int j) {
         R rsum = 0;
         for (int64_t k = S.cnfe[j]; k < S.cnfe[j + 1]; ++k) rsum = rsum + S.frech[k] * x[S.fcoln[k] - 1];
         ga[j] = rsum / S.cd[j];
-    }
+    });
 }
 
 // (G^T y)_i over the transpose
@@ -167,6 +187,14 @@ R gt_row(const System<R> &S, int i, const std::vector<R> &y)
     R rsum = 0;
     for (int64_t k = S.tcnfe[i]; k < S.tcnfe[i + 1]; ++k) rsum = rsum + S.tfrech[k] * y[S.tfcoln[k] - 1];
     return rsum;
+}
+
+// (G^T y)_i for every model parameter i, in parallel
+template <typename R>
+void gt_times(const System<R> &S, const std::vector<R> &y, std::vector<R> &out)
+{
+    out.resize(S.nmp);
+    parallel_for(S.nmp, [&](int i) { out[i] = gt_row(S, i, y); });
 }
 
 }  // namespace
@@ -362,10 +390,11 @@ void subspace(const fm3dt_subinv_desc &d, const System<R> &S, const std::vector<
     std::vector<R> dtrav(ntr);
     for (int i = 0; i < ntr; ++i) dtrav[i] = (S.dmod[i] - S.dobs[i]) / S.cd[i];
     // gradient
-    std::vector<R> gamma(nmp);
+    std::vector<R> gamma(nmp), gtv;
+    gt_times(S, dtrav, gtv);
     R epst = eps;
     for (int i = 0; i < nmp; ++i) {
-        const R rsum = gt_row(S, i, dtrav);
+        const R rsum = gtv[i];
         if (i >= nmpv) epst = stdf;
         gamma[i] = rsum + (epst * (mc[i] - mo[i])) / cm[i];
     }
@@ -407,12 +436,13 @@ void subspace(const fm3dt_subinv_desc &d, const System<R> &S, const std::vector<
             for (int i = 1; i <= nits && !done; ++i) {
                 const int src = is2 - nits + i - 1;      // 0-based source column
                 g_times(S, &A(0, src), ga);
+                gt_times(S, ga, gtv);
                 for (int jj = 0; jj < npc; ++jj) {
                     is1 += 1;
                     if (is1 > subdim) break;
                     const int dst = is1 - 1;
                     for (int j = inds[jj]; j < inde[jj]; ++j) {
-                        const R rsum = gt_row(S, j, ga);
+                        const R rsum = gtv[j];
                         A(j, dst) = rsum * cm[j] + (j < nmpv ? eps : stdf) * A(j, src);
                     }
                     normalise(dst, jj);
@@ -437,10 +467,11 @@ void subspace(const fm3dt_subinv_desc &d, const System<R> &S, const std::vector<
     auto M = [&](int r, int c) -> R & { return mati[(size_t)c * subdim + r]; };
     for (int ii = 0; ii < subdim; ++ii) {
         g_times(S, &A(0, ii), ga);
+        gt_times(S, ga, gtv);
         if (d.asds != 1) {
             R ep = eps;
             for (int j = 0; j < nmp; ++j) {
-                R rsum = gt_row(S, j, ga);
+                R rsum = gtv[j];
                 if (j >= nmpv) ep = stdf;
                 rsum = rsum + (ep * A(j, ii)) / cm[j];
                 for (int k = 0; k < subdim; ++k) M(k, ii) = M(k, ii) + rsum * A(j, k);
@@ -451,14 +482,14 @@ void subspace(const fm3dt_subinv_desc &d, const System<R> &S, const std::vector<
                 for (int j = 0; j < sm.nvt; ++j)
                     for (int k = 0; k < sm.nvr; ++k) {
                         const int q = (int)sm.at(i, j, k);
-                        R rsum = gt_row(S, q, ga);
+                        R rsum = gtv[q];
                         const R dd = sm.ddem_at(dem, i, j, k);
                         rsum = rsum + (eps * A(q, ii)) / cm[q] + eta * dd;
                         for (int l = 0; l < subdim; ++l) M(l, ii) = M(l, ii) + rsum * A(q, l);
                     }
             if (d.invst == 1)
                 for (int j = nmpv; j < nmp; ++j) {
-                    R rsum = gt_row(S, j, ga);
+                    R rsum = gtv[j];
                     rsum = rsum + (stdf * A(j, ii)) / cm[j];
                     for (int k = 0; k < subdim; ++k) M(k, ii) = M(k, ii) + rsum * A(j, k);
                 }
