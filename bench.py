@@ -295,6 +295,7 @@ def run_ours(a):
     launches = solver.launch_count - l0
     tt, tu = solver.round_trace()
     trace_tiles, trace_updates = [int(x) for x in tt], [int(x) for x in tu]
+    trace_ms = [round(float(x), 4) for x in solver.round_trace_ms()]
     clk = clocks.stop() if clocks else None
     dev_ms = sum(s["ms"] for s in sts)
     step_s = max(wall, dev_ms / 1000.0)
@@ -395,7 +396,8 @@ def run_ours(a):
                    "round_ms_per_step": round_ms / a.steps, "sweep_ms_per_step": sweep_ms / a.steps,
                    "sweep_launches_per_step": sweep_launches / a.steps,
                    "kernel_shares": {k: v[0] / max(1e-9, dev_ms) for k, v in kernels.items()},
-                   "round_trace_tiles": trace_tiles, "round_trace_updates": trace_updates},
+                   "round_trace_tiles": trace_tiles, "round_trace_updates": trace_updates,
+                   "round_trace_ms": trace_ms},
     }
     line.update(extras)
     if clk:

@@ -209,6 +209,10 @@ int fm3dt_set_sweep_segments(fm3dt_ctx *ctx, int segments, int tie_segments);
  * error. */
 int fm3dt_round_trace(fm3dt_ctx *ctx, int cap, int64_t *tiles, int64_t *updates);
 
+/* Device time (ms, CUDA events around each launch) of each round of the last
+ * solve, up to cap rounds.  Returns the number of rounds recorded. */
+int fm3dt_round_trace_ms(fm3dt_ctx *ctx, int cap, float *ms);
+
 /* Number of available tile shapes and the shape (TR, TX, TZ) of one. */
 int fm3dt_tile_shapes(int *count);
 int fm3dt_tile_shape(int index, int *tr, int *tx, int *tz);

@@ -394,6 +394,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     int rounds = 0;
     bool done = false;
     double round_ms = 0.0;
+    ctx->round_ms_trace.clear();
     while (!done && rounds < max_rounds) {
         int k;
         const int first_round = rounds;
@@ -430,6 +431,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             float m = 0.0f;
             cudaEventElapsedTime(&m, ctx->round_events[2 * q], ctx->round_events[2 * q + 1]);
             round_ms += m;
+            if ((int)ctx->round_ms_trace.size() < fm3dt_ctx::kTraceRounds) ctx->round_ms_trace.push_back(m);
         }
         if (*ctx->h_count == 0) done = true;
     }
@@ -1009,6 +1011,14 @@ int fm3dt_round_trace(fm3dt_ctx *ctx, int cap, int64_t *tiles, int64_t *updates)
         }
     }
     return ctx->last_rounds;
+}
+
+int fm3dt_round_trace_ms(fm3dt_ctx *ctx, int cap, float *ms)
+{
+    if (!ctx || cap < 0) return FM3DT_EINVAL;
+    const int n = std::min(cap, (int)ctx->round_ms_trace.size());
+    for (int i = 0; i < n && ms; ++i) ms[i] = ctx->round_ms_trace[i];
+    return (int)ctx->round_ms_trace.size();
 }
 
 int fm3dt_tile_shapes(int *count)

@@ -233,6 +233,7 @@ struct fm3dt_ctx {
     struct Graph { int shape, nev, rounds; cudaGraphExec_t exec; };
     std::vector<Graph> graphs;
     std::vector<cudaEvent_t> round_events;   // start/stop pairs of round kernels
+    std::vector<float> round_ms_trace;       // device time of each round of the last solve
     // point sources: fixed node boxes, and the refined source grids' contexts
     int *d_box = nullptr;         // [maxev][6] fixed nodes
     int *d_box_init = nullptr;    // [maxev][6] nodes whose tiles start active
