@@ -73,6 +73,11 @@ __global__ void finalize_kernel(Geom g, const double *__restrict__ frames, R *__
     }
 }
 
+// Lateral components within this ratio of each other count as a near tie.
+#ifndef FM_TIE_RATIO
+#define FM_TIE_RATIO 0.1
+#endif
+
 // One block per event: the dominant lateral propagation direction of the
 // boundary frame (sign of its summed theta and phi differences over pairs of
 // fixed nodes), which orders the solver's sweep.  bit 0: times grow with
@@ -105,7 +110,7 @@ __global__ void directions_kernel(Geom g, const double *__restrict__ frames, int
         // axis, so its theta / phi direction is ambiguous under heterogeneity
         // and a second sweep with that direction reversed is worth its cost
         const double mx = fabs(ax), mz = fabs(az);
-        dir[e] = (ax >= 0.0 ? 1 : 0) | (az >= 0.0 ? 2 : 0) | (mx < 0.1 * mz ? 4 : 0) | (mz < 0.1 * mx ? 8 : 0);
+        dir[e] = (ax >= 0.0 ? 1 : 0) | (az >= 0.0 ? 2 : 0) | (mx < FM_TIE_RATIO * mz ? 4 : 0) | (mz < FM_TIE_RATIO * mx ? 8 : 0);
     }
 }
 

@@ -201,6 +201,10 @@ int stream_segments(const fm3dt_ctx *ctx, int nitems, int nbx, int nbz, int sgri
 // How a solve starts: from boundary frames (initialisation, sweep, rounds),
 // from the current fields (resume: rounds with every tile active), or from
 // point-source boxes the caller already wrote (rounds from the boxes' tiles).
+#ifndef FM_TIE_SWEEPS
+#define FM_TIE_SWEEPS 2
+#endif
+
 enum SolveMode { kFrames = 0, kResume = 1, kPoint = 2 };
 
 int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
@@ -281,7 +285,12 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
             CK(cudaMemsetAsync(ctx->d_count[0], 0, sizeof(int), s));
         }
-        for (int pass = 0; pass < 3; ++pass) {
+        // (FM_TIE_SWEEPS sweeps of the near-tie events, alternating reversed
+        // and forward, stand for pass 1)
+        const int tie_sweeps = FM_TIE_SWEEPS;
+        for (int pp = 0; pp < 2 + tie_sweeps; ++pp) {
+            const int pass = pp == 0 ? 0 : (pp <= tie_sweeps ? 1 : 2);
+            const bool tie_forward = pass == 1 && ((pp - 1) & 1);
             if ((pass == 1 && ties.empty()) || (pass == 2 && !ctx->verify)) continue;
             const int nitems = pass == 1 ? (int)ties.size() : nev;
             sweep_nodes += (int64_t)nitems * (int64_t)ctx->N;
@@ -300,7 +309,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                     a.hp_blocks = P.d_tiles; a.hoff = P.off[h]; a.hcount = P.cnt[h];
                     a.dir = ctx->d_dir; a.nev = nitems; a.nbx = nbx; a.nbz = nbz;
                     a.events = pass == 1 ? ctx->d_events : nullptr;
-                    a.flip = pass == 1;
+                    a.flip = pass == 1 && !tie_forward;
                     a.seg_len = seg_len;
                     a.flag = pass == 2 ? ctx->d_flag : nullptr;
                     a.list = ctx->d_list[0]; a.count = ctx->d_count[0];

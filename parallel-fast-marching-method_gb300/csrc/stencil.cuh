@@ -151,11 +151,20 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
         R k0 = key[dr], e0 = e[dr], g0 = g[dr], w0 = w[dr];
         R k1 = key[dx], e1 = e[dx], g1 = g[dx], w1 = w[dx];
         R k2 = key[dz], e2 = e[dz], g2 = g[dz], w2 = w[dz];
-#define FM_SWAP(a, b) { R q_ = a; a = b; b = q_; }
-        if (k1 < k0) { FM_SWAP(k0, k1) FM_SWAP(e0, e1) FM_SWAP(g0, g1) FM_SWAP(w0, w1) }
-        if (k2 < k1) { FM_SWAP(k1, k2) FM_SWAP(e1, e2) FM_SWAP(g1, g2) FM_SWAP(w1, w2) }
-        if (k1 < k0) { FM_SWAP(k0, k1) FM_SWAP(e0, e1) FM_SWAP(g0, g1) FM_SWAP(w0, w1) }
-#undef FM_SWAP
+        // conditional swaps as selects (a branch around four moves costs more)
+#define FM_CSWAP(i, j)                                                        \
+    {                                                                         \
+        const bool p_ = k##j < k##i;                                          \
+        R q_;                                                                 \
+        q_ = p_ ? k##j : k##i; k##j = p_ ? k##i : k##j; k##i = q_;            \
+        q_ = p_ ? e##j : e##i; e##j = p_ ? e##i : e##j; e##i = q_;            \
+        q_ = p_ ? g##j : g##i; g##j = p_ ? g##i : g##j; g##i = q_;            \
+        q_ = p_ ? w##j : w##i; w##j = p_ ? w##i : w##j; w##i = q_;            \
+    }
+        FM_CSWAP(0, 1)
+        FM_CSWAP(1, 2)
+        FM_CSWAP(0, 1)
+#undef FM_CSWAP
         if (!(k0 < INF)) continue;
         R x = fm_fma<R>(s, g0, e0);
         if (k1 < x) {
