@@ -32,7 +32,7 @@ namespace {
 struct Args {
     std::string dir, in = "fm3dt_parallel.in";
     int precision = FM3DT_FP64;
-    int batch = 64;
+    int batch = 512;
     bool check = false;
 };
 

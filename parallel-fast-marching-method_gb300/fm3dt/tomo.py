@@ -75,7 +75,7 @@ class Tomography:
     ``params``: subinv.in values."""
 
     def __init__(self, header, velv_ref, cm_sd, survey: Survey, params: SI.Params, precision=None,
-                 subinv_precision=SI.FP32, batch: int = 64, fom: int = 1):
+                 subinv_precision=SI.FP32, batch: int = 512, fom: int = 1):
         import fm3dt
         import torch
         self.header = header
