@@ -13,6 +13,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 namespace {
@@ -27,17 +28,69 @@ struct Fail {
     std::string msg;
 };
 
+// fn(i) for i in [0, n) on the host's cores.  Each i is computed whole by
+// one thread, so results do not depend on the number of threads.
+template <typename F>
+void parallel_for(int n, F fn)
+{
+    const int nt = std::max(1, std::min((int)std::thread::hardware_concurrency(), std::min(32, n / 256)));
+    if (nt <= 1) {
+        for (int i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back([&, t] {
+            const int a = (int)((int64_t)n * t / nt), b = (int)((int64_t)n * (t + 1) / nt);
+            for (int i = a; i < b; ++i) fn(i);
+        });
+    for (auto &x : th) x.join();
+}
+
+// fn(t, a, b) on T contiguous chunks [a, b) of [0, n), one thread each.
+template <typename F>
+void parallel_chunks(int64_t n, int T, F fn)
+{
+    if (T <= 1) {
+        fn(0, (int64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < T; ++t)
+        th.emplace_back([&, t] { fn(t, n * t / T, n * (t + 1) / T); });
+    for (auto &x : th) x.join();
+}
+
+int host_threads(int64_t work, int64_t per_thread)
+{
+    const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
+    return (int)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(hw, 32), work / per_thread));
+}
+
+// Allocator whose resize leaves new elements uninitialised: the entry
+// arrays (tens of millions of entries) are written once, in parallel, so
+// zero-filling them first would only add a serial pass over the memory.
+template <typename T>
+struct NoInit : std::allocator<T> {
+    template <typename U> struct rebind { using other = NoInit<U>; };
+    NoInit() = default;
+    template <typename U> NoInit(const NoInit<U> &) {}
+    template <typename U> void construct(U *p) { ::new ((void *)p) U; }
+    template <typename U, typename... A> void construct(U *p, A &&...a) { ::new ((void *)p) U(std::forward<A>(a)...); }
+};
+template <typename T> using Big = std::vector<T, NoInit<T>>;
+
 // Picked rows of G and their data plus the transpose.
 template <typename R>
 struct System {
     int ntr = 0, nmpv = 0, nmp = 0;
     std::vector<int64_t> cnfe{0};          // row starts, ntr+1
-    std::vector<int32_t> fcoln;            // 1-based model columns
-    std::vector<R> frech;
+    Big<int32_t> fcoln;                    // 1-based model columns
+    Big<R> frech;
     std::vector<R> dobs, dmod, cd;         // cd = variance
     std::vector<int64_t> tcnfe;            // column starts, nmp+1
-    std::vector<int32_t> tfcoln;           // 1-based rows
-    std::vector<R> tfrech;
+    Big<int32_t> tfcoln;                   // 1-based rows
+    Big<R> tfrech;
 };
 
 template <typename R>
@@ -69,33 +122,25 @@ System<R> assemble(const fm3dt_subinv_desc &d, int nra, const int *nsrc, const i
         srcm.assign(nsum, R(0));
         ntsrc.assign(nsum, 0);
     }
+    // pass 1, in row order: the reference's size check (its running entry
+    // count), each picked row's place, the data columns
+    std::vector<int> pick;                 // picked rows, in order
+    pick.reserve(ntr_all);
+    S.cnfe.reserve((size_t)ntr_all + 1);
     int64_t jstep = 0;
     for (int i = 0; i < ntr_all; ++i) {
         R dm_i = (R)mtimes[i];
         const R dref = (R)rtimes[i];
         int64_t nrow = row_ptr[i + 1] - row_ptr[i];
-        int stnm = 0;
         if (d.invst == 1) {
-            stnm = idrt[i];
-            dm_i = dm_i + mc[nmpv + stnm - 1];
+            dm_i = dm_i + mc[nmpv + idrt[i] - 1];
             nrow += 1;
         }
         if (nrow > 0) {
-            const int64_t first = jstep;        // 0-based index of the row's first entry
-            if (first + nrow > maxf)
+            if (jstep + nrow > maxf)
                 throw Fail{FM3DT_SUBINV_ETOOBIG, "Frechet matrix too large for last input\nparameter in file "
                                                  "subinv.in\nSTOPPING PROGRAM!!!"};
-            if (tstat[i] == 1) {
-                for (int64_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
-                    S.fcoln.push_back(cols[k]);
-                    S.frech.push_back((R)vals[k]);
-                }
-                if (d.invst == 1) {
-                    S.fcoln.push_back(nmpv + stnm);
-                    S.frech.push_back(R(1));
-                }
-                jstep += nrow;
-            }
+            if (tstat[i] == 1) jstep += nrow;
         }
         if (tstat[i] == 1) {
             const R c = (R)cd_sd[i];
@@ -103,13 +148,42 @@ System<R> assemble(const fm3dt_subinv_desc &d, int nra, const int *nsrc, const i
             S.cd.push_back(c * c);
             dm_i = dm_i - dref;
             S.dmod.push_back(dm_i);
-            S.cnfe.push_back((int64_t)S.fcoln.size());
+            S.cnfe.push_back(jstep);
+            pick.push_back(i);
             if (d.rmtr == 1) {
                 const int iscn = idst[i] - 1;
                 srcm[iscn] = srcm[iscn] + dm_i;
                 ntsrc[iscn] += 1;
             }
         }
+    }
+    // pass 2, rows in parallel: entries (and the station-term entry)
+    S.fcoln.resize((size_t)jstep);
+    S.frech.resize((size_t)jstep);
+    {
+        const int np = (int)pick.size();
+        std::vector<int> bad(32, 0);
+        const int T = host_threads(jstep, 1 << 20);
+        parallel_chunks(np, T, [&](int t, int64_t a, int64_t b) {
+            for (int64_t r = a; r < b; ++r) {
+                const int i = pick[r];
+                int64_t o = S.cnfe[r];
+                for (int64_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k, ++o) {
+                    const int32_t c = cols[k];
+                    if (c < 1 || c > nmp) bad[t] = bad[t] ? bad[t] : c;
+                    S.fcoln[o] = c;
+                    S.frech[o] = (R)vals[k];
+                }
+                if (d.invst == 1) {
+                    S.fcoln[o] = nmpv + idrt[i];
+                    S.frech[o] = R(1);
+                }
+            }
+        });
+        for (int t = 0; t < 32; ++t)
+            if (bad[t])
+                throw Fail{FM3DT_SUBINV_EINVAL, "Frechet column " + std::to_string(bad[t]) + " outside 1.." +
+                                                    std::to_string(nmp)};
     }
     S.ntr = (int)S.dobs.size();
     if (d.rmtr == 1) {
@@ -120,52 +194,51 @@ System<R> assemble(const fm3dt_subinv_desc &d, int nra, const int *nsrc, const i
             for (int j = 0; j < ntsrc[s]; ++j, ++is) S.dmod[is] = S.dmod[is] - mean;
         }
     }
-    for (int32_t c : S.fcoln)
-        if (c < 1 || c > nmp) throw Fail{FM3DT_SUBINV_EINVAL, "Frechet column " + std::to_string(c) + " outside 1.." +
-                                                                  std::to_string(nmp)};
     // Transpose.  The reference walks columns i = 1..nmp and, in
     // each row, takes the next pending entry when its column equals i; so it
     // keeps each row's leading strictly increasing run of columns (all of a
     // sorted row) and drops the rest.  Entries within a column are by row.
+    // Counting sort by column in parallel: each thread counts and then fills
+    // a contiguous range of rows, after the earlier ranges' entries of every
+    // column, so each column lists its rows in order whatever the threads.
     std::vector<int64_t> take(S.ntr);
-    for (int j = 0; j < S.ntr; ++j) {
-        int64_t k = S.cnfe[j];
-        while (k < S.cnfe[j + 1] && (k == S.cnfe[j] || S.fcoln[k] > S.fcoln[k - 1])) ++k;
-        take[j] = k;
-    }
+    const int T = host_threads((int64_t)S.fcoln.size(), 1 << 20);
+    std::vector<std::vector<int64_t>> cnt(T, std::vector<int64_t>(nmp, 0));
+    parallel_chunks(S.ntr, T, [&](int t, int64_t a, int64_t b) {
+        for (int64_t j = a; j < b; ++j) {
+            int64_t k = S.cnfe[j];
+            while (k < S.cnfe[j + 1] && (k == S.cnfe[j] || S.fcoln[k] > S.fcoln[k - 1])) ++k;
+            take[j] = k;
+            for (int64_t q = S.cnfe[j]; q < k; ++q) cnt[t][S.fcoln[q] - 1] += 1;
+        }
+    });
     S.tcnfe.assign(nmp + 1, 0);
-    for (int j = 0; j < S.ntr; ++j)
-        for (int64_t k = S.cnfe[j]; k < take[j]; ++k) S.tcnfe[S.fcoln[k]] += 1;
-    for (int i = 0; i < nmp; ++i) S.tcnfe[i + 1] += S.tcnfe[i];
+    for (int i = 0; i < nmp; ++i) {
+        int64_t c = 0;
+        for (int t = 0; t < T; ++t) c += cnt[t][i];
+        S.tcnfe[i + 1] = S.tcnfe[i] + c;
+    }
+    // thread t starts each column after the threads before it
+    for (int i = 0; i < nmp; ++i) {
+        int64_t o = S.tcnfe[i];
+        for (int t = 0; t < T; ++t) {
+            const int64_t c = cnt[t][i];
+            cnt[t][i] = o;
+            o += c;
+        }
+    }
     S.tfcoln.resize(S.tcnfe[nmp]);
     S.tfrech.resize(S.tcnfe[nmp]);
-    std::vector<int64_t> fill(S.tcnfe.begin(), S.tcnfe.end() - 1);
-    for (int j = 0; j < S.ntr; ++j)
-        for (int64_t k = S.cnfe[j]; k < take[j]; ++k) {
-            const int64_t p = fill[S.fcoln[k] - 1]++;
-            S.tfcoln[p] = j + 1;
-            S.tfrech[p] = S.frech[k];
-        }
+    parallel_chunks(S.ntr, T, [&](int t, int64_t a, int64_t b) {
+        std::vector<int64_t> &fill = cnt[t];
+        for (int64_t j = a; j < b; ++j)
+            for (int64_t k = S.cnfe[j]; k < take[j]; ++k) {
+                const int64_t p = fill[S.fcoln[k] - 1]++;
+                S.tfcoln[p] = (int32_t)(j + 1);
+                S.tfrech[p] = S.frech[k];
+            }
+    });
     return S;
-}
-
-// fn(i) for i in [0, n) on the host's cores.  Each i is computed whole by
-// one thread, so results do not depend on the number of threads.
-template <typename F>
-void parallel_for(int n, F fn)
-{
-    const int nt = std::max(1, std::min((int)std::thread::hardware_concurrency(), std::min(32, n / 256)));
-    if (nt <= 1) {
-        for (int i = 0; i < n; ++i) fn(i);
-        return;
-    }
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; ++t)
-        th.emplace_back([&, t] {
-            const int a = (int)((int64_t)n * t / nt), b = (int)((int64_t)n * (t + 1) / nt);
-            for (int i = a; i < b; ++i) fn(i);
-        });
-    for (auto &x : th) x.join();
 }
 
 // y = G x / cd over the picked rows (the ga of S:764-773)
