@@ -163,6 +163,14 @@ def measured_peak_hbm():
 # by the nodes they process.
 KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.25, "stream_sweep_kernel": 28.6}
 
+# Warp instructions per node of the same kernels, from ncu's
+# smsp__inst_executed.sum summed over every launch of three solves of that
+# case: per node swept (main and near-tie sweeps), and per node staged by
+# the rounds (first round and tail rounds together).  The kernels are bound
+# by instruction issue, so the bench also reports the issue rate they reach
+# against the SMs' peak of four warp instructions per cycle.
+KERNEL_WARP_INST_PER_NODE = {"round_kernel": 34.04, "stream_sweep_kernel": 27.44}
+
 
 def _oracle_event(args):
     """One serial fast-marching solve of one event (spawned worker)."""
@@ -329,6 +337,15 @@ def run_ours(a):
     traffic = (KERNEL_DRAM_BYTES_PER_NODE[top] * k_nodes / max(1, k_launches)
                if top in KERNEL_DRAM_BYTES_PER_NODE and a.prec == "f32" else None)
 
+    issue = None
+    if top in KERNEL_WARP_INST_PER_NODE and a.prec == "f32" and k_ms > 0:
+        n_sm = torch.cuda.get_device_properties(0).multi_processor_count
+        mhz = clk["sm_mhz"] if clk else 2070.0
+        ach = KERNEL_WARP_INST_PER_NODE[top] * k_nodes / (k_ms / 1000.0) / 1e9
+        pk = n_sm * 4 * mhz * 1e6 / 1e9
+        issue = {"achieved": ach, "peak": pk, "unit": "G warp-instructions/s", "frac": ach / pk,
+                 "inst_per_node": KERNEL_WARP_INST_PER_NODE[top], "sm_mhz": mhz}
+
     extras = {}
     if not a.no_extras:
         # e2e through the public API with pinned host buffers
@@ -388,13 +405,14 @@ def run_ours(a):
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": top, "peak_source": peak_kind,
                      "alg_bytes_per_launch": per_launch,
-                     "avg_launch_ms": k_ms / max(1, k_launches)},
+                     "avg_launch_ms": k_ms / max(1, k_launches), "issue": issue},
         "solver": {"rounds_per_solve": round_launches / a.steps,
                    "tile_activations": sum(s["tile_updates"] for s in sts) / a.steps,
                    "node_passes_per_solve": sum(s["node_passes"] for s in sts) / a.steps,
                    "staged_nodes_per_solve": staged / a.steps, "device_ms_per_step": dev_ms / a.steps,
                    "round_ms_per_step": round_ms / a.steps, "sweep_ms_per_step": sweep_ms / a.steps,
                    "sweep_launches_per_step": sweep_launches / a.steps,
+                   "sweep_nodes_per_solve": sweep_nodes / a.steps,
                    "kernel_shares": {k: v[0] / max(1e-9, dev_ms) for k, v in kernels.items()},
                    "round_trace_tiles": trace_tiles, "round_trace_updates": trace_updates,
                    "round_trace_ms": trace_ms},
