@@ -204,6 +204,12 @@ int stream_segments(const fm3dt_ctx *ctx, int nitems, int nbx, int nbz, int sgri
 #ifndef FM_TIE_SWEEPS
 #define FM_TIE_SWEEPS 2
 #endif
+#ifndef FM_RESWEEPS
+#define FM_RESWEEPS 4
+#endif
+#ifndef FM_RESWEEP_FRAC
+#define FM_RESWEEP_FRAC 0.01
+#endif
 
 enum SolveMode { kFrames = 0, kResume = 1, kPoint = 2 };
 
@@ -261,14 +267,59 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     int sweep_launches = 0;
     int64_t sweep_nodes = 0;      // nodes visited by all sweep passes
     bool verified = false;
+    const bool streaming = ctx->sweep_shape >= kNumShapes;
+    const int sidx = streaming ? ctx->sweep_shape - kNumShapes : 0;
+    const int nbx = (g.nnx + kStreamShapes[sidx].sx - 1) / kStreamShapes[sidx].sx;
+    const int nbz = (g.nnz + kStreamShapes[sidx].sz - 1) / kStreamShapes[sidx].sz;
+    const int sgrid = streaming ? std::max(1, ctx->prec == FM3DT_FP64 ? occupancy_stream_f64(sidx)
+                                                                     : occupancy_stream_f32(sidx)) * sm_count()
+                                : 1;
+    // One streaming sweep of nitems events (events == null: all), lateral
+    // directions flipped by `flip`; with `flag`, changed nodes queue their
+    // tiles (and face neighbours) on list/count for the rounds.
+    auto stream_pass = [&](int nitems, const int *events, int flip, int nseg, int *flag, int *list,
+                           int *count) -> int {
+        sweep_nodes += (int64_t)nitems * (int64_t)ctx->N;
+        if (nseg <= 0) nseg = stream_segments(ctx, nitems, nbx, nbz, sgrid);
+        nseg = std::min(nseg, g.nnr);
+        const fm3dt_ctx::Planes *PP = nullptr;
+        int rc = ensure_block_planes(ctx, ctx->sweep_shape, nseg, &PP);
+        if (rc) return rc;
+        const auto &P = *PP;
+        const int seg_len = (g.nnr + nseg - 1) / nseg;
+        for (size_t h = 0; h < P.off.size(); ++h) {
+            const long long items = (long long)P.cnt[h] * nitems;
+            const int grid = (int)std::min<long long>(items, sgrid);
+            auto fill = [&](auto &a) {
+                a.hp_blocks = P.d_tiles; a.hoff = P.off[h]; a.hcount = P.cnt[h];
+                a.dir = ctx->d_dir; a.nev = nitems; a.nbx = nbx; a.nbz = nbz;
+                a.events = events;
+                a.flip = flip;
+                a.seg_len = seg_len;
+                a.flag = flag;
+                a.list = list; a.count = count;
+                a.tr = ts.tr; a.tx = ts.tx; a.tz = ts.tz;
+                a.ntr = ntr; a.ntx = ntx; a.ntz = ntz; a.tiles_per_event = tpe;
+            };
+            if (ctx->prec == FM3DT_FP64) {
+                StreamArgs<double> a{};
+                a.f = f64;
+                fill(a);
+                launch_stream_f64(sidx, grid, a, s);
+            } else {
+                StreamArgs<float> a{};
+                a.f = f32;
+                fill(a);
+                launch_stream_f32(sidx, grid, a, s);
+            }
+            ++sweep_launches;
+            ctx->launches += 1;
+        }
+        return FM3DT_OK;
+    };
     CK(cudaEventRecord(sw0, s));
-    if (do_sweep && ctx->sweep_shape >= kNumShapes) {
+    if (do_sweep && streaming) {
         // streaming sweep: one launch per column-block hyperplane
-        const int idx = ctx->sweep_shape - kNumShapes;
-        const StreamShape ss = kStreamShapes[idx];
-        const int nbx = (g.nnx + ss.sx - 1) / ss.sx, nbz = (g.nnz + ss.sz - 1) / ss.sz;
-        const int occ = ctx->prec == FM3DT_FP64 ? occupancy_stream_f64(idx) : occupancy_stream_f32(idx);
-        const int sgrid = std::max(1, occ) * sm_count();
         // the events whose lateral direction is a near tie get a second
         // sweep with it reversed
         CK(cudaMemcpyAsync(ctx->h_dir, ctx->d_dir, nev * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -287,50 +338,19 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         }
         // (FM_TIE_SWEEPS sweeps of the near-tie events, alternating reversed
         // and forward, stand for pass 1)
-        const int tie_sweeps = FM_TIE_SWEEPS;
-        for (int pp = 0; pp < 2 + tie_sweeps; ++pp) {
-            const int pass = pp == 0 ? 0 : (pp <= tie_sweeps ? 1 : 2);
-            const bool tie_forward = pass == 1 && ((pp - 1) & 1);
+        struct PassPlan { int pass, flip; };
+        std::vector<PassPlan> plan{{0, 0}};
+        for (int k = 0; k < FM_TIE_SWEEPS; ++k) plan.push_back({1, (k & 1) ? 0 : 4});
+        plan.push_back({2, 0});
+        for (const PassPlan &pl : plan) {
+            const int pass = pl.pass;
             if ((pass == 1 && ties.empty()) || (pass == 2 && !ctx->verify)) continue;
             const int nitems = pass == 1 ? (int)ties.size() : nev;
-            sweep_nodes += (int64_t)nitems * (int64_t)ctx->N;
-            int nseg = pass == 1 ? ctx->tie_segments : ctx->sweep_segments;
-            if (nseg <= 0) nseg = stream_segments(ctx, nitems, nbx, nbz, sgrid);
-            nseg = std::min(nseg, g.nnr);
-            const fm3dt_ctx::Planes *PP = nullptr;
-            int rc = ensure_block_planes(ctx, ctx->sweep_shape, nseg, &PP);
+            const int rc = stream_pass(nitems, pass == 1 ? ctx->d_events : nullptr, pl.flip,
+                                       pass == 1 ? ctx->tie_segments : ctx->sweep_segments,
+                                       pass == 2 ? ctx->d_flag : nullptr, ctx->d_list[0], ctx->d_count[0]);
             if (rc) return rc;
-            const auto &P = *PP;
-            const int seg_len = (g.nnr + nseg - 1) / nseg;
-            for (size_t h = 0; h < P.off.size(); ++h) {
-                const long long items = (long long)P.cnt[h] * nitems;
-                const int grid = (int)std::min<long long>(items, sgrid);
-                auto fill = [&](auto &a) {
-                    a.hp_blocks = P.d_tiles; a.hoff = P.off[h]; a.hcount = P.cnt[h];
-                    a.dir = ctx->d_dir; a.nev = nitems; a.nbx = nbx; a.nbz = nbz;
-                    a.events = pass == 1 ? ctx->d_events : nullptr;
-                    a.flip = pass == 1 && !tie_forward;
-                    a.seg_len = seg_len;
-                    a.flag = pass == 2 ? ctx->d_flag : nullptr;
-                    a.list = ctx->d_list[0]; a.count = ctx->d_count[0];
-                    a.tr = ts.tr; a.tx = ts.tx; a.tz = ts.tz;
-                    a.ntr = ntr; a.ntx = ntx; a.ntz = ntz; a.tiles_per_event = tpe;
-                };
-                if (ctx->prec == FM3DT_FP64) {
-                    StreamArgs<double> a{};
-                    a.f = f64;
-                    fill(a);
-                    launch_stream_f64(idx, grid, a, s);
-                } else {
-                    StreamArgs<float> a{};
-                    a.f = f32;
-                    fill(a);
-                    launch_stream_f32(idx, grid, a, s);
-                }
-                ++sweep_launches;
-            }
         }
-        ctx->launches += sweep_launches;
         CKL();
         verified = ctx->verify != 0;
     } else if (do_sweep) {
@@ -402,17 +422,24 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
 
     int rounds = 0;
     bool done = false;
-    double round_ms = 0.0;
+    double round_ms = 0.0, resweep_ms = 0.0;
     ctx->round_ms_trace.clear();
+    // after the first round of a swept solve, the events that still change
+    // on many tiles are swept again (FM_RESWEEPS times at most): corrections
+    // that the first round made deep in the grid then reach the top in one
+    // pass instead of one tile layer per round; the sweep queues the tiles
+    // it changes for the next round
+    int resweeps_left = (do_sweep && streaming && !verified) ? FM_RESWEEPS : 0;
     while (!done && rounds < max_rounds) {
         int k;
         const int first_round = rounds;
+        const int chunk_now = resweeps_left > 0 ? 1 : chunk;
         while ((int)ctx->round_events.size() < 2 * chunk) {
             cudaEvent_t e;
             CK(cudaEventCreate(&e));
             ctx->round_events.push_back(e);
         }
-        for (k = 0; k < chunk && rounds < max_rounds; ++k, ++rounds) {
+        for (k = 0; k < chunk_now && rounds < max_rounds; ++k, ++rounds) {
             const int cur = rounds & 1, nxt = cur ^ 1;
             CK(cudaMemsetAsync(ctx->d_count[nxt], 0, sizeof(int), s));
             CK(cudaEventRecord(ctx->round_events[2 * k], s));
@@ -442,6 +469,38 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             round_ms += m;
             if ((int)ctx->round_ms_trace.size() < fm3dt_ctx::kTraceRounds) ctx->round_ms_trace.push_back(m);
         }
+        if (resweeps_left > 0) {
+            --resweeps_left;
+            const int queued = *ctx->h_count;
+            if ((double)queued > FM_RESWEEP_FRAC * (double)nev * (double)tpe) {
+                std::vector<int> lst(queued);
+                CK(cudaMemcpy(lst.data(), ctx->d_list[last_next], (size_t)queued * sizeof(int), cudaMemcpyDeviceToHost));
+                std::vector<int> per(nev, 0);
+                for (int w : lst) per[w / tpe] += 1;
+                std::vector<int> busy;
+                for (int e = 0; e < nev; ++e)
+                    if ((double)per[e] > FM_RESWEEP_FRAC * (double)tpe) busy.push_back(e);
+                if (!busy.empty()) {
+                    cudaEvent_t r0, r1;
+                    CK(cudaEventCreate(&r0));
+                    CK(cudaEventCreate(&r1));
+                    CK(cudaMemcpyAsync(ctx->d_events, busy.data(), busy.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+                    CK(cudaEventRecord(r0, s));
+                    const int rc = stream_pass((int)busy.size(), ctx->d_events, 0, 0, ctx->d_flag,
+                                               ctx->d_list[last_next], ctx->d_count[last_next]);
+                    if (rc) return rc;
+                    CK(cudaEventRecord(r1, s));
+                    CKL();
+                    CK(cudaMemcpyAsync(ctx->h_count, ctx->d_count[last_next], sizeof(int), cudaMemcpyDeviceToHost, s));
+                    CK(cudaStreamSynchronize(s));
+                    float m = 0.0f;
+                    cudaEventElapsedTime(&m, r0, r1);
+                    resweep_ms += m;
+                    cudaEventDestroy(r0);
+                    cudaEventDestroy(r1);
+                }
+            }
+        }
         if (*ctx->h_count == 0) done = true;
     }
     CK(cudaEventRecord(ev1, s));
@@ -468,7 +527,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         st->ms = ms;
         st->round_ms = round_ms;
         st->round_launches = rounds;
-        st->sweep_ms = do_sweep ? sms : 0.0;
+        st->sweep_ms = do_sweep ? sms + resweep_ms : 0.0;
         st->sweep_launches = sweep_launches;
         st->sweep_nodes = sweep_nodes;
     }

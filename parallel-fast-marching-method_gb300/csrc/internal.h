@@ -90,7 +90,7 @@ struct StreamArgs {
     const int *dir;             // [E] bit 0: sweep +theta, bit 1: sweep +phi, bits 2/3: near ties
     const int *events;          // the events swept (indices), or null for events 0..nev-1
     int nev;
-    int flip;                   // reverse each near-tie lateral direction
+    int flip;                   // bit 0 / 1: reverse theta / phi; bit 2: reverse each near-tie lateral direction
     int nbx, nbz;               // column blocks per axis
     int seg_len;                // layers per height segment
     // verification sweep: when flag is set, every node whose value changes

@@ -75,7 +75,8 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
         const int packed = a.hp_blocks[a.hoff + j];
         const int seg = packed >> 24, bxp = (packed >> 12) & 0xfff, bzp = packed & 0xfff;
         int dir = a.dir[e];
-        if (a.flip) dir ^= ((dir >> 2) & 1) | (((dir >> 3) & 1) << 1);
+        if (a.flip & 4) dir ^= ((dir >> 2) & 1) | (((dir >> 3) & 1) << 1);
+        dir ^= a.flip & 3;
         const bool sx = dir & 1, sz = (dir >> 1) & 1;
         // this item's layers, counted upward from the bottom: [lo, hi)
         const int lo = seg * a.seg_len, hi = min(f.nnr, lo + a.seg_len);
