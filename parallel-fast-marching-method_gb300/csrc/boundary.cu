@@ -121,12 +121,13 @@ __global__ void fill_inf_kernel(R *__restrict__ T, size_t n)
         T[q] = (R)INFINITY;
 }
 
-__global__ void initial_tiles_kernel(int nev, int tiles_per_event, int first, int cnt, int *list, int *count,
-                                     int *flag)
+__global__ void initial_tiles_kernel(int nev, const int *events, int tiles_per_event, int first, int cnt,
+                                     int *list, int *count, int *flag)
 {
     const int total = nev * cnt;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
-        const int e = q / cnt, j = q - e * cnt;
+        const int k = q / cnt, j = q - k * cnt;
+        const int e = events ? events[k] : k;
         const int w = e * tiles_per_event + first + j;
         list[q] = w;
         flag[w] = kFull | kQueued;   // new to the solve: recompute every node
@@ -188,12 +189,13 @@ void launch_fill_inf(void *T, size_t n, int prec, cudaStream_t st)
         fill_inf_kernel<float><<<blocks_for((long long)n, 256), 256, 0, st>>>((float *)T, n);
 }
 
-void launch_initial_tiles(int nev, int tiles_per_event, int first_tile, int count_per_event, int *list,
-                          int *count, int *flag, cudaStream_t st)
+void launch_initial_tiles(int nev, const int *events, int tiles_per_event, int first_tile, int count_per_event,
+                          int *list, int *count, int *flag, cudaStream_t st)
 {
     const long long n = (long long)nev * count_per_event;
-    initial_tiles_kernel<<<blocks_for(n, 256), 256, 0, st>>>(nev, tiles_per_event, first_tile, count_per_event,
-                                                           list, count, flag);
+    if (n <= 0) return;
+    initial_tiles_kernel<<<blocks_for(n, 256), 256, 0, st>>>(nev, events, tiles_per_event, first_tile,
+                                                           count_per_event, list, count, flag);
 }
 
 void launch_to_absolute(const Geom &g, int prec, const void *T, size_t offset, double base, double *out,

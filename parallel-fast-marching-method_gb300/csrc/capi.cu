@@ -204,6 +204,9 @@ int stream_segments(const fm3dt_ctx *ctx, int nitems, int nbx, int nbz, int sgri
 #ifndef FM_TIE_SWEEPS
 #define FM_TIE_SWEEPS 2
 #endif
+#ifndef FM_OVERLAP_TIES
+#define FM_OVERLAP_TIES 1
+#endif
 #ifndef FM_RESWEEPS
 #define FM_RESWEEPS 4
 #endif
@@ -278,7 +281,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     // directions flipped by `flip`; with `flag`, changed nodes queue their
     // tiles (and face neighbours) on list/count for the rounds.
     auto stream_pass = [&](int nitems, const int *events, int flip, int nseg, int *flag, int *list,
-                           int *count) -> int {
+                           int *count, cudaStream_t st) -> int {
         sweep_nodes += (int64_t)nitems * (int64_t)ctx->N;
         if (nseg <= 0) nseg = stream_segments(ctx, nitems, nbx, nbz, sgrid);
         nseg = std::min(nseg, g.nnr);
@@ -305,12 +308,12 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                 StreamArgs<double> a{};
                 a.f = f64;
                 fill(a);
-                launch_stream_f64(sidx, grid, a, s);
+                launch_stream_f64(sidx, grid, a, st);
             } else {
                 StreamArgs<float> a{};
                 a.f = f32;
                 fill(a);
-                launch_stream_f32(sidx, grid, a, s);
+                launch_stream_f32(sidx, grid, a, st);
             }
             ++sweep_launches;
             ctx->launches += 1;
@@ -318,15 +321,17 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         return FM3DT_OK;
     };
     CK(cudaEventRecord(sw0, s));
+    std::vector<int> ties, others;     // near-tie events and the rest
+    bool overlap = false;              // ties' extra sweeps beside the others' first round
     if (do_sweep && streaming) {
         // streaming sweep: one launch per column-block hyperplane
         // the events whose lateral direction is a near tie get a second
         // sweep with it reversed
         CK(cudaMemcpyAsync(ctx->h_dir, ctx->d_dir, nev * sizeof(int), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
-        std::vector<int> ties;
         for (int e = 0; e < nev; ++e)
-            if (ctx->h_dir[e] & 12) ties.push_back(e);
+            (ctx->h_dir[e] & 12 ? ties : others).push_back(e);
+        overlap = FM_OVERLAP_TIES && !ctx->verify && !ties.empty() && !others.empty() && FM_TIE_SWEEPS > 0;
         if (!ties.empty())
             CK(cudaMemcpyAsync(ctx->d_events, ties.data(), ties.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         // pass 0 sweeps every event from the boundary, pass 1 the near-tie
@@ -344,11 +349,11 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         plan.push_back({2, 0});
         for (const PassPlan &pl : plan) {
             const int pass = pl.pass;
-            if ((pass == 1 && ties.empty()) || (pass == 2 && !ctx->verify)) continue;
+            if ((pass == 1 && (ties.empty() || overlap)) || (pass == 2 && !ctx->verify)) continue;
             const int nitems = pass == 1 ? (int)ties.size() : nev;
             const int rc = stream_pass(nitems, pass == 1 ? ctx->d_events : nullptr, pl.flip,
                                        pass == 1 ? ctx->tie_segments : ctx->sweep_segments,
-                                       pass == 2 ? ctx->d_flag : nullptr, ctx->d_list[0], ctx->d_count[0]);
+                                       pass == 2 ? ctx->d_flag : nullptr, ctx->d_list[0], ctx->d_count[0], s);
             if (rc) return rc;
         }
         CKL();
@@ -399,11 +404,13 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     CK(cudaMemsetAsync(ctx->d_trace, 0, 2 * sizeof(unsigned long long) * fm3dt_ctx::kTraceRounds, s));
     if (!verified) {
         CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
-        if (mode == kPoint)
+        if (overlap) {
+            // the first round is launched below, in two parts
+        } else if (mode == kPoint)
             launch_initial_tiles_box(nev, tpe, ntx, ntz, ts.tr, ts.tx, ts.tz, ctx->d_box_init, ctx->d_list[0],
                                      ctx->d_count[0], ctx->d_flag, s);
         else
-            launch_initial_tiles(nev, tpe, first, cnt, ctx->d_list[0], ctx->d_count[0], ctx->d_flag, s);
+            launch_initial_tiles(nev, nullptr, tpe, first, cnt, ctx->d_list[0], ctx->d_count[0], ctx->d_flag, s);
         ctx->launches += 1;
         CKL();
     }
@@ -430,6 +437,109 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     // pass instead of one tile layer per round; the sweep queues the tiles
     // it changes for the next round
     int resweeps_left = (do_sweep && streaming && !verified) ? FM_RESWEEPS : 0;
+    int grid_override = 0;   // launch grid other than the persistent one (0: persistent)
+    auto launch_round = [&](int round, int *cur_list, int *cur_count, int *next_list, int *next_count,
+                            cudaStream_t st) {
+        const int gr = grid_override > 0 ? grid_override : grid;
+        if (ctx->prec == FM3DT_FP64) {
+            a64.trace = round < fm3dt_ctx::kTraceRounds ? ctx->d_trace : nullptr;
+            a64.round = round;
+            a64.cur_list = cur_list; a64.cur_count = cur_count;
+            a64.next_list = next_list; a64.next_count = next_count;
+            launch_round_f64(shape, gr, a64, st);
+        } else {
+            a32.trace = round < fm3dt_ctx::kTraceRounds ? ctx->d_trace : nullptr;
+            a32.round = round;
+            a32.cur_list = cur_list; a32.cur_count = cur_count;
+            a32.next_list = next_list; a32.next_count = next_count;
+            launch_round_f32(shape, gr, a32, st);
+        }
+        ctx->launches += 1;
+    };
+    // events that still change on many tiles after a round are swept again
+    // (see resweeps_left); `nl` is the list the next round takes
+    auto maybe_resweep = [&](int nl) -> int {
+        if (resweeps_left <= 0) return FM3DT_OK;
+        --resweeps_left;
+        const int queued = *ctx->h_count;
+        if (!((double)queued > FM_RESWEEP_FRAC * (double)nev * (double)tpe)) return FM3DT_OK;
+        std::vector<int> lst(queued);
+        CK(cudaMemcpy(lst.data(), ctx->d_list[nl], (size_t)queued * sizeof(int), cudaMemcpyDeviceToHost));
+        std::vector<int> per(nev, 0);
+        for (int w : lst) per[w / tpe] += 1;
+        std::vector<int> busy;
+        for (int e = 0; e < nev; ++e)
+            if ((double)per[e] > FM_RESWEEP_FRAC * (double)tpe) busy.push_back(e);
+        if (busy.empty()) return FM3DT_OK;
+        cudaEvent_t r0, r1;
+        CK(cudaEventCreate(&r0));
+        CK(cudaEventCreate(&r1));
+        CK(cudaMemcpyAsync(ctx->d_events, busy.data(), busy.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaEventRecord(r0, s));
+        const int rc = stream_pass((int)busy.size(), ctx->d_events, 0, 0, ctx->d_flag, ctx->d_list[nl],
+                                   ctx->d_count[nl], s);
+        if (rc) return rc;
+        CK(cudaEventRecord(r1, s));
+        CKL();
+        CK(cudaMemcpyAsync(ctx->h_count, ctx->d_count[nl], sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        float m = 0.0f;
+        cudaEventElapsedTime(&m, r0, r1);
+        resweep_ms += m;
+        cudaEventDestroy(r0);
+        cudaEventDestroy(r1);
+        return FM3DT_OK;
+    };
+    if (overlap) {
+        // first round, in two parts that run side by side: the other events'
+        // tiles on the context stream from the end of the main sweep, one CTA
+        // per tile so that blocks free up as they finish; the near-tie events'
+        // extra sweeps and then their tiles on stream2, whose higher priority
+        // gets its blocks scheduled first; both queue onto list 1
+        cudaEvent_t fork, join, r0, r1;
+        CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+        CK(cudaEventCreate(&r0));
+        CK(cudaEventCreate(&r1));
+        CK(cudaMemcpyAsync(ctx->d_events, ties.data(), ties.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->d_events_b, others.data(), others.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaEventRecord(r0, s));
+        CK(cudaEventRecord(fork, s));
+        cudaStream_t s2 = ctx->stream2;
+        CK(cudaStreamWaitEvent(s2, fork, 0));
+        for (int k = 0; k < FM_TIE_SWEEPS; ++k) {
+            const int rc = stream_pass((int)ties.size(), ctx->d_events, (k & 1) ? 0 : 4, ctx->tie_segments,
+                                       nullptr, ctx->d_list[0], ctx->d_count[0], s2);
+            if (rc) return rc;
+        }
+        launch_initial_tiles((int)ties.size(), ctx->d_events, tpe, first, cnt, ctx->d_list_b, ctx->d_count_b,
+                             ctx->d_flag, s2);
+        launch_round(0, ctx->d_list_b, ctx->d_count_b, ctx->d_list[1], ctx->d_count[1], s2);
+        CK(cudaEventRecord(join, s2));
+        launch_initial_tiles((int)others.size(), ctx->d_events_b, tpe, first, cnt, ctx->d_list[0], ctx->d_count[0],
+                             ctx->d_flag, s);
+        grid_override = (int)std::min<long long>((long long)others.size() * cnt, 1LL << 30);
+        launch_round(0, ctx->d_list[0], ctx->d_count[0], ctx->d_list[1], ctx->d_count[1], s);
+        grid_override = 0;
+        CK(cudaStreamWaitEvent(s, join, 0));
+        CK(cudaEventRecord(r1, s));
+        ctx->launches += 2;
+        CKL();
+        CK(cudaMemcpyAsync(ctx->h_count, ctx->d_count[1], sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        float m = 0.0f;
+        cudaEventElapsedTime(&m, r0, r1);
+        round_ms += m;
+        ctx->round_ms_trace.push_back(m);
+        cudaEventDestroy(fork);
+        cudaEventDestroy(join);
+        cudaEventDestroy(r0);
+        cudaEventDestroy(r1);
+        rounds = 1;
+        const int rc = maybe_resweep(1);
+        if (rc) return rc;
+        if (*ctx->h_count == 0) done = true;
+    }
     while (!done && rounds < max_rounds) {
         int k;
         const int first_round = rounds;
@@ -443,21 +553,8 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             const int cur = rounds & 1, nxt = cur ^ 1;
             CK(cudaMemsetAsync(ctx->d_count[nxt], 0, sizeof(int), s));
             CK(cudaEventRecord(ctx->round_events[2 * k], s));
-            if (ctx->prec == FM3DT_FP64) {
-                a64.trace = rounds < fm3dt_ctx::kTraceRounds ? ctx->d_trace : nullptr;
-                a64.round = rounds;
-                a64.cur_list = ctx->d_list[cur]; a64.cur_count = ctx->d_count[cur];
-                a64.next_list = ctx->d_list[nxt]; a64.next_count = ctx->d_count[nxt];
-                launch_round_f64(shape, grid, a64, s);
-            } else {
-                a32.trace = rounds < fm3dt_ctx::kTraceRounds ? ctx->d_trace : nullptr;
-                a32.round = rounds;
-                a32.cur_list = ctx->d_list[cur]; a32.cur_count = ctx->d_count[cur];
-                a32.next_list = ctx->d_list[nxt]; a32.next_count = ctx->d_count[nxt];
-                launch_round_f32(shape, grid, a32, s);
-            }
+            launch_round(rounds, ctx->d_list[cur], ctx->d_count[cur], ctx->d_list[nxt], ctx->d_count[nxt], s);
             CK(cudaEventRecord(ctx->round_events[2 * k + 1], s));
-            ctx->launches += 1;
         }
         CKL();
         const int last_next = ((rounds - 1) & 1) ^ 1;
@@ -469,38 +566,8 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             round_ms += m;
             if ((int)ctx->round_ms_trace.size() < fm3dt_ctx::kTraceRounds) ctx->round_ms_trace.push_back(m);
         }
-        if (resweeps_left > 0) {
-            --resweeps_left;
-            const int queued = *ctx->h_count;
-            if ((double)queued > FM_RESWEEP_FRAC * (double)nev * (double)tpe) {
-                std::vector<int> lst(queued);
-                CK(cudaMemcpy(lst.data(), ctx->d_list[last_next], (size_t)queued * sizeof(int), cudaMemcpyDeviceToHost));
-                std::vector<int> per(nev, 0);
-                for (int w : lst) per[w / tpe] += 1;
-                std::vector<int> busy;
-                for (int e = 0; e < nev; ++e)
-                    if ((double)per[e] > FM_RESWEEP_FRAC * (double)tpe) busy.push_back(e);
-                if (!busy.empty()) {
-                    cudaEvent_t r0, r1;
-                    CK(cudaEventCreate(&r0));
-                    CK(cudaEventCreate(&r1));
-                    CK(cudaMemcpyAsync(ctx->d_events, busy.data(), busy.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-                    CK(cudaEventRecord(r0, s));
-                    const int rc = stream_pass((int)busy.size(), ctx->d_events, 0, 0, ctx->d_flag,
-                                               ctx->d_list[last_next], ctx->d_count[last_next]);
-                    if (rc) return rc;
-                    CK(cudaEventRecord(r1, s));
-                    CKL();
-                    CK(cudaMemcpyAsync(ctx->h_count, ctx->d_count[last_next], sizeof(int), cudaMemcpyDeviceToHost, s));
-                    CK(cudaStreamSynchronize(s));
-                    float m = 0.0f;
-                    cudaEventElapsedTime(&m, r0, r1);
-                    resweep_ms += m;
-                    cudaEventDestroy(r0);
-                    cudaEventDestroy(r1);
-                }
-            }
-        }
+        const int rc = maybe_resweep(last_next);
+        if (rc) return rc;
         if (*ctx->h_count == 0) done = true;
     }
     CK(cudaEventRecord(ev1, s));
@@ -643,6 +710,14 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMallocHost(&ctx->h_count, sizeof(int)));
     CKC(cudaMallocHost(&ctx->h_dir, ctx->maxev * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_events, ctx->maxev * sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_events_b, ctx->maxev * sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_list_b, ctx->flag_capacity * sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_count_b, sizeof(int)));
+    {
+        int least = 0, greatest = 0;
+        CKC(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CKC(cudaStreamCreateWithPriority(&ctx->stream2, cudaStreamNonBlocking, greatest));
+    }
     CKC(cudaMallocHost(&ctx->h_stats, 3 * sizeof(unsigned long long)));
     CKC(cudaMemset(ctx->d_base, 0, ctx->maxev * sizeof(double)));
     int rc = ctx->prec == FM3DT_FP64 ? upload_geometry<double>(ctx) : upload_geometry<float>(ctx);
@@ -1126,6 +1201,10 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     for (auto &P : ctx->planes) cudaFree(P.d_tiles);
     for (auto &P : ctx->block_planes) cudaFree(P.d_tiles);
     cudaFree(ctx->d_events);
+    cudaFree(ctx->d_events_b);
+    cudaFree(ctx->d_list_b);
+    cudaFree(ctx->d_count_b);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     if (ctx->h_dir) cudaFreeHost(ctx->h_dir);
     cudaFree(ctx->d_T);
     cudaFree(ctx->d_frames);

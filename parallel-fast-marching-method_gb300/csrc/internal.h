@@ -135,7 +135,8 @@ void launch_finalize_frames(const Geom &g, int nev, int prec, const double *fram
                             uint8_t *frozen, double *base, cudaStream_t st);
 void launch_fill_inf(void *T, size_t n, int prec, cudaStream_t st);
 void launch_sweep_directions(const Geom &g, int nev, const double *frames, int *dir, cudaStream_t st);
-void launch_initial_tiles(int nev, int tiles_per_event, int first_tile, int count_per_event,
+// (events: the event of each of the nev entries; null = 0..nev-1)
+void launch_initial_tiles(int nev, const int *events, int tiles_per_event, int first_tile, int count_per_event,
                           int *list, int *count, int *flag, cudaStream_t st);
 void launch_initial_tiles_box(int nev, int tiles_per_event, int ntx, int ntz, int tr, int tx, int tz,
                               const int *box, int *list, int *count, int *flag, cudaStream_t st);
@@ -225,6 +226,12 @@ struct fm3dt_ctx {
     int tie_segments = 0;         // the same for the reversed sweep of near-tie events
     int *h_dir = nullptr;         // pinned [maxev] sweep directions of the last solve
     int *d_events = nullptr;      // [maxev] the near-tie events of the last solve
+    // the first round of the other events runs on stream2 while the near-tie
+    // events get their extra sweeps; their first round then takes list_b
+    cudaStream_t stream2 = nullptr;
+    int *d_events_b = nullptr;    // [maxev] the other events
+    int *d_list_b = nullptr;      // [flag_capacity]
+    int *d_count_b = nullptr;
     Planes planes[fm3dt::kNumSweepShapes];   // tile hyperplanes, then column-block hyperplanes
     size_t flag_capacity = 0;     // tiles allocated for flags/lists
     int64_t launches = 0;
