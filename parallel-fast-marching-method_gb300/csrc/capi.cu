@@ -508,8 +508,12 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         cudaStream_t s2 = ctx->stream2;
         CK(cudaStreamWaitEvent(s2, fork, 0));
         for (int k = 0; k < FM_TIE_SWEEPS; ++k) {
-            const int rc = stream_pass((int)ties.size(), ctx->d_events, (k & 1) ? 0 : 4, ctx->tie_segments,
-                                       nullptr, ctx->d_list[0], ctx->d_count[0], s2);
+            // beside the first round the extra sweeps need no parallelism of
+            // their own: two height segments (less pipeline ramp than the
+            // automatic choice for a few dozen events)
+            const int rc = stream_pass((int)ties.size(), ctx->d_events, (k & 1) ? 0 : 4,
+                                       ctx->tie_segments > 0 ? ctx->tie_segments : 2, nullptr, ctx->d_list[0],
+                                       ctx->d_count[0], s2);
             if (rc) return rc;
         }
         launch_initial_tiles((int)ties.size(), ctx->d_events, tpe, first, cnt, ctx->d_list_b, ctx->d_count_b,
