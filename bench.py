@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--sweep-shape", type=int, default=-1, help="sweep tile shape index (-1: same as --shape)")
     ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline, FP64 check and e2e leg")
     ap.add_argument("--duration", type=float, default=30.0, help="config 4: seconds of Poisson arrivals")
+    ap.add_argument("--sweep-mode", type=int, default=1,
+                    help="with --shape: 1 sweep then rounds, 2 sweep + verifying sweep, 0 no sweep")
     ap.add_argument("--segments", type=int, nargs=2, default=(0, 0),
                     help="streaming sweep height segments (all events, near-tie events); 0 = automatic")
     return ap.parse_args()
@@ -279,7 +281,7 @@ def run_ours(a):
 
     if a.shape >= 0:
         sweep_shape = a.sweep_shape if a.sweep_shape >= 0 else a.shape
-        solver.set_tuning(a.shape, a.passes or 64, 0, 1)
+        solver.set_tuning(a.shape, a.passes or 64, 0, a.sweep_mode)
         solver.set_sweep_shape(sweep_shape)
         tuned = (a.shape, a.passes or 64, sweep_shape, None)
     else:
