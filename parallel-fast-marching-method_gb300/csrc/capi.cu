@@ -204,6 +204,9 @@ int stream_segments(const fm3dt_ctx *ctx, int nitems, int nbx, int nbz, int sgri
 #ifndef FM_TIE_SWEEPS
 #define FM_TIE_SWEEPS 2
 #endif
+#ifndef FM_ROUND0_PER_TILE
+#define FM_ROUND0_PER_TILE 1
+#endif
 #ifndef FM_OVERLAP_TIES
 #define FM_OVERLAP_TIES 1
 #endif
@@ -557,7 +560,12 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             const int cur = rounds & 1, nxt = cur ^ 1;
             CK(cudaMemsetAsync(ctx->d_count[nxt], 0, sizeof(int), s));
             CK(cudaEventRecord(ctx->round_events[2 * k], s));
+            // the first round's tile count is known on the host: one CTA per
+            // tile, so blocks free up as they finish
+            if (rounds == 0 && FM_ROUND0_PER_TILE && !verified && mode != kPoint)
+                grid_override = (int)std::min<long long>((long long)nev * cnt, 1LL << 30);
             launch_round(rounds, ctx->d_list[cur], ctx->d_count[cur], ctx->d_list[nxt], ctx->d_count[nxt], s);
+            grid_override = 0;
             CK(cudaEventRecord(ctx->round_events[2 * k + 1], s));
         }
         CKL();
