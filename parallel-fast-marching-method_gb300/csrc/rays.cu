@@ -6,8 +6,9 @@
 // reference's ray hand-off between subdomains (F:6464-6501) and the partial
 // rows it creates disappear; the global outer faces stop a ray exactly where
 // the reference's boundary subdomains stop it (clip to the first face
-// crossed, F:7474-7541).  The row accumulates in single precision in the same
-// order as the reference's REAL(4) fdm (F:7722-7732), including its quirks:
+// crossed, F:7474-7541).  The ray path is double precision like the
+// reference's; the row's weights are single precision and accumulate in the
+// same order as the reference's REAL(4) fdm (F:7722-7732), including its quirks:
 // the segment clipped at the grid face is integrated with the full nominal
 // step length (dinc from vrat*dpl), and the start-point B-spline weights of a
 // sub-segment that follows a velocity-cell crossing keep the indices of the
@@ -17,17 +18,17 @@
 
 namespace fm3dt {
 
-// Cubic B-spline weights.  The Frechet weights (not the ray path) use
-// products with reciprocals where the reference divides: the row values move
-// by an FP64 rounding at most, far inside their single-precision storage.
-__device__ __forceinline__ void bspl(double u, double w[4])
+// Single-precision Frechet weights: the row is accumulated in REAL(4), so its
+// weights need no more; the FP64 pipe (a small fraction of FP32 throughput on
+// this GPU) is kept for the ray path itself, whose end points must match.
+__device__ __forceinline__ void bsplf(float u, float w[4])
 {
-    const double sixth = 1.0 / 6.0;
-    const double u2 = u * u, u3 = u * u * u;
-    const double om = 1.0 - u;
+    const float sixth = 1.0f / 6.0f;
+    const float u2 = u * u, u3 = u * u * u;
+    const float om = 1.0f - u;
     w[0] = om * om * om * sixth;
-    w[1] = (4.0 - 6.0 * u2 + 3.0 * u3) * sixth;
-    w[2] = (1.0 + 3.0 * u + 3.0 * u2 - 3.0 * u3) * sixth;
+    w[1] = (4.0f - 6.0f * u2 + 3.0f * u3) * sixth;
+    w[2] = (1.0f + 3.0f * u + 3.0f * u2 - 3.0f * u3) * sixth;
     w[3] = u3 * sixth;
 }
 
@@ -41,20 +42,21 @@ __device__ __forceinline__ double veln_at(const Geom &g, const double *veln, int
     return veln[(size_t)(iz + 1) + (size_t)(g.nnz + 3) * ((size_t)(ix + 1) + (size_t)(g.nnx + 3) * (size_t)(ir + 1))];
 }
 
-// trilinear velocity at a point of propagation cell (ipz,ipx,ipr) (F:7629-7641);
-// inr/inx/inz: reciprocals of the node spacings
-__device__ double trilin(const Geom &g, const double *veln, int ipz, int ipx, int ipr, double drr, double drx,
-                         double drz, double inr, double inx, double inz)
+// trilinear velocity at a point of propagation cell (ipz,ipx,ipr) (F:7629-7641),
+// in single precision (it only weights the Frechet row); inr/inx/inz: reciprocals
+// of the node spacings
+__device__ float trilinf(const Geom &g, const double *veln, int ipz, int ipx, int ipr, float drr, float drx, float drz,
+                         float dnr, float dnx, float dnz, float inr, float inx, float inz)
 {
-    double vel = 0.0;
+    float vel = 0.0f;
     for (int k = 1; k <= 2; ++k)
         for (int l = 1; l <= 2; ++l)
             for (int m = 1; m <= 2; ++m) {
-                double produ = (1.0 - fabs(((double)(m - 1) * g.dnz - drz) * inz));
-                produ = produ * (1.0 - fabs(((double)(l - 1) * g.dnx - drx) * inx));
-                produ = produ * (1.0 - fabs(((double)(k - 1) * g.dnr - drr) * inr));
+                float produ = (1.0f - fabsf(((float)(m - 1) * dnz - drz) * inz));
+                produ = produ * (1.0f - fabsf(((float)(l - 1) * dnx - drx) * inx));
+                produ = produ * (1.0f - fabsf(((float)(k - 1) * dnr - drr) * inr));
                 if (ipz - 1 + m <= g.nnz + 1 && ipx - 1 + l <= g.nnx + 1 && ipr - 1 + k <= g.nnr + 1)
-                    vel = vel + veln_at(g, veln, ipz - 1 + m, ipx - 1 + l, ipr - 1 + k) * produ;
+                    vel = vel + (float)veln_at(g, veln, ipz - 1 + m, ipx - 1 + l, ipr - 1 + k) * produ;
             }
     return vel;
 }
@@ -69,7 +71,8 @@ __global__ void rays_kernel(RayArgs a)
     const size_t nmp = (size_t)(g.nvr + 2) * (g.nvx + 2) * (g.nvz + 2);
     const int maxrp = 100000;        // F:7262
     const double dpl = g.dnr;        // F:7290
-    const double inr = 1.0 / g.dnr, inx = 1.0 / g.dnx, inz = 1.0 / g.dnz;
+    const float fnr = (float)g.dnr, fnx = (float)g.dnx, fnz = (float)g.dnz;
+    const float inr = 1.0f / fnr, inx = 1.0f / fnx, inz = 1.0f / fnz;
     const double ivr_ = 1.0 / g.dvr, ivx_ = 1.0 / g.dvx, ivz_ = 1.0 / g.dvz;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
         const int e = q / a.nrc, i = q - e * a.nrc;
@@ -200,18 +203,19 @@ __global__ void rays_kernel(RayArgs a)
                     double drr = (g.rgor - rgr) - (double)(ipro - 1) * g.dnr;
                     double drx = (rgx - g.rgox) - (double)(ipxo - 1) * g.dnx;
                     double drz = (rgz - g.rgoz) - (double)(ipzo - 1) * g.dnz;
-                    double vel = trilin(g, a.veln, ipzo, ipxo, ipro, drr, drx, drz, inr, inx, inz);
-                    double iv2 = 1.0 / (vel * vel);
-                    double ui[4], vi[4], wi[4], uio[4], vio[4], wio[4];
+                    float vel = trilinf(g, a.veln, ipzo, ipxo, ipro, (float)drr, (float)drx, (float)drz, fnr, fnx, fnz,
+                                        inr, inx, inz);
+                    float iv2 = 1.0f / (vel * vel);
+                    float ui[4], vi[4], wi[4], uio[4], vio[4], wio[4];
                     drr = (g.gor - rgr) - (double)(ivro - 1) * g.dvr;
                     drx = (rgx - g.gox) - (double)(ivxo - 1) * g.dvx;
                     drz = (rgz - g.goz) - (double)(ivzo - 1) * g.dvz;
-                    bspl(drr * ivr_, ui);
-                    bspl(drx * ivx_, vi);
-                    bspl(drz * ivz_, wi);
+                    bsplf((float)(drr * ivr_), ui);
+                    bsplf((float)(drx * ivx_), vi);
+                    bsplf((float)(drz * ivz_), wi);
                     int ivrt = ivro, ivxt = ivxo, ivzt = ivzo;
                     for (int k = 0; k < nhp; ++k) {
-                        const double iv2o = iv2;
+                        const float iv2o = iv2;
                         for (int m = 0; m < 4; ++m) { uio[m] = ui[m]; vio[m] = vi[m]; wio[m] = wi[m]; }
                         if (k > 0) {
                             if (chp[k - 1] == 1) ivrt = ivr;
@@ -227,16 +231,17 @@ __global__ void rays_kernel(RayArgs a)
                         drr = (g.rgor - rigr) - (double)(iprt - 1) * g.dnr;
                         drx = (rigx - g.rgox) - (double)(ipxt - 1) * g.dnx;
                         drz = (rigz - g.rgoz) - (double)(ipzt - 1) * g.dnz;
-                        vel = trilin(g, a.veln, ipzt, ipxt, iprt, drr, drx, drz, inr, inx, inz);
-                        iv2 = 1.0 / (vel * vel);
+                        vel = trilinf(g, a.veln, ipzt, ipxt, iprt, (float)drr, (float)drx, (float)drz, fnr, fnx, fnz,
+                                      inr, inx, inz);
+                        iv2 = 1.0f / (vel * vel);
                         drr = (g.gor - rigr) - (double)(ivrt - 1) * g.dvr;
                         drx = (rigx - g.gox) - (double)(ivxt - 1) * g.dvx;
                         drz = (rigz - g.goz) - (double)(ivzt - 1) * g.dvz;
-                        bspl(drr * ivr_, ui);
-                        bspl(drx * ivx_, vi);
-                        bspl(drz * ivz_, wi);
+                        bsplf((float)(drr * ivr_), ui);
+                        bsplf((float)(drx * ivx_), vi);
+                        bsplf((float)(drz * ivz_), wi);
                         const double dinc = (k == 0) ? vrat[k] * dpl : (vrat[k] - vrat[k - 1]) * dpl;
-                        const double hd = 0.5 * dinc;
+                        const float hd = (float)(0.5 * dinc);
                         if (ivzt - 1 < 0 || ivzt + 2 > g.nvz + 1 || ivxt - 1 < 0 || ivxt + 2 > g.nvx + 1 ||
                             ivrt - 1 < 0 || ivrt + 2 > g.nvr + 1) {
                             st = 1;
@@ -247,11 +252,11 @@ __global__ void rays_kernel(RayArgs a)
                             for (int m = 0; m < 4; ++m) {
                                 float *rowp = fdm + (size_t)(ivrt - 1 + n) +
                                               (size_t)(g.nvr + 2) * ((size_t)(ivxt - 1 + m) + (size_t)(g.nvx + 2) * (size_t)(ivzt - 1));
-                                const double uv = ui[n] * vi[m] * iv2, uvo = uio[n] * vio[m] * iv2o;
+                                const float uv = ui[n] * vi[m] * iv2, uvo = uio[n] * vio[m] * iv2o;
                                 for (int l = 0; l < 4; ++l) {
-                                    const double a1 = -(uv * wi[l] + uvo * wio[l]) * hd;
+                                    const float a1 = -(uv * wi[l] + uvo * wio[l]) * hd;
                                     float *p = rowp + zstride * (size_t)l;
-                                    *p = (float)(a1 + (double)*p);
+                                    *p = a1 + *p;
                                 }
                             }
                     }
