@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -201,6 +202,51 @@ int stream_segments(const fm3dt_ctx *ctx, int nitems, int nbx, int nbz, int sgri
 // How a solve starts: from boundary frames (initialisation, sweep, rounds),
 // from the current fields (resume: rounds with every tile active), or from
 // point-source boxes the caller already wrote (rounds from the boxes' tiles).
+// The field as a 4-D tensor (phi, theta, r, event) for TMA copies of a round
+// tile's box; null when TMA cannot be used (phi rows not a multiple of 16
+// bytes, the driver entry point missing, or switched off).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled_fn()
+{
+    static EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return (EncodeTiledFn)p;
+    }();
+    return fn;
+}
+
+const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
+{
+    if (!ctx->use_tma) return nullptr;
+    if (ctx->tmap_ok[shape]) return &ctx->tmap[shape];
+    const Geom &g = ctx->g;
+    const size_t es = ctx->prec == FM3DT_FP64 ? 8 : 4;
+    if (((size_t)g.nnz * es) % 16 != 0) return nullptr;
+    EncodeTiledFn enc = encode_tiled_fn();
+    if (!enc) return nullptr;
+    const TileShape ts = kShapes[shape];
+    const cuuint64_t dims[4] = {(cuuint64_t)g.nnz, (cuuint64_t)g.nnx, (cuuint64_t)g.nnr, (cuuint64_t)ctx->maxev};
+    const cuuint64_t strides[3] = {(cuuint64_t)g.nnz * es, (cuuint64_t)g.nnz * g.nnx * es,
+                                   (cuuint64_t)g.nnz * g.nnx * g.nnr * es};
+    // the box of Tile<R, tr, tx, tz>: tz + 8 phi columns, 2-deep halos in theta and r
+    const cuuint32_t box[4] = {(cuuint32_t)(ts.tz + 8), (cuuint32_t)(ts.tx + 4), (cuuint32_t)(ts.tr + 4), 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = enc(&ctx->tmap[shape], es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                           ctx->d_T, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NAN_REQUEST_ZERO_FMA);
+    if (r != CUDA_SUCCESS) return nullptr;
+    ctx->tmap_ok[shape] = true;
+    return &ctx->tmap[shape];
+}
+
 #ifndef FM_TIE_SWEEPS
 #define FM_TIE_SWEEPS 2
 #endif
@@ -429,6 +475,16 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     a64.flag = a32.flag = ctx->d_flag;
     a64.max_passes = a32.max_passes = ctx->max_passes;
     a64.stats = a32.stats = ctx->d_stats;
+    a64.err = a32.err = ctx->d_err;
+    {
+        const CUtensorMap *map = field_tensor_map(ctx, shape);
+        a64.tma = a32.tma = map ? 1 : 0;
+        if (map) {
+            a64.tmap = *map;
+            a32.tmap = *map;
+        }
+    }
+    CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), s));
 
     int rounds = 0;
     bool done = false;
@@ -584,6 +640,8 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     }
     CK(cudaEventRecord(ev1, s));
     CK(cudaMemcpyAsync(ctx->h_stats, ctx->d_stats, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    int kerr = 0;
+    CK(cudaMemcpyAsync(&kerr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     ctx->h_base.resize(nev);
     CK(cudaMemcpyAsync(ctx->h_base.data(), ctx->d_base, nev * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -610,6 +668,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         st->sweep_launches = sweep_launches;
         st->sweep_nodes = sweep_nodes;
     }
+    if (kerr) return fail(ctx, FM3DT_ECUDA, "a tile copy (TMA) did not complete in time");
     if (!done) return fail(ctx, FM3DT_ENOCONV, "solver round limit reached before convergence");
     return FM3DT_OK;
 }
@@ -725,6 +784,11 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMalloc(&ctx->d_events_b, ctx->maxev * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_list_b, ctx->flag_capacity * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_count_b, sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_err, sizeof(int)));
+    {
+        const char *env = std::getenv("FM3DT_TMA");
+        if (env && env[0] == '0') ctx->use_tma = 0;
+    }
     {
         int least = 0, greatest = 0;
         CKC(cudaDeviceGetStreamPriorityRange(&least, &greatest));
@@ -1216,6 +1280,7 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_events_b);
     cudaFree(ctx->d_list_b);
     cudaFree(ctx->d_count_b);
+    cudaFree(ctx->d_err);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     if (ctx->h_dir) cudaFreeHost(ctx->h_dir);
     cudaFree(ctx->d_T);

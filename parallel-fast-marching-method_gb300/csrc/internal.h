@@ -1,6 +1,7 @@
 // internal.h -- device data layout and kernel launchers of libfm3dt_gpu.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -62,6 +63,12 @@ struct RoundArgs {
     unsigned long long *stats;  // [0] tiles processed, [1] node updates, [2] staged nodes
     unsigned long long *trace;  // per round: [2*round] tiles, [2*round+1] node updates (or null)
     int round;
+    // tile + halo box by one TMA copy (tma != 0): the field as a 4-D tensor
+    // (phi, theta, r, event) with the box of the tile shape; err is raised if
+    // a copy does not complete in time
+    int tma;
+    int *err;
+    alignas(64) CUtensorMap tmap;
 };
 
 // Arguments of one sweep launch (one tile hyperplane).
@@ -232,6 +239,11 @@ struct fm3dt_ctx {
     int *d_events_b = nullptr;    // [maxev] the other events
     int *d_list_b = nullptr;      // [flag_capacity]
     int *d_count_b = nullptr;
+    // TMA tensor maps of the field, by round tile shape (encoded on first use)
+    int *d_err = nullptr;         // raised by a kernel whose bounded wait gave up
+    bool tmap_ok[fm3dt::kNumShapes] = {};
+    CUtensorMap tmap[fm3dt::kNumShapes];
+    int use_tma = 1;
     Planes planes[fm3dt::kNumSweepShapes];   // tile hyperplanes, then column-block hyperplanes
     size_t flag_capacity = 0;     // tiles allocated for flags/lists
     int64_t launches = 0;

@@ -37,10 +37,16 @@ namespace fm3dt {
 __device__ __forceinline__ unsigned long long fbits(float v) { return __float_as_uint(v); }
 __device__ __forceinline__ unsigned long long fbits(double v) { return (unsigned long long)__double_as_longlong(v); }
 
+// Shared box of a tile: the tile with 2-deep halos in r and theta, and in phi
+// (contiguous) 4 columns either side, so that a TMA copy of the box starts on a
+// 16-byte boundary (the tile starts at a multiple of TZ; 4 elements before it
+// is 16 bytes before in single precision, 32 in double).  Only the 2 columns
+// next to the tile are read.
 template <typename R, int TR, int TX, int TZ>
 struct Tile {
     static constexpr int NT = TX * TZ;
-    static constexpr int BR = TR + 4, BX = TX + 4, BZ = TZ + 4;
+    static constexpr int ZOFF = 4;        // phi index of the tile's first node in the box
+    static constexpr int BR = TR + 4, BX = TX + 4, BZ = TZ + 2 * ZOFF;
     static constexpr int SR = BX * BZ;     // shared stride of one r layer
     static constexpr int NBOX = BR * BX * BZ;
     // shared-memory layout after the box: slowness of the tile's nodes, then
@@ -59,10 +65,11 @@ struct Tile {
         const R INF = Lim<R>::inf();
         for (int q = threadIdx.x; q < NBOX; q += NT) {
             const int bz = q % BZ, bx = (q / BZ) % BX, br = q / SR;
-            const int out = (bz < 2 || bz >= TZ + 2) + (bx < 2 || bx >= TX + 2) + (br < 2 || br >= TR + 2);
+            const bool zfar = bz < ZOFF - 2 || bz >= TZ + ZOFF + 2;
+            const int out = (bz < ZOFF || bz >= TZ + ZOFF) + (bx < 2 || bx >= TX + 2) + (br < 2 || br >= TR + 2);
             R v = INF;
-            if (out <= 1) {
-                const int gr = r0 + br - 2, gx = x0 + bx - 2, gz = z0 + bz - 2;
+            if (out <= 1 && !zfar) {
+                const int gr = r0 + br - 2, gx = x0 + bx - 2, gz = z0 + bz - ZOFF;
                 if (gr >= 0 && gr < a.nnr && gx >= 0 && gx < a.nnx && gz >= 0 && gz < a.nnz)
                     v = __ldcg(Te + ((size_t)gr * a.nnx + gx) * a.nnz + gz);
             }
@@ -183,12 +190,64 @@ struct MinBlocks {
 // ---------------------------------------------------------------------------
 // Rounds (fast-iterative cleanup until the fixed point)
 // ---------------------------------------------------------------------------
+
+// TMA (bulk tensor copy) of a tile box: one thread arms the CTA's mbarrier
+// with the box's byte count and issues the copy; every thread then waits for
+// the barrier's phase.  The wait gives up after ~1 s of clock cycles
+// (kTmaWaitCycles) and reports it, so a copy that never completes cannot hang
+// the GPU.
+constexpr long long kTmaWaitCycles = 2000000000LL;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_box(void *dst, const CUtensorMap *map, unsigned long long *bar,
+                                             unsigned bytes, int c0, int c1, int c2, int c3)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(smem_u32(dst)),
+        "l"((unsigned long long)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// true when the barrier completed phase `phase` before the time limit
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, int phase)
+{
+    const long long t0 = clock64();
+    while (true) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(phase)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > kTmaWaitCycles) return false;
+    }
+}
 template <typename R, int TR, int TX, int TZ>
-__global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round)) round_kernel(RoundArgs<R> a)
+__global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
+    round_kernel(const __grid_constant__ RoundArgs<R> a)
 {
     using TL = Tile<R, TR, TX, TZ>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     R *box = reinterpret_cast<R *>(smem_raw);
+    __shared__ __align__(8) unsigned long long s_bar;
+    __shared__ int s_abort;
+    int phase = 0;
     __shared__ int s_face;
     __shared__ int s_w;
     __shared__ unsigned s_chg[2][TX * TZ];        // per column: nodes changed in a pass
@@ -202,6 +261,11 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round)) round
     if (tid == 0) s_upd = 0;
 
     __shared__ int s_dirty_faces;
+    if (tid == 0) {
+        s_abort = 0;
+        if (a.tma) mbar_init(&s_bar);
+    }
+    __syncthreads();
     for (int item = blockIdx.x; item < count; item += gridDim.x) {
         if (tid == 0) {
             const int w = a.cur_list[item];
@@ -221,8 +285,29 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round)) round
         const int tri = t / (f.ntz * f.ntx);
         const int r0 = tri * TR, x0 = txi * TX, z0 = tzi * TZ;
         R *Te = f.T + (size_t)e * N;
-        TL::load(box, Te, f, r0, x0, z0);
-        TL::load_params(box, f, r0, x0, z0);
+        if (a.tma) {
+            // outside the grid the copy fills NaN, which the stencil never
+            // uses: an out-of-grid first neighbour is masked, and a NaN second
+            // neighbour fails t2 < t1 like +inf
+            if (tid == 0)
+                tma_load_box(box, &a.tmap, &s_bar, (unsigned)(TL::NBOX * sizeof(R)), z0 - TL::ZOFF, x0 - 2, r0 - 2, e);
+            TL::load_params(box, f, r0, x0, z0);
+            if (!mbar_wait(&s_bar, phase)) atomicExch(&s_abort, 1);
+            phase ^= 1;
+            __syncthreads();
+            if (s_abort) {
+                // the copy did not arrive: report it, give it one more bounded
+                // wait so that nothing writes into shared memory after exit
+                if (tid == 0) {
+                    atomicExch(a.err, 1);
+                    mbar_wait(&s_bar, phase ^ 1);
+                }
+                return;
+            }
+        } else {
+            TL::load(box, Te, f, r0, x0, z0);
+            TL::load_params(box, f, r0, x0, z0);
+        }
 
         const int gx = x0 + tx, gz = z0 + tz;
         const bool colv = gx < f.nnx && gz < f.nnz;
@@ -242,7 +327,7 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round)) round
         // update never reads its own value, so nothing else can change.
         unsigned chm = 0;
         bool last_changed = false;
-        const int cbase = (2 * TL::BX + (tx + 2)) * TL::BZ + (tz + 2);
+        const int cbase = (2 * TL::BX + (tx + 2)) * TL::BZ + (tz + TL::ZOFF);
         const int df = s_dirty_faces;
         unsigned dirty;
         if (df & kFull) {
@@ -332,6 +417,9 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round)) round
             my_tiles += 1;
             my_staged += (unsigned long long)(vr * vx * vz);
         }
+        // every thread's accesses to the box come before the next copy's
+        // writes (generic proxy, then async proxy)
+        if (a.tma) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
     }
     if (my_upd) atomicAdd(&s_upd, my_upd);
@@ -378,7 +466,7 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::sweep)) sweep
         const bool colv = gx < f.nnx && gz < f.nnz;
         const int xs = sx ? tx : TX - 1 - tx;
         const int zs = sz ? tz : TZ - 1 - tz;
-        const int cbase = (2 * TL::BX + (tx + 2)) * TL::BZ + (tz + 2);
+        const int cbase = (2 * TL::BX + (tx + 2)) * TL::BZ + (tz + TL::ZOFF);
         __syncthreads();
         // pipelined wavefront: layer rp (counted upward from the tile bottom)
         // of column (xs, zs) is updated at step rp + xs + zs

@@ -237,6 +237,29 @@ def test_sweeps_many_azimuths_bitwise(gpu_lib, prec, cfg, scale):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
+def test_tma_staging_bitwise(gpu_lib, prec, monkeypatch):
+    """The rounds stage a tile and its halos by one TMA copy when the phi rows
+    are a multiple of 16 bytes, else by thread loads; both give the same field
+    bit for bit (the copy fills outside the grid with NaN, which the stencil
+    never uses)."""
+    import fm3dt
+    w = _setup(1, 32, nev=3)
+    params = _params(w)
+    out = {}
+    for tma in ("1", "0"):
+        monkeypatch.setenv("FM3DT_TMA", tma)
+        with fm3dt.Solver(w.header, precision=prec, max_events=3) as s:
+            s.set_velocity(w.velv)
+            for shape in range(len(fm3dt.tile_shapes())):
+                s.set_tuning(shape, 16, 0, 1)
+                st = s.solve_planewave(params)
+                assert st["converged"] == 1
+                out[(tma, shape)] = np.concatenate([s.get_times(e) for e in range(3)])
+    for shape in range(len(fm3dt.tile_shapes())):
+        assert np.array_equal(out[("1", shape)], out[("0", shape)]), f"shape {shape}"
+
+
+@pytest.mark.parametrize("prec", [0, 1])
 def test_resume_changes_nothing(gpu_lib, prec):
     """A finished solve is a true fixed point: running the rounds again from
     it, every tile active, changes no bit."""
