@@ -232,11 +232,11 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
     if (((size_t)g.nnz * es) % 16 != 0) return nullptr;
     EncodeTiledFn enc = encode_tiled_fn();
     if (!enc) return nullptr;
-    const TileShape ts = kShapes[shape];
     const cuuint64_t dims[4] = {(cuuint64_t)g.nnz, (cuuint64_t)g.nnx, (cuuint64_t)g.nnr, (cuuint64_t)ctx->maxev};
     const cuuint64_t strides[3] = {(cuuint64_t)g.nnz * es, (cuuint64_t)g.nnz * g.nnx * es,
                                    (cuuint64_t)g.nnz * g.nnx * g.nnr * es};
     // the box of Tile<R, tr, tx, tz>: tz + 8 phi columns, 2-deep halos in theta and r
+    const TileShape ts = kShapes[shape];
     const cuuint32_t box[4] = {(cuuint32_t)(ts.tz + 8), (cuuint32_t)(ts.tx + 4), (cuuint32_t)(ts.tr + 4), 1};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     const CUresult r = enc(&ctx->tmap[shape], es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
@@ -277,6 +277,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     CK(cudaEventCreate(&sw0));
     CK(cudaEventCreate(&sw1));
     CK(cudaEventRecord(ev0, s));
+    CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), s));
     const bool do_sweep = ctx->sweep && mode == kFrames;
 
     if (mode == kFrames) {
@@ -484,7 +485,6 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             a32.tmap = *map;
         }
     }
-    CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), s));
 
     int rounds = 0;
     bool done = false;

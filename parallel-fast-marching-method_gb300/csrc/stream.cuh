@@ -153,7 +153,12 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
                     if (fbits(v) != fbits(old)) {
                         ring[((rp + RING) & (RING - 1)) * LAYER + c] = v;
                         Te[((size_t)gr * f.nnx + gx) * f.nnz + gz] = v;
-                        if (a.flag) stream_mark(a, e, gr, gx, gz);
+                        if (a.flag) {
+                            // the value before its tile's flag, for rounds
+                            // that read it
+                            __threadfence();
+                            stream_mark(a, e, gr, gx, gz);
+                        }
                     }
                 }
             }
