@@ -8,7 +8,7 @@ Tolerances (stated per test):
 * solver, first order: the iterative fixed point equals the fast-marching
   result to 1e-9 s;
 * solver, mixed order: receiver times within 1e-5 relative and 1 ms absolute
-  (the spec bar); field within 5 ms everywhere and within 1e-6 s at 95%
+  (the parity bar of the batched path); field within 5 ms everywhere and within 1e-6 s at 95%
   of nodes (on rough models fast marching keeps a few sticky intermediate
   minima that the fixed point does not: ~2% of nodes of the slab model by up
   to 2.7 ms; smooth models agree to 1e-12 s);
