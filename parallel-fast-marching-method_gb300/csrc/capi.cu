@@ -243,6 +243,13 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
                            ctx->d_T, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NAN_REQUEST_ZERO_FMA);
     if (r != CUDA_SUCCESS) return nullptr;
+    // the slowness [r][theta][phi]: the tile's own nodes, no halo
+    const cuuint32_t sbox[3] = {(cuuint32_t)ts.tz, (cuuint32_t)ts.tx, (cuuint32_t)ts.tr};
+    const CUresult r2 = enc(&ctx->smap[shape], es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                            3, ctx->d_s, dims, strides, sbox, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NAN_REQUEST_ZERO_FMA);
+    if (r2 != CUDA_SUCCESS) return nullptr;
     ctx->tmap_ok[shape] = true;
     return &ctx->tmap[shape];
 }
@@ -481,8 +488,8 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         const CUtensorMap *map = field_tensor_map(ctx, shape);
         a64.tma = a32.tma = map ? 1 : 0;
         if (map) {
-            a64.tmap = *map;
-            a32.tmap = *map;
+            a64.tmap = a32.tmap = *map;
+            a64.smap = a32.smap = ctx->smap[shape];
         }
     }
 

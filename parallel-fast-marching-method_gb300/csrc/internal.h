@@ -69,6 +69,7 @@ struct RoundArgs {
     int tma;
     int *err;
     alignas(64) CUtensorMap tmap;
+    alignas(64) CUtensorMap smap;   // the slowness as a 3-D tensor, the box of a tile's nodes
 };
 
 // Arguments of one sweep launch (one tile hyperplane).
@@ -243,6 +244,7 @@ struct fm3dt_ctx {
     int *d_err = nullptr;         // raised by a kernel whose bounded wait gave up
     bool tmap_ok[fm3dt::kNumShapes] = {};
     CUtensorMap tmap[fm3dt::kNumShapes];
+    CUtensorMap smap[fm3dt::kNumShapes];
     int use_tma = 1;
     Planes planes[fm3dt::kNumSweepShapes];   // tile hyperplanes, then column-block hyperplanes
     size_t flag_capacity = 0;     // tiles allocated for flags/lists

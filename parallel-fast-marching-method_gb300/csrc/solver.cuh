@@ -79,9 +79,10 @@ struct Tile {
 
     // stage the slowness of the tile's nodes and the spacings its rows use
     // (the rounds reuse them over several passes)
-    static __device__ void load_params(R *sm, const FieldArgs<R> &a, int r0, int x0, int z0)
+    static __device__ void load_params(R *sm, const FieldArgs<R> &a, int r0, int x0, int z0,
+                                       bool slowness = true)
     {
-        for (int q = threadIdx.x; q < TR * TX * TZ; q += NT) {
+        for (int q = threadIdx.x; slowness && q < TR * TX * TZ; q += NT) {
             const int lz = q % TZ, lx = (q / TZ) % TX, lr = q / (TZ * TX);
             const int gr = r0 + lr, gx = x0 + lx, gz = z0 + lz;
             sm[OFF_S + q] = (gr < a.nnr && gx < a.nnx && gz < a.nnz)
@@ -209,11 +210,26 @@ __device__ __forceinline__ void mbar_init(unsigned long long *bar)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-__device__ __forceinline__ void tma_load_box(void *dst, const CUtensorMap *map, unsigned long long *bar,
-                                             unsigned bytes, int c0, int c1, int c2, int c3)
+__device__ __forceinline__ void mbar_expect(unsigned long long *bar, unsigned bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, unsigned long long *bar, int c0,
+                                            int c1, int c2)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"((unsigned long long)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// (the caller has armed the barrier with the bytes of every copy of the phase)
+__device__ __forceinline__ void tma_load_box(void *dst, const CUtensorMap *map, unsigned long long *bar,
+                                             int c0, int c1, int c2, int c3)
+{
     asm volatile(
         "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
         "[%6];" ::"r"(smem_u32(dst)),
@@ -289,9 +305,14 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
             // outside the grid the copy fills NaN, which the stencil never
             // uses: an out-of-grid first neighbour is masked, and a NaN second
             // neighbour fails t2 < t1 like +inf
-            if (tid == 0)
-                tma_load_box(box, &a.tmap, &s_bar, (unsigned)(TL::NBOX * sizeof(R)), z0 - TL::ZOFF, x0 - 2, r0 - 2, e);
-            TL::load_params(box, f, r0, x0, z0);
+            // one phase: the box and the tile's slowness (a 3-D copy of its
+            // own nodes, beside the box); the threads load the spacings
+            if (tid == 0) {
+                mbar_expect(&s_bar, (unsigned)((TL::NBOX + TR * TX * TZ) * sizeof(R)));
+                tma_load_box(box, &a.tmap, &s_bar, z0 - TL::ZOFF, x0 - 2, r0 - 2, e);
+                tma_load_3d(box + TL::OFF_S, &a.smap, &s_bar, z0, x0, r0);
+            }
+            TL::load_params(box, f, r0, x0, z0, false);
             if (!mbar_wait(&s_bar, phase)) atomicExch(&s_abort, 1);
             phase ^= 1;
             __syncthreads();
