@@ -199,9 +199,11 @@ int fm3dt_set_sweep_shape(fm3dt_ctx *ctx, int tile_shape);
 
 /* Height segments of the streaming sweep (its work items are column blocks
  * of one segment; more segments give more parallel items per launch and a
- * longer pipeline ramp), for the sweep of every event and for the second,
- * reversed sweep of the events whose lateral direction is a near tie
- * (within ~6 degrees of an axis).  0 = chosen from the batch size. */
+ * longer pipeline ramp), for the sweep of every event and for the two extra
+ * sweeps of the events whose lateral direction is a near tie (within ~6
+ * degrees of an axis).  0 = automatic: chosen from the batch size for the
+ * main sweep, two segments for the extra sweeps (they run beside the other
+ * events' first round). */
 int fm3dt_set_sweep_segments(fm3dt_ctx *ctx, int segments, int tie_segments);
 
 /* Per-round trace of the last solve: tiles processed and node updates of

@@ -382,8 +382,8 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     bool overlap = false;              // ties' extra sweeps beside the others' first round
     if (do_sweep && streaming) {
         // streaming sweep: one launch per column-block hyperplane
-        // the events whose lateral direction is a near tie get a second
-        // sweep with it reversed
+        // the events whose lateral direction is a near tie get two more
+        // sweeps, reversed and then forward
         CK(cudaMemcpyAsync(ctx->h_dir, ctx->d_dir, nev * sizeof(int), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         for (int e = 0; e < nev; ++e)

@@ -12,8 +12,10 @@
 // layers.  Work items (segment, column block) go in hyperplanes of the
 // event's sweep direction (one launch per hyperplane); an item's upwind
 // neighbours are in earlier launches.  Events whose lateral direction is a
-// near tie are swept a second time with that direction reversed.  The sweep
-// is only a good start for the rounds, which reach the same fixed point from
+// near tie are swept twice more, with that direction reversed and then
+// forward again; events still changing on many tiles after a round are swept
+// again (flag mode: changed nodes queue their tiles).  The sweep is only a
+// good start for the rounds, which reach the same fixed point from
 // any start.
 #pragma once
 #include "solver.cuh"
