@@ -191,17 +191,42 @@ int ensure_block_planes(fm3dt_ctx *ctx, int sweep_shape, int nseg, const fm3dt_c
 
 // Height segments for a streaming sweep over nitems events: enough work
 // items per launch to fill the GPU once, each segment at least 16 layers.
-int stream_segments(const fm3dt_ctx *ctx, int nitems, int nbx, int nbz, int sgrid)
+// Height segments for a streaming sweep of nitems events: the count that
+// minimises a model of its time.  Hyperplane h of the items (segment s,
+// column block (x', z')) with s + x' + z' = h is one launch; its items run in
+// ceil(items / sgrid) waves of seg_len + SX + SZ - 2 steps each (the
+// wavefront ramp), plus a few steps' worth of launch gap.  More segments give
+// a launch more items (fewer idle SMs) but more launches and more ramp.
+int stream_segments(const fm3dt_ctx *ctx, int nitems, int nbx, int nbz, int sgrid, int ramp)
 {
-    const double per_plane = (double)nbx * nbz / (double)(nbx + nbz - 1);
-    int nseg = 1;
-    while (nseg * 2 <= std::max(1, ctx->g.nnr / 16) && nitems * per_plane * nseg < (double)sgrid) nseg *= 2;
-    return nseg;
+    const int nnr = ctx->g.nnr;
+    constexpr double kLaunchSteps = 4.0;
+    // blocks per lateral hyperplane (x' + z' = d)
+    std::vector<long long> lat(nbx + nbz - 1, 0);
+    for (int d = 0; d < nbx + nbz - 1; ++d)
+        lat[d] = std::min(d, nbx - 1) - std::max(0, d - (nbz - 1)) + 1;
+    int best = 1;
+    double best_t = 0.0;
+    for (int nseg = 1; nseg <= std::max(1, nnr / 8); nseg *= 2) {
+        const int seg_len = (nnr + nseg - 1) / nseg;
+        double t = 0.0;
+        for (int h = 0; h < nbx + nbz - 1 + nseg - 1; ++h) {
+            long long cnt = 0;
+            for (int sg = 0; sg < nseg; ++sg) {
+                const int d = h - sg;
+                if (d >= 0 && d < nbx + nbz - 1) cnt += lat[d];
+            }
+            const long long items = cnt * (long long)nitems;
+            t += (double)((items + sgrid - 1) / sgrid) * (seg_len + ramp) + kLaunchSteps;
+        }
+        if (nseg == 1 || t < best_t) {
+            best = nseg;
+            best_t = t;
+        }
+    }
+    return best;
 }
 
-// How a solve starts: from boundary frames (initialisation, sweep, rounds),
-// from the current fields (resume: rounds with every tile active), or from
-// point-source boxes the caller already wrote (rounds from the boxes' tiles).
 // The field as a 4-D tensor (phi, theta, r, event) for TMA copies of a round
 // tile's box; null when TMA cannot be used (phi rows not a multiple of 16
 // bytes, the driver entry point missing, or switched off).
@@ -270,6 +295,9 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #define FM_RESWEEP_FRAC 0.01
 #endif
 
+// How a solve starts: from boundary frames (initialisation, sweep, rounds),
+// from the current fields (resume: rounds with every tile active), or from
+// point-source boxes the caller already wrote (rounds from the boxes' tiles).
 enum SolveMode { kFrames = 0, kResume = 1, kPoint = 2 };
 
 int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
@@ -340,7 +368,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     auto stream_pass = [&](int nitems, const int *events, int flip, int nseg, int *flag, int *list,
                            int *count, cudaStream_t st) -> int {
         sweep_nodes += (int64_t)nitems * (int64_t)ctx->N;
-        if (nseg <= 0) nseg = stream_segments(ctx, nitems, nbx, nbz, sgrid);
+        if (nseg <= 0) nseg = stream_segments(ctx, nitems, nbx, nbz, sgrid, kStreamShapes[sidx].sx + kStreamShapes[sidx].sz - 2);
         nseg = std::min(nseg, g.nnr);
         const fm3dt_ctx::Planes *PP = nullptr;
         int rc = ensure_block_planes(ctx, ctx->sweep_shape, nseg, &PP);
