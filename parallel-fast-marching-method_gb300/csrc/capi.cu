@@ -285,6 +285,9 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #ifndef FM_ROUND0_PER_TILE
 #define FM_ROUND0_PER_TILE 1
 #endif
+#ifndef FM_OVERLAP_MIN_EVENTS
+#define FM_OVERLAP_MIN_EVENTS 32
+#endif
 #ifndef FM_OVERLAP_TIES
 #define FM_OVERLAP_TIES 1
 #endif
@@ -416,7 +419,11 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         CK(cudaStreamSynchronize(s));
         for (int e = 0; e < nev; ++e)
             (ctx->h_dir[e] & 12 ? ties : others).push_back(e);
-        overlap = FM_OVERLAP_TIES && !ctx->verify && !ties.empty() && !others.empty() && FM_TIE_SWEEPS > 0;
+        // (only for large batches: with a few events the first round is short,
+        // and contexts that solve side by side, as a service runs them, lose
+        // more to the priority stream than they gain)
+        overlap = FM_OVERLAP_TIES && !ctx->verify && !ties.empty() && (int)others.size() >= FM_OVERLAP_MIN_EVENTS &&
+                  FM_TIE_SWEEPS > 0;
         if (!ties.empty())
             CK(cudaMemcpyAsync(ctx->d_events, ties.data(), ties.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         // pass 0 sweeps every event from the boundary, pass 1 the near-tie
