@@ -279,6 +279,13 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
     return &ctx->tmap[shape];
 }
 
+// Solve schedule (compile-time tuning; the measured best on this GPU):
+//   FM_TIE_SWEEPS          extra sweeps of near-tie events (reversed, forward, ...)
+//   FM_ROUND0_PER_TILE     first round with one CTA per tile when its tile count is known
+//   FM_OVERLAP_TIES        near-tie sweeps beside the other events' first round ...
+//   FM_OVERLAP_MIN_EVENTS  ... when at least this many other events are in the batch
+//   FM_RESWEEPS            re-sweeps after the first rounds, at most
+//   FM_RESWEEP_FRAC        ... of events with more than this fraction of tiles queued
 #ifndef FM_TIE_SWEEPS
 #define FM_TIE_SWEEPS 2
 #endif
