@@ -144,14 +144,14 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
         w[d] = o2 ? sp.w[a] * R(2.25) : sp.w[a];
     }
     R best = INF;
-#pragma unroll
-    for (int o = 0; o < 8; ++o) {
-        const int dr = (o >> 2) & 1, dx = 2 + ((o >> 1) & 1), dz = 4 + (o & 1);
-        if (!(((inb >> dr) & (inb >> dx) & (inb >> dz)) & 1u)) continue;
-        R k0 = key[dr], e0 = e[dr], g0 = g[dr], w0 = w[dr];
-        R k1 = key[dx], e1 = e[dx], g1 = g[dx], w1 = w[dx];
-        R k2 = key[dz], e2 = e[dz], g2 = g[dz], w2 = w[dz];
-        // conditional swaps as selects (a branch around four moves costs more)
+    // Each octant sorts its three terms by key, stably (ties keep the order
+    // r, theta, phi).  The lateral pair is sorted once and shared by the two
+    // octants that differ only in the radial direction, and the radial term
+    // is then inserted in front: two compare-and-swaps per octant instead of
+    // three, and the same order as a full three-term network (a stable sort's
+    // result is unique).  The minimum over octants does not depend on the
+    // order they are visited in.
+    // conditional swaps as selects (a branch around four moves costs more)
 #define FM_CSWAP(i, j)                                                        \
     {                                                                         \
         const bool p_ = k##j < k##i;                                          \
@@ -161,30 +161,43 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
         q_ = p_ ? g##j : g##i; g##j = p_ ? g##i : g##j; g##i = q_;            \
         q_ = p_ ? w##j : w##i; w##j = p_ ? w##i : w##j; w##i = q_;            \
     }
-        FM_CSWAP(0, 1)
-        FM_CSWAP(1, 2)
-        FM_CSWAP(0, 1)
-#undef FM_CSWAP
-        if (!(k0 < INF)) continue;
-        R x = fm_fma<R>(s, g0, e0);
-        if (k1 < x) {
-            R a = w0 + w1;
-            const R we0 = w0 * e0, we1 = w1 * e1;
-            R b = we0 + we1;
-            R c = fm_fma<R>(we0, e0, fm_fma<R>(we1, e1, -s2));
-            R disc = fm_fma<R>(b, b, -(a * c));
-            x = Fast<R>::div(b + Fast<R>::sqrt(disc > R(0) ? disc : R(0)), a);
-            if (k2 < x) {
-                const R we2 = w2 * e2;
-                a += w2;
-                b += we2;
-                c = fm_fma<R>(we2, e2, c);
-                disc = fm_fma<R>(b, b, -(a * c));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int dx = 2 + ((q >> 1) & 1), dz = 4 + (q & 1);
+        if (!(((inb >> dx) & (inb >> dz)) & 1u)) continue;
+        R ka = key[dx], ea = e[dx], ga = g[dx], wa = w[dx];
+        R kb = key[dz], eb = e[dz], gb = g[dz], wb = w[dz];
+        FM_CSWAP(a, b)
+#pragma unroll
+        for (int dr = 0; dr < 2; ++dr) {
+            if (!((inb >> dr) & 1u)) continue;
+            R k0 = key[dr], e0 = e[dr], g0 = g[dr], w0 = w[dr];
+            R k1 = ka, e1 = ea, g1 = ga, w1 = wa;
+            R k2 = kb, e2 = eb, g2 = gb, w2 = wb;
+            FM_CSWAP(0, 1)
+            FM_CSWAP(1, 2)
+            if (!(k0 < INF)) continue;
+            R x = fm_fma<R>(s, g0, e0);
+            if (k1 < x) {
+                R a = w0 + w1;
+                const R we0 = w0 * e0, we1 = w1 * e1;
+                R b = we0 + we1;
+                R c = fm_fma<R>(we0, e0, fm_fma<R>(we1, e1, -s2));
+                R disc = fm_fma<R>(b, b, -(a * c));
                 x = Fast<R>::div(b + Fast<R>::sqrt(disc > R(0) ? disc : R(0)), a);
+                if (k2 < x) {
+                    const R we2 = w2 * e2;
+                    a += w2;
+                    b += we2;
+                    c = fm_fma<R>(we2, e2, c);
+                    disc = fm_fma<R>(b, b, -(a * c));
+                    x = Fast<R>::div(b + Fast<R>::sqrt(disc > R(0) ? disc : R(0)), a);
+                }
             }
+            best = fm_min(best, x);
         }
-        best = fm_min(best, x);
     }
+#undef FM_CSWAP
     return tmin + best;
 }
 
