@@ -62,7 +62,24 @@ template <> FM_HD float fm_sqrt<float>(float x) {
 #endif
 }
 
-template <typename R> FM_HD R fm_min(R a, R b) { return b < a ? b : a; }
+// Minimum and maximum as the hardware min/max instructions.  They differ from
+// a compare-and-select only for NaN and for a +0/-0 pair; in-grid times are
+// never NaN and never -0 (offsets from an event's earliest time start at +0,
+// and sums of non-negative terms stay +0 or above), so the results are the
+// same bits.
+template <typename R> FM_HD R fm_min(R a, R b);
+template <typename R> FM_HD R fm_max(R a, R b);
+#ifdef __CUDA_ARCH__
+template <> FM_HD float fm_min<float>(float a, float b) { return fminf(a, b); }
+template <> FM_HD double fm_min<double>(double a, double b) { return fmin(a, b); }
+template <> FM_HD float fm_max<float>(float a, float b) { return fmaxf(a, b); }
+template <> FM_HD double fm_max<double>(double a, double b) { return fmax(a, b); }
+#else
+template <> FM_HD float fm_min<float>(float a, float b) { return __builtin_fminf(a, b); }
+template <> FM_HD double fm_min<double>(double a, double b) { return __builtin_fmin(a, b); }
+template <> FM_HD float fm_max<float>(float a, float b) { return __builtin_fmaxf(a, b); }
+template <> FM_HD double fm_max<double>(double a, double b) { return __builtin_fmax(a, b); }
+#endif
 
 // Explicit fused multiply-add.  The solver is compiled without automatic
 // contraction, so every kernel instantiation (and the host) evaluates the
@@ -176,7 +193,8 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
             R k2 = kb, e2 = eb, g2 = gb, w2 = wb;
             FM_CSWAP(0, 1)
             FM_CSWAP(1, 2)
-            if (!(k0 < INF)) continue;
+            // (an octant with no neighbour set has e0 = +inf: x = +inf
+            // leaves best as it is, and no further term passes k < x)
             R x = fm_fma<R>(s, g0, e0);
             if (k1 < x) {
                 R a = w0 + w1;
@@ -184,14 +202,14 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
                 R b = we0 + we1;
                 R c = fm_fma<R>(we0, e0, fm_fma<R>(we1, e1, -s2));
                 R disc = fm_fma<R>(b, b, -(a * c));
-                x = Fast<R>::div(b + Fast<R>::sqrt(disc > R(0) ? disc : R(0)), a);
+                x = Fast<R>::div(b + Fast<R>::sqrt(fm_max<R>(disc, R(0))), a);
                 if (k2 < x) {
                     const R we2 = w2 * e2;
                     a += w2;
                     b += we2;
                     c = fm_fma<R>(we2, e2, c);
                     disc = fm_fma<R>(b, b, -(a * c));
-                    x = Fast<R>::div(b + Fast<R>::sqrt(disc > R(0) ? disc : R(0)), a);
+                    x = Fast<R>::div(b + Fast<R>::sqrt(fm_max<R>(disc, R(0))), a);
                 }
             }
             best = fm_min(best, x);
