@@ -81,6 +81,24 @@ template <> FM_HD float fm_max<float>(float a, float b) { return __builtin_fmaxf
 template <> FM_HD double fm_max<double>(double a, double b) { return __builtin_fmax(a, b); }
 #endif
 
+// The two keys of a conditional swap, in order (p: the second is smaller).
+// Single precision takes min and max, which do not wait for the comparison;
+// double precision keeps the selects, which run on the integer pipe rather
+// than the narrow double-precision one.
+template <typename R> FM_HD void fm_order_keys(bool p, R &ki, R &kj);
+template <> FM_HD void fm_order_keys<float>(bool, float &ki, float &kj)
+{
+    const float lo = fm_min<float>(ki, kj);
+    kj = fm_max<float>(ki, kj);
+    ki = lo;
+}
+template <> FM_HD void fm_order_keys<double>(bool p, double &ki, double &kj)
+{
+    const double lo = p ? kj : ki;
+    kj = p ? ki : kj;
+    ki = lo;
+}
+
 // Explicit fused multiply-add.  The solver is compiled without automatic
 // contraction, so every kernel instantiation (and the host) evaluates the
 // stencil with exactly the same roundings; otherwise the compiler may fuse
@@ -155,7 +173,9 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
         const int a = d >> 1;
         const bool o2 = order2 && (t2[d] < t1[d]);
         const R dt = t1[d] - tmin;
-        key[d] = ((inb >> d) & 1u) ? dt : INF;
+        // (an octant is evaluated only when its three neighbours are in the
+        // grid, so an outside direction's key is never read)
+        key[d] = dt;
         e[d] = o2 ? fm_fma<R>(t1[d] - t2[d], R(1.0 / 3.0), dt) : dt;
         g[d] = o2 ? sp.h[a] * R(2.0 / 3.0) : sp.h[a];
         w[d] = o2 ? sp.w[a] * R(2.25) : sp.w[a];
@@ -172,9 +192,8 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
 #define FM_CSWAP(i, j)                                                        \
     {                                                                         \
         const bool p_ = k##j < k##i;                                          \
-        R q_;                                                                 \
-        q_ = p_ ? k##j : k##i; k##j = p_ ? k##i : k##j; k##i = q_;            \
-        q_ = p_ ? e##j : e##i; e##j = p_ ? e##i : e##j; e##i = q_;            \
+        fm_order_keys<R>(p_, k##i, k##j);                                     \
+        R q_ = p_ ? e##j : e##i; e##j = p_ ? e##i : e##j; e##i = q_;          \
         q_ = p_ ? g##j : g##i; g##j = p_ ? g##i : g##j; g##i = q_;            \
         q_ = p_ ? w##j : w##i; w##j = p_ ? w##i : w##j; w##i = q_;            \
     }
