@@ -200,13 +200,16 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int dx = 2 + ((q >> 1) & 1), dz = 4 + (q & 1);
-        if (!(((inb >> dx) & (inb >> dz)) & 1u)) continue;
         R ka = key[dx], ea = e[dx], ga = g[dx], wa = w[dx];
         R kb = key[dz], eb = e[dz], gb = g[dz], wb = w[dz];
         FM_CSWAP(a, b)
 #pragma unroll
         for (int dr = 0; dr < 2; ++dr) {
-            if (!((inb >> dr) & 1u)) continue;
+            // an octant with a neighbour outside the grid is evaluated all
+            // the same (from whatever its keys hold) and then left out of
+            // the minimum: no branch around it
+            const unsigned om = (1u << dr) | (1u << dx) | (1u << dz);
+            const bool inside = (inb & om) == om;
             R k0 = key[dr], e0 = e[dr], g0 = g[dr], w0 = w[dr];
             R k1 = ka, e1 = ea, g1 = ga, w1 = wa;
             R k2 = kb, e2 = eb, g2 = gb, w2 = wb;
@@ -231,7 +234,7 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
                     x = Fast<R>::div(b + Fast<R>::sqrt(fm_max<R>(disc, R(0))), a);
                 }
             }
-            best = fm_min(best, x);
+            best = inside ? fm_min(best, x) : best;
         }
     }
 #undef FM_CSWAP
