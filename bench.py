@@ -163,7 +163,7 @@ def measured_peak_hbm():
 # of the same kernels (96^3, 64 events): the first round's launch (every tile
 # staged) and one mid-sweep launch; the bench scales it to its own launches
 # by the nodes they process.
-KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.17, "stream_sweep_kernel": 31.8}
+KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.15, "stream_sweep_kernel": 31.8}
 
 # Warp instructions per node of the same kernels, from ncu's
 # smsp__inst_executed.sum summed over every launch of three solves of that
@@ -171,7 +171,7 @@ KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.17, "stream_sweep_kernel": 31.8}
 # the rounds (first round and tail rounds together).  The kernels are bound
 # by instruction issue, so the bench also reports the issue rate they reach
 # against the SMs' peak of four warp instructions per cycle.
-KERNEL_WARP_INST_PER_NODE = {"round_kernel": 26.18, "stream_sweep_kernel": 33.15}
+KERNEL_WARP_INST_PER_NODE = {"round_kernel": 25.28, "stream_sweep_kernel": 32.47}
 
 
 def _oracle_event(args):
