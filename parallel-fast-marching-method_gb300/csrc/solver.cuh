@@ -368,12 +368,12 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
             unsigned pch = 0;
             // r changes only shared-memory offsets and mask bits: no unrolling
             const int k0 = (p & 1) ? 0 : TR - 1, dk = (p & 1) ? 1 : -1;
+            my_upd += __popc(dirty);
 #pragma unroll 1
             for (int i = 0, k = k0; i < TR; ++i, k += dk) {
                 if (!((dirty >> k) & 1u)) continue;
                 const int c = cbase + k * TL::SR;
                 const R nv = TL::update(box, c, f, k, tx, tz, r0 + k, gx, gz);
-                ++my_upd;
                 if (fbits(nv) != fbits(box[c])) {
                     box[c] = nv;
                     pch |= 1u << k;

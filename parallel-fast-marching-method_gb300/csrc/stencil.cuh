@@ -145,8 +145,9 @@ template <typename R> struct Spacing {
 // Neighbour directions: 0 = r-1 (up), 1 = r+1 (down), 2 = x-1, 3 = x+1,
 // 4 = z-1, 5 = z+1.
 //
-// t1[d]: neighbour value (+inf if unset; ignored when bit d of inb is clear)
-// t2[d]: second neighbour value (+inf if unset or outside the grid)
+// t1[d]: neighbour value (+inf if unset; +inf or NaN when bit d of inb is
+//        clear, i.e. outside the grid)
+// t2[d]: second neighbour value (+inf if unset; +inf or NaN outside the grid)
 // sp:    spacings at the centre node
 // s:     slowness at the centre node
 // order2: 1 for the mixed-order scheme (fom=1), 0 for first order (fom=0)
@@ -161,10 +162,11 @@ template <typename R>
 FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing<R> &sp, int order2)
 {
     const R INF = Lim<R>::inf();
+    // (a neighbour outside the grid holds +inf or NaN, which the hardware
+    // minimum passes over: no mask needed)
     R tmin = INF;
 #pragma unroll
-    for (int d = 0; d < 6; ++d)
-        if ((inb >> d) & 1u) tmin = fm_min(tmin, t1[d]);
+    for (int d = 0; d < 6; ++d) tmin = fm_min(tmin, t1[d]);
     if (!(tmin < INF)) return INF;
     const R s2 = s * s;
     R key[6], e[6], g[6], w[6];
