@@ -188,7 +188,11 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
     // octants that differ only in the radial direction, and the radial term
     // is then inserted in front: two compare-and-swaps per octant instead of
     // three, and the same order as a full three-term network (a stable sort's
-    // result is unique).  The minimum over octants does not depend on the
+    // result is unique).  Both octants of a pair are sorted before either
+    // solves, so that their sorts form one straight run of code.  An octant
+    // with a neighbour outside the grid is evaluated all the same (from
+    // whatever its keys hold) and left out of the minimum by a select rather
+    // than branched around.  The minimum over octants does not depend on the
     // order they are visited in.
     // conditional swaps as selects (a branch around four moves costs more)
 #define FM_CSWAP(i, j)                                                        \
@@ -199,45 +203,53 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
         q_ = p_ ? g##j : g##i; g##j = p_ ? g##i : g##j; g##i = q_;            \
         q_ = p_ ? w##j : w##i; w##j = p_ ? w##i : w##j; w##i = q_;            \
     }
+    // the causal two- and three-term solves of a sorted octant, from its
+    // one-term solution x
+    auto solve = [&](R k1, R k2, R e0, R e1, R e2, R w0, R w1, R w2, R x) -> R {
+        if (k1 < x) {
+            R a = w0 + w1;
+            const R we0 = w0 * e0, we1 = w1 * e1;
+            R b = we0 + we1;
+            R c = fm_fma<R>(we0, e0, fm_fma<R>(we1, e1, -s2));
+            R disc = fm_fma<R>(b, b, -(a * c));
+            x = Fast<R>::div(b + Fast<R>::sqrt(fm_max<R>(disc, R(0))), a);
+            if (k2 < x) {
+                const R we2 = w2 * e2;
+                a += w2;
+                b += we2;
+                c = fm_fma<R>(we2, e2, c);
+                disc = fm_fma<R>(b, b, -(a * c));
+                x = Fast<R>::div(b + Fast<R>::sqrt(fm_max<R>(disc, R(0))), a);
+            }
+        }
+        return x;
+    };
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int dx = 2 + ((q >> 1) & 1), dz = 4 + (q & 1);
         R ka = key[dx], ea = e[dx], ga = g[dx], wa = w[dx];
         R kb = key[dz], eb = e[dz], gb = g[dz], wb = w[dz];
         FM_CSWAP(a, b)
-#pragma unroll
-        for (int dr = 0; dr < 2; ++dr) {
-            // an octant with a neighbour outside the grid is evaluated all
-            // the same (from whatever its keys hold) and then left out of
-            // the minimum: no branch around it
-            const unsigned om = (1u << dr) | (1u << dx) | (1u << dz);
-            const bool inside = (inb & om) == om;
-            R k0 = key[dr], e0 = e[dr], g0 = g[dr], w0 = w[dr];
-            R k1 = ka, e1 = ea, g1 = ga, w1 = wa;
-            R k2 = kb, e2 = eb, g2 = gb, w2 = wb;
-            FM_CSWAP(0, 1)
-            FM_CSWAP(1, 2)
-            // (an octant with no neighbour set has e0 = +inf: x = +inf
-            // leaves best as it is, and no further term passes k < x)
-            R x = fm_fma<R>(s, g0, e0);
-            if (k1 < x) {
-                R a = w0 + w1;
-                const R we0 = w0 * e0, we1 = w1 * e1;
-                R b = we0 + we1;
-                R c = fm_fma<R>(we0, e0, fm_fma<R>(we1, e1, -s2));
-                R disc = fm_fma<R>(b, b, -(a * c));
-                x = Fast<R>::div(b + Fast<R>::sqrt(fm_max<R>(disc, R(0))), a);
-                if (k2 < x) {
-                    const R we2 = w2 * e2;
-                    a += w2;
-                    b += we2;
-                    c = fm_fma<R>(we2, e2, c);
-                    disc = fm_fma<R>(b, b, -(a * c));
-                    x = Fast<R>::div(b + Fast<R>::sqrt(fm_max<R>(disc, R(0))), a);
-                }
-            }
-            best = inside ? fm_min(best, x) : best;
-        }
+        // terms 0-2: the octant with the upper (r-1) neighbour; 3-5: the
+        // lower (r+1) one; om*: the neighbours each needs inside the grid
+        const unsigned omu = 1u | (1u << dx) | (1u << dz), omd = 2u | (1u << dx) | (1u << dz);
+        R k0 = key[0], e0 = e[0], g0 = g[0], w0 = w[0];
+        R k1 = ka, e1 = ea, g1 = ga, w1 = wa;
+        R k2 = kb, e2 = eb, g2 = gb, w2 = wb;
+        R k3 = key[1], e3 = e[1], g3 = g[1], w3 = w[1];
+        R k4 = ka, e4 = ea, g4 = ga, w4 = wa;
+        R k5 = kb, e5 = eb, g5 = gb, w5 = wb;
+        FM_CSWAP(0, 1)
+        FM_CSWAP(3, 4)
+        FM_CSWAP(1, 2)
+        FM_CSWAP(4, 5)
+        // (an octant with no neighbour set has e0 = +inf: its x = +inf leaves
+        // best as it is, and no further term passes k < x)
+        const R xu = fm_fma<R>(s, g0, e0), xd = fm_fma<R>(s, g3, e3);
+        const R vu = solve(k1, k2, e0, e1, e2, w0, w1, w2, xu);
+        best = (inb & omu) == omu ? fm_min(best, vu) : best;
+        const R vd = solve(k4, k5, e3, e4, e5, w3, w4, w5, xd);
+        best = (inb & omd) == omd ? fm_min(best, vd) : best;
     }
 #undef FM_CSWAP
     return tmin + best;
