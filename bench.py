@@ -314,29 +314,43 @@ def run_ours(a):
     lat = sorted(s["ms"] for s in sts)
     p50 = lat[len(lat) // 2]
     p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
-    # the two solver kernels: rounds (tile activations) and the directional
-    # sweep (every node staged once); the roofline line reports the one with
-    # the larger share of device time
+    # The two solver kernels: the rounds (nodes of staged tiles) and the
+    # directional sweep.  The solver's sweep interval (start of the sweep to
+    # the end of the other events' main sweep) holds only sweep launches:
+    # every event's main sweep, on the context stream and, for the near-tie
+    # events, beside it on the second stream.  The rounds' interval also holds
+    # the near-tie events' extra sweeps, which run beside the first round, so
+    # no interval times the round kernel alone.  The roofline line reports
+    # the kernel with more work (warp instructions per node from the ncu count
+    # x nodes; device time when there is no count) and, for the sweep, the
+    # main sweeps' nodes over the sweep interval: a lower bound, since the
+    # near-tie events' extra sweeps start in that interval too.
     round_ms = sum(s["round_ms"] for s in sts)
     round_launches = sum(s["round_launches"] for s in sts)
     staged = sum(s["tile_nodes"] for s in sts)
     sweep_ms = sum(s["sweep_ms"] for s in sts)
     sweep_launches = sum(s["sweep_launches"] for s in sts)
     sweep_nodes = sum(s["sweep_nodes"] for s in sts)
+    main_nodes = nev * nnr * nnx * nnz * a.steps if a.sweep_mode == 1 else sweep_nodes
     sweep_name = "stream_sweep_kernel" if sweep_shape_dims[0] == "stream" else "sweep_kernel"
+    # name: (interval ms, nodes in it, launches, nodes of all launches)
     kernels = {
-        "round_kernel": (round_ms, round_launches, staged * B_NODE[a.prec], staged),
-        sweep_name: (sweep_ms, sweep_launches, sweep_nodes * B_NODE[a.prec], sweep_nodes),
+        "round_kernel": (round_ms, staged, round_launches, staged),
+        sweep_name: (sweep_ms, main_nodes, sweep_launches, sweep_nodes),
     }
-    top = max(kernels, key=lambda k: kernels[k][0])
-    k_ms, k_launches, alg_bytes, k_nodes = kernels[top]
-    achieved = alg_bytes / (k_ms / 1000.0) / 1e9 if k_ms > 0 else 0.0
+    if a.prec == "f32" and all(k in KERNEL_WARP_INST_PER_NODE for k in kernels):
+        work = {k: KERNEL_WARP_INST_PER_NODE[k] * v[3] for k, v in kernels.items()}
+    else:
+        work = {k: v[0] for k, v in kernels.items()}
+    top = max(kernels, key=lambda k: work[k])
+    k_ms, k_nodes, k_launches, all_nodes = kernels[top]
+    achieved = k_nodes * B_NODE[a.prec] / (k_ms / 1000.0) / 1e9 if k_ms > 0 else 0.0
     peak, peak_kind = measured_peak_hbm()
-    per_launch = alg_bytes / max(1, k_launches)
+    per_launch = all_nodes * B_NODE[a.prec] / max(1, k_launches)
     # DRAM bytes per node processed, from the ncu capture of the small case
     # (profiles/solver_kernels_small_case.md), times the nodes one launch
     # processes here on average
-    traffic = (KERNEL_DRAM_BYTES_PER_NODE[top] * k_nodes / max(1, k_launches)
+    traffic = (KERNEL_DRAM_BYTES_PER_NODE[top] * all_nodes / max(1, k_launches)
                if top in KERNEL_DRAM_BYTES_PER_NODE and a.prec == "f32" else None)
 
     issue = None
@@ -407,7 +421,8 @@ def run_ours(a):
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": top, "peak_source": peak_kind,
                      "alg_bytes_per_launch": per_launch,
-                     "avg_launch_ms": k_ms / max(1, k_launches), "issue": issue},
+                     "avg_launch_ms": per_launch / (achieved * 1e6) if achieved > 0 else None,
+                     "interval_ms": k_ms, "interval_nodes": k_nodes, "issue": issue},
         "solver": {"rounds_per_solve": round_launches / a.steps,
                    "tile_activations": sum(s["tile_updates"] for s in sts) / a.steps,
                    "node_passes_per_solve": sum(s["node_passes"] for s in sts) / a.steps,
@@ -415,7 +430,7 @@ def run_ours(a):
                    "round_ms_per_step": round_ms / a.steps, "sweep_ms_per_step": sweep_ms / a.steps,
                    "sweep_launches_per_step": sweep_launches / a.steps,
                    "sweep_nodes_per_solve": sweep_nodes / a.steps,
-                   "kernel_shares": {k: v[0] / max(1e-9, dev_ms) for k, v in kernels.items()},
+                   "work_shares": {k: v / max(1e-9, sum(work.values())) for k, v in work.items()},
                    "round_trace_tiles": trace_tiles, "round_trace_updates": trace_updates,
                    "round_trace_ms": trace_ms},
     }

@@ -284,6 +284,10 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 //   FM_ROUND0_PER_TILE     first round with one CTA per tile when its tile count is known
 //   FM_OVERLAP_TIES        near-tie sweeps beside the other events' first round ...
 //   FM_OVERLAP_MIN_EVENTS  ... when at least this many other events are in the batch
+//   FM_CERTIFY             the other events' first round only where the certification
+//                          of their single sweep fails
+//   FM_OVERLAP_MAIN        the near-tie events' main sweep on stream2 too, ahead of
+//                          their extra sweeps, beside the other events' main sweep
 //   FM_RESWEEPS            re-sweeps after the first rounds, at most
 //   FM_RESWEEP_FRAC        ... of events with more than this fraction of tiles queued
 #ifndef FM_TIE_SWEEPS
@@ -297,6 +301,12 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #endif
 #ifndef FM_OVERLAP_TIES
 #define FM_OVERLAP_TIES 1
+#endif
+#ifndef FM_CERTIFY
+#define FM_CERTIFY 1
+#endif
+#ifndef FM_OVERLAP_MAIN
+#define FM_OVERLAP_MAIN 1
 #endif
 #ifndef FM_RESWEEPS
 #define FM_RESWEEPS 4
@@ -448,7 +458,9 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         plan.push_back({2, 0});
         for (const PassPlan &pl : plan) {
             const int pass = pl.pass;
-            if ((pass == 1 && (ties.empty() || overlap)) || (pass == 2 && !ctx->verify)) continue;
+            if ((pass == 0 && overlap && FM_OVERLAP_MAIN) || (pass == 1 && (ties.empty() || overlap)) ||
+                (pass == 2 && !ctx->verify))
+                continue;
             const int nitems = pass == 1 ? (int)ties.size() : nev;
             const int rc = stream_pass(nitems, pass == 1 ? ctx->d_events : nullptr, pl.flip,
                                        pass == 1 ? ctx->tie_segments : ctx->sweep_segments,
@@ -490,7 +502,9 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         ctx->launches += sweep_launches;
         CKL();
     }
-    CK(cudaEventRecord(sw1, s));
+    // (with the main sweeps in the first round's two parts, the sweep time ends
+    // with the other events' main sweep there)
+    if (!(overlap && FM_OVERLAP_MAIN)) CK(cudaEventRecord(sw1, s));
 
     // 2. rounds until no tile changes: all tiles after a sweep, else the
     //    tiles whose nodes or 2-deep halos include the bottom layer
@@ -526,6 +540,8 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     a64.max_passes = a32.max_passes = ctx->max_passes;
     a64.stats = a32.stats = ctx->d_stats;
     a64.err = a32.err = ctx->d_err;
+    a64.cert = a32.cert = ctx->d_cert;
+    a64.cert_nw = a32.cert_nw = ctx->cert_nw;
     {
         const CUtensorMap *map = field_tensor_map(ctx, shape);
         a64.tma = a32.tma = map ? 1 : 0;
@@ -611,28 +627,63 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         CK(cudaEventCreate(&r1));
         CK(cudaMemcpyAsync(ctx->d_events, ties.data(), ties.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->d_events_b, others.data(), others.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-        CK(cudaEventRecord(r0, s));
+        if (!FM_OVERLAP_MAIN) CK(cudaEventRecord(r0, s));
         CK(cudaEventRecord(fork, s));
         cudaStream_t s2 = ctx->stream2;
         CK(cudaStreamWaitEvent(s2, fork, 0));
+        if (FM_OVERLAP_MAIN) {
+            // each part's main sweep: the near-tie events' on stream2 ahead of
+            // their extra sweeps, the others' on the context stream
+            int rc = stream_pass((int)ties.size(), ctx->d_events, 0, ctx->tie_segments, nullptr, ctx->d_list[0],
+                                 ctx->d_count[0], s2);
+            if (rc) return rc;
+            rc = stream_pass((int)others.size(), ctx->d_events_b, 0, ctx->sweep_segments, nullptr, ctx->d_list[0],
+                             ctx->d_count[0], s);
+            if (rc) return rc;
+            CK(cudaEventRecord(sw1, s));
+            CK(cudaEventRecord(r0, s));
+        }
         for (int k = 0; k < FM_TIE_SWEEPS; ++k) {
-            // beside the first round the extra sweeps need no parallelism of
-            // their own: two height segments (less pipeline ramp than the
-            // automatic choice for a few dozen events)
+            // (height segments by the time model for the near-tie events alone:
+            // their sweeps are the longer chain of the two parts)
             const int rc = stream_pass((int)ties.size(), ctx->d_events, (k & 1) ? 0 : 4,
-                                       ctx->tie_segments > 0 ? ctx->tie_segments : 2, nullptr, ctx->d_list[0],
-                                       ctx->d_count[0], s2);
+                                       FM_OVERLAP_MAIN ? ctx->tie_segments : (ctx->tie_segments > 0 ? ctx->tie_segments : 2),
+                                       nullptr, ctx->d_list[0], ctx->d_count[0], s2);
             if (rc) return rc;
         }
         launch_initial_tiles((int)ties.size(), ctx->d_events, tpe, first, cnt, ctx->d_list_b, ctx->d_count_b,
                              ctx->d_flag, s2);
         launch_round(0, ctx->d_list_b, ctx->d_count_b, ctx->d_list[1], ctx->d_count[1], s2);
         CK(cudaEventRecord(join, s2));
-        launch_initial_tiles((int)others.size(), ctx->d_events_b, tpe, first, cnt, ctx->d_list[0], ctx->d_count[0],
-                             ctx->d_flag, s);
-        grid_override = (int)std::min<long long>((long long)others.size() * cnt, 1LL << 30);
-        launch_round(0, ctx->d_list[0], ctx->d_count[0], ctx->d_list[1], ctx->d_count[1], s);
-        grid_override = 0;
+        if (FM_CERTIFY) {
+            // the other events were swept once: only the tiles holding a node
+            // the certification cannot clear, from those nodes
+            CK(cudaMemsetAsync(ctx->d_count[0], 0, sizeof(int), s));
+            auto certify = [&](auto &ca, const auto &f) {
+                ca.f = f;
+                ca.events = ctx->d_events_b; ca.nev = (int)others.size();
+                ca.dir = ctx->d_dir;
+                ca.cert = ctx->d_cert; ca.cert_nw = ctx->cert_nw;
+                ca.tr = ts.tr; ca.tx = ts.tx; ca.tz = ts.tz;
+                ca.flag = ctx->d_flag; ca.list = ctx->d_list[0]; ca.count = ctx->d_count[0];
+            };
+            if (ctx->prec == FM3DT_FP64) {
+                CertifyArgs<double> ca{};
+                certify(ca, f64);
+                launch_certify_f64(ca, s);
+            } else {
+                CertifyArgs<float> ca{};
+                certify(ca, f32);
+                launch_certify_f32(ca, s);
+            }
+            launch_round(0, ctx->d_list[0], ctx->d_count[0], ctx->d_list[1], ctx->d_count[1], s);
+        } else {
+            launch_initial_tiles((int)others.size(), ctx->d_events_b, tpe, first, cnt, ctx->d_list[0],
+                                 ctx->d_count[0], ctx->d_flag, s);
+            grid_override = (int)std::min<long long>((long long)others.size() * cnt, 1LL << 30);
+            launch_round(0, ctx->d_list[0], ctx->d_count[0], ctx->d_list[1], ctx->d_count[1], s);
+            grid_override = 0;
+        }
         CK(cudaStreamWaitEvent(s, join, 0));
         CK(cudaEventRecord(r1, s));
         ctx->launches += 2;
@@ -818,6 +869,8 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMalloc(&ctx->d_base, ctx->maxev * sizeof(double)));
     CKC(cudaMalloc(&ctx->d_frozen, ctx->NB * ctx->maxev));
     CKC(cudaMalloc(&ctx->d_flag, ctx->flag_capacity * sizeof(int)));
+    ctx->cert_nw = (d.nnr + 31) / 32;
+    CKC(cudaMalloc(&ctx->d_cert, (size_t)ctx->maxev * d.nnx * d.nnz * ctx->cert_nw * sizeof(unsigned)));
     CKC(cudaMalloc(&ctx->d_list[0], ctx->flag_capacity * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_list[1], ctx->flag_capacity * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_count[0], sizeof(int)));
@@ -1337,6 +1390,7 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_base);
     cudaFree(ctx->d_frozen);
     cudaFree(ctx->d_flag);
+    cudaFree(ctx->d_cert);
     cudaFree(ctx->d_list[0]);
     cudaFree(ctx->d_list[1]);
     cudaFree(ctx->d_count[0]);

@@ -49,6 +49,9 @@ struct FieldArgs {
 // every node", and "in the next round's list".
 constexpr int kFaceUp = 1, kFaceDown = 2, kFaceXm = 4, kFaceXp = 8, kFaceZm = 16, kFaceZp = 32;
 constexpr int kFaceMask = 63, kFull = 64, kQueued = 128;
+// A tile queued by the certification after a sweep: its first pass
+// recomputes only the nodes the certification bitmap marks.
+constexpr int kCert = 256;
 
 // Arguments of one solver round.
 template <typename R>
@@ -63,6 +66,10 @@ struct RoundArgs {
     unsigned long long *stats;  // [0] tiles processed, [1] node updates, [2] staged nodes
     unsigned long long *trace;  // per round: [2*round] tiles, [2*round+1] node updates (or null)
     int round;
+    // nodes a certified tile recomputes first: bit r%32 of word
+    // ((e*nnx + x)*nnz + z)*cert_nw + r/32 (or null)
+    const unsigned *cert;
+    int cert_nw;
     // tile + halo box by one TMA copy (tma != 0): the field as a 4-D tensor
     // (phi, theta, r, event) with the box of the tile shape; err is raised if
     // a copy does not complete in time
@@ -113,6 +120,22 @@ void launch_stream_f32(int idx, int grid, const StreamArgs<float> &a, cudaStream
 void launch_stream_f64(int idx, int grid, const StreamArgs<double> &a, cudaStream_t st);
 int occupancy_stream_f32(int idx);
 int occupancy_stream_f64(int idx);
+
+// After a single sweep from an unset field: mark the nodes a recomputation
+// could change (certification bitmap) and queue their tiles (kCert).
+template <typename R>
+struct CertifyArgs {
+    FieldArgs<R> f;
+    const int *events;          // the events (indices), all swept once
+    int nev;
+    const int *dir;             // [E] sweep directions (bit 0: +theta, bit 1: +phi)
+    unsigned *cert;
+    int cert_nw;
+    int tr, tx, tz;             // the rounds' tile shape
+    int *flag, *list, *count;
+};
+void launch_certify_f32(const CertifyArgs<float> &a, cudaStream_t st);
+void launch_certify_f64(const CertifyArgs<double> &a, cudaStream_t st);
 
 void launch_round_f64(int shape, int grid, const RoundArgs<double> &a, cudaStream_t st);
 void launch_round_f32(int shape, int grid, const RoundArgs<float> &a, cudaStream_t st);
@@ -207,6 +230,8 @@ struct fm3dt_ctx {
     double *d_base = nullptr;
     uint8_t *d_frozen = nullptr;
     int *d_flag = nullptr;
+    unsigned *d_cert = nullptr;   // [maxev][nnx][nnz][cert_nw] certification bitmap
+    int cert_nw = 0;
     int *d_list[2] = {nullptr, nullptr};
     int *d_count[2] = {nullptr, nullptr};
     unsigned long long *d_stats = nullptr;

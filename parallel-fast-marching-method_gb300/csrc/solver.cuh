@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
             s_face = 0;
             // take the halo faces changed since this tile's last pass; later
             // activations re-queue it
-            s_dirty_faces = atomicExch(&a.flag[w], 0) & (kFaceMask | kFull);
+            s_dirty_faces = atomicExch(&a.flag[w], 0) & (kFaceMask | kFull | kCert);
             __threadfence();
         }
         __syncthreads();
@@ -362,6 +362,11 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
             if ((df & kFaceXp) && tx >= TX - 2) dirty = all;
             if ((df & kFaceZm) && tz < 2) dirty = all;
             if ((df & kFaceZp) && tz >= TZ - 2) dirty = all;
+            // a certified tile: the nodes whose sweep value a recomputation
+            // could change (TR divides 32, so a column's rows of the tile lie
+            // in one bitmap word)
+            if ((df & kCert) && colv)
+                dirty |= (a.cert[(((size_t)e * f.nnx + gx) * f.nnz + gz) * a.cert_nw + (r0 >> 5)] >> (r0 & 31)) & all;
             dirty &= updm;
         }
         for (int p = 0; p < a.max_passes; ++p) {
@@ -454,6 +459,114 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
             atomicAdd(&a.trace[2 * a.round + 1], s_upd);
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Certification after a single sweep
+// ---------------------------------------------------------------------------
+
+// A node swept once from an unset field holds F(T) with its three
+// downstream neighbours (up, and the lateral directions the sweep runs
+// toward) unset; every other input was final when it was computed.  The
+// rounds need to recompute it only if one of those neighbours, now set, can
+// change F.  It cannot when, with B = T - (earliest upstream neighbour):
+//   * every downstream neighbour is first order (its second neighbour is not
+//     earlier) and its key is at least B (1 + 1/32), and
+//   * no neighbour with a key of B (1 - 1/32) or more is second order.
+// Why: adding a first-order causal term with key k to an octant's solve
+// gives a root above k (the quadratic is below s^2 at k, or its vertex is
+// above k), so every octant that now takes such a term ends above
+// B (1 + 1/32) less the solve's rounding, which the margin covers tenfold
+// (about 1e-3 of the octant's largest term in single precision); octants
+// that take none are unchanged bit for bit; the earliest neighbour stays the
+// same, and the terms below B come first in every sort as before.  Nodes
+// that fail, and unreached nodes, go into the bitmap.
+template <typename R>
+__global__ void __launch_bounds__(256) certify_kernel(const CertifyArgs<R> a)
+{
+    const FieldArgs<R> &f = a.f;
+    const R INF = Lim<R>::inf();
+    const R margin = R(1.0 / 32.0);
+    const size_t N = (size_t)f.nnx * f.nnz * (size_t)f.nnr;
+    const long long ncol = (long long)f.nnx * f.nnz;
+    const long long total = ncol * a.nev;
+    const int tiles_r = 32 / a.tr;    // tiles of the column in one bitmap word
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(q / ncol);
+        const int c = (int)(q - (long long)k * ncol);
+        const int gx = c / f.nnz, gz = c - gx * f.nnz;
+        const int e = a.events[k];
+        const R *Te = f.T + (size_t)e * N;
+        const int db = a.dir[e];
+        const unsigned down = 1u | (1u << ((db & 1) ? 3 : 2)) | (1u << ((db & 2) ? 5 : 4));
+        auto at = [&](int gr, int x, int z) -> R {
+            return (gr >= 0 && gr < f.nnr && x >= 0 && x < f.nnx && z >= 0 && z < f.nnz)
+                       ? __ldg(Te + ((size_t)gr * f.nnx + x) * f.nnz + z)
+                       : INF;
+        };
+        const unsigned lat = (gx > 0 ? 4u : 0u) | (gx < f.nnx - 1 ? 8u : 0u) | (gz > 0 ? 16u : 0u) |
+                             (gz < f.nnz - 1 ? 32u : 0u);
+        // the column around the node: v[0..4] = layers gr-2 .. gr+2
+        R v0 = INF, v1 = INF, v2 = at(0, gx, gz), v3 = at(1, gx, gz), v4 = at(2, gx, gz);
+        for (int w = 0; w < a.cert_nw; ++w) {
+            unsigned bits = 0;
+            for (int rr = 0; rr < 32; ++rr) {
+                const int gr = w * 32 + rr;
+                if (gr >= f.nnr) break;
+                bool ok = true;
+                const bool frozen = gr == f.nnr - 1 && f.frozen[(size_t)e * f.nnx * f.nnz + (size_t)gx * f.nnz + gz];
+                if (!frozen) {
+                    R t1[6], t2[6];
+                    t1[0] = v1; t2[0] = v0; t1[1] = v3; t2[1] = v4;
+                    t1[2] = at(gr, gx - 1, gz); t2[2] = at(gr, gx - 2, gz);
+                    t1[3] = at(gr, gx + 1, gz); t2[3] = at(gr, gx + 2, gz);
+                    t1[4] = at(gr, gx, gz - 1); t2[4] = at(gr, gx, gz - 2);
+                    t1[5] = at(gr, gx, gz + 1); t2[5] = at(gr, gx, gz + 2);
+                    const unsigned inb = lat | (gr > 0 ? 1u : 0u) | (gr < f.nnr - 1 ? 2u : 0u);
+                    R tu = INF;
+#pragma unroll
+                    for (int d = 0; d < 6; ++d)
+                        if (((inb & ~down) >> d) & 1u) tu = fm_min(tu, t1[d]);
+                    const R T = v2;
+                    ok = T < INF && tu < INF;
+                    const R B = T - tu;
+                    const R hi = B + B * margin, lo = B - B * margin;
+#pragma unroll
+                    for (int d = 0; d < 6; ++d) {
+                        if (!((inb >> d) & 1u)) continue;
+                        const R kd = t1[d] - tu;
+                        const bool o2 = f.order2 && (t2[d] < t1[d]);
+                        if ((down >> d) & 1u) {
+                            if (!(kd >= hi) || o2) ok = false;
+                        } else if (!(kd < lo) && o2) {
+                            ok = false;
+                        }
+                    }
+                }
+                if (!ok) bits |= 1u << rr;
+                v0 = v1; v1 = v2; v2 = v3; v3 = v4; v4 = at(gr + 3, gx, gz);
+            }
+            a.cert[((size_t)e * ncol + c) * a.cert_nw + w] = bits;
+            // queue the tiles of this word's rows that hold a marked node
+            for (int j = 0; j < tiles_r; ++j) {
+                if (!((bits >> (j * a.tr)) & ((a.tr >= 32) ? 0xffffffffu : ((1u << a.tr) - 1u)))) continue;
+                const int tri = (w * 32) / a.tr + j;
+                if (tri >= f.ntr) break;
+                const int t = e * f.tiles_per_event + (tri * f.ntx + gx / a.tx) * f.ntz + gz / a.tz;
+                if (!(atomicOr(&a.flag[t], kCert | kQueued) & kQueued)) a.list[atomicAdd(a.count, 1)] = t;
+            }
+        }
+    }
+}
+
+template <typename R>
+void launch_certify(const CertifyArgs<R> &a, cudaStream_t st)
+{
+    const long long total = (long long)a.f.nnx * a.f.nnz * a.nev;
+    if (total <= 0) return;
+    const int grid = (int)std::min<long long>((total + 255) / 256, 1LL << 20);
+    certify_kernel<R><<<grid, 256, 0, st>>>(a);
 }
 
 // ---------------------------------------------------------------------------

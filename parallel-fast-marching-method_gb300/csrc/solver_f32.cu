@@ -4,6 +4,11 @@
 
 namespace fm3dt {
 
+void launch_certify_f32(const CertifyArgs<float> &a, cudaStream_t st)
+{
+    launch_certify<float>(a, st);
+}
+
 void launch_round_f32(int shape, int grid, const RoundArgs<float> &a, cudaStream_t st)
 {
 #define C_(S) ShapeKernels<float, S>::round(grid, a, st)

@@ -4,6 +4,11 @@
 
 namespace fm3dt {
 
+void launch_certify_f64(const CertifyArgs<double> &a, cudaStream_t st)
+{
+    launch_certify<double>(a, st);
+}
+
 void launch_round_f64(int shape, int grid, const RoundArgs<double> &a, cudaStream_t st)
 {
 #define C_(S) ShapeKernels<double, S>::round(grid, a, st)

@@ -237,6 +237,46 @@ def test_sweeps_many_azimuths_bitwise(gpu_lib, prec, cfg, scale):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("cfg,scale", [(1, 40), (3, 30)])
+def test_two_part_first_round_bitwise(gpu_lib, prec, cfg, scale):
+    """A batch with at least 32 events that are not near ties takes the
+    two-part schedule: the near-tie events swept and their first round run on
+    a second stream, the others swept once, certified, and recomputed only
+    where the certification fails.  It gives the same fields bit for bit as
+    the same events in batches of 8 (one sweep pass, every tile in the first
+    round), and they are a fixed point."""
+    import fm3dt
+    baz = np.concatenate([np.linspace(0.0, 352.5, 48), [0.4, 90.3, 179.6, 270.2]])
+    events = np.stack([np.linspace(32.0, 88.0, len(baz)), baz], axis=1)
+    w = _setup(cfg, scale, events=events)
+    params = _params(w)
+    n = len(params)
+    with fm3dt.Solver(w.header, precision=prec, max_events=n) as s:
+        s.set_velocity(w.velv)
+        s.set_tuning(1, 16, 0, 1)                     # (8, 8, 32) tiles, streaming sweep
+        ref = []
+        for e0 in range(0, n, 8):
+            st = s.solve_planewave(params[e0:e0 + 8])
+            assert st["converged"] == 1
+            ref += [s.get_times(e) for e in range(len(params[e0:e0 + 8]))]
+        ref = np.concatenate(ref)
+        st = s.solve_planewave(params)
+        assert st["converged"] == 1
+        # the certification left most of the other events' tiles out of the
+        # first round (the batches of 8 visit every tile)
+        tiles0 = s.round_trace()[0][0]
+        got = np.concatenate([s.get_times(e) for e in range(n)])
+        assert np.array_equal(got, ref)
+        st = s.solve_resume()
+        assert st["converged"] == 1
+        again = np.concatenate([s.get_times(e) for e in range(n)])
+    assert np.array_equal(again, ref)
+    h = w.header
+    tiles_per_event = -(-h.nn[0] // 8) * -(-h.nn[1] // 8) * -(-h.nn[2] // 32)
+    assert 0 < tiles0 < n * tiles_per_event // 2
+
+
+@pytest.mark.parametrize("prec", [0, 1])
 def test_tma_staging_bitwise(gpu_lib, prec, monkeypatch):
     """The rounds stage a tile and its halos by one TMA copy when the phi rows
     are a multiple of 16 bytes, else by thread loads; both give the same field
