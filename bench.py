@@ -171,7 +171,7 @@ KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.15, "stream_sweep_kernel": 31.8}
 # the rounds (first round and tail rounds together).  The kernels are bound
 # by instruction issue, so the bench also reports the issue rate they reach
 # against the SMs' peak of four warp instructions per cycle.
-KERNEL_WARP_INST_PER_NODE = {"round_kernel": 25.28, "stream_sweep_kernel": 32.47}
+KERNEL_WARP_INST_PER_NODE = {"round_kernel": 25.28, "stream_sweep_kernel": 20.15}
 
 
 def _oracle_event(args):

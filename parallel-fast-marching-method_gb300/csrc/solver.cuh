@@ -482,75 +482,75 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
 // same, and the terms below B come first in every sort as before.  Nodes
 // that fail, and unreached nodes, go into the bitmap.
 template <typename R>
-__global__ void __launch_bounds__(256) certify_kernel(const CertifyArgs<R> a)
+__global__ void __launch_bounds__(256, 4) certify_kernel(const CertifyArgs<R> a)
 {
     const FieldArgs<R> &f = a.f;
     const R INF = Lim<R>::inf();
     const R margin = R(1.0 / 32.0);
-    const size_t N = (size_t)f.nnx * f.nnz * (size_t)f.nnr;
-    const long long ncol = (long long)f.nnx * f.nnz;
+    const size_t layer = (size_t)f.nnx * f.nnz;
+    const size_t N = layer * (size_t)f.nnr;
+    const long long ncol = (long long)layer;
     const long long total = ncol * a.nev;
     const int tiles_r = 32 / a.tr;    // tiles of the column in one bitmap word
+    const unsigned tmask = (a.tr >= 32) ? 0xffffffffu : ((1u << a.tr) - 1u);
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
          q += (long long)gridDim.x * blockDim.x) {
         const int k = (int)(q / ncol);
         const int c = (int)(q - (long long)k * ncol);
         const int gx = c / f.nnz, gz = c - gx * f.nnz;
         const int e = a.events[k];
-        const R *Te = f.T + (size_t)e * N;
+        const R *col = f.T + (size_t)e * N + c;    // this column's node in layer 0
+        // lateral neighbours: downstream (the way the sweep runs) and
+        // upstream steps in theta (elements of nnz) and phi, and whether the
+        // first and second neighbours lie inside the grid
         const int db = a.dir[e];
-        const unsigned down = 1u | (1u << ((db & 1) ? 3 : 2)) | (1u << ((db & 2) ? 5 : 4));
-        auto at = [&](int gr, int x, int z) -> R {
-            return (gr >= 0 && gr < f.nnr && x >= 0 && x < f.nnx && z >= 0 && z < f.nnz)
-                       ? __ldg(Te + ((size_t)gr * f.nnx + x) * f.nnz + z)
-                       : INF;
-        };
-        const unsigned lat = (gx > 0 ? 4u : 0u) | (gx < f.nnx - 1 ? 8u : 0u) | (gz > 0 ? 16u : 0u) |
-                             (gz < f.nnz - 1 ? 32u : 0u);
-        // the column around the node: v[0..4] = layers gr-2 .. gr+2
-        R v0 = INF, v1 = INF, v2 = at(0, gx, gz), v3 = at(1, gx, gz), v4 = at(2, gx, gz);
+        const int sx = (db & 1) ? 1 : -1, sz = (db & 2) ? 1 : -1;
+        const long long ox = (long long)sx * f.nnz;
+        const bool xd1 = (unsigned)(gx + sx) < (unsigned)f.nnx, xd2 = (unsigned)(gx + 2 * sx) < (unsigned)f.nnx;
+        const bool xu1 = (unsigned)(gx - sx) < (unsigned)f.nnx, xu2 = (unsigned)(gx - 2 * sx) < (unsigned)f.nnx;
+        const bool zd1 = (unsigned)(gz + sz) < (unsigned)f.nnz, zd2 = (unsigned)(gz + 2 * sz) < (unsigned)f.nnz;
+        const bool zu1 = (unsigned)(gz - sz) < (unsigned)f.nnz, zu2 = (unsigned)(gz - 2 * sz) < (unsigned)f.nnz;
+        const bool frozen_col = f.frozen[(size_t)e * layer + c] != 0;
+        auto colv = [&](int gr) -> R { return (gr >= 0 && gr < f.nnr) ? __ldg(col + (size_t)gr * layer) : INF; };
+        // the column around the node: v0..v4 = layers gr-2 .. gr+2
+        R v0 = INF, v1 = INF, v2 = colv(0), v3 = colv(1), v4 = colv(2);
         for (int w = 0; w < a.cert_nw; ++w) {
             unsigned bits = 0;
             for (int rr = 0; rr < 32; ++rr) {
                 const int gr = w * 32 + rr;
                 if (gr >= f.nnr) break;
                 bool ok = true;
-                const bool frozen = gr == f.nnr - 1 && f.frozen[(size_t)e * f.nnx * f.nnz + (size_t)gx * f.nnz + gz];
-                if (!frozen) {
-                    R t1[6], t2[6];
-                    t1[0] = v1; t2[0] = v0; t1[1] = v3; t2[1] = v4;
-                    t1[2] = at(gr, gx - 1, gz); t2[2] = at(gr, gx - 2, gz);
-                    t1[3] = at(gr, gx + 1, gz); t2[3] = at(gr, gx + 2, gz);
-                    t1[4] = at(gr, gx, gz - 1); t2[4] = at(gr, gx, gz - 2);
-                    t1[5] = at(gr, gx, gz + 1); t2[5] = at(gr, gx, gz + 2);
-                    const unsigned inb = lat | (gr > 0 ? 1u : 0u) | (gr < f.nnr - 1 ? 2u : 0u);
-                    R tu = INF;
-#pragma unroll
-                    for (int d = 0; d < 6; ++d)
-                        if (((inb & ~down) >> d) & 1u) tu = fm_min(tu, t1[d]);
+                if (!(gr == f.nnr - 1 && frozen_col)) {
+                    const R *p = col + (size_t)gr * layer;
                     const R T = v2;
+                    // upstream first neighbours: down (r+1) and the lateral ones
+                    const R td = gr < f.nnr - 1 ? v3 : INF;
+                    const R txu = xu1 ? __ldg(p - ox) : INF;
+                    const R tzu = zu1 ? __ldg(p - sz) : INF;
+                    const R tu = fm_min(td, fm_min(txu, tzu));
                     ok = T < INF && tu < INF;
                     const R B = T - tu;
                     const R hi = B + B * margin, lo = B - B * margin;
-#pragma unroll
-                    for (int d = 0; d < 6; ++d) {
-                        if (!((inb >> d) & 1u)) continue;
-                        const R kd = t1[d] - tu;
-                        const bool o2 = f.order2 && (t2[d] < t1[d]);
-                        if ((down >> d) & 1u) {
-                            if (!(kd >= hi) || o2) ok = false;
-                        } else if (!(kd < lo) && o2) {
-                            ok = false;
-                        }
+                    // a downstream neighbour passes when its key is at least hi
+                    // and it is first order (its second neighbour not earlier)
+                    auto down_ok = [&](R t1, R t2) { return (t1 - tu) >= hi && !(f.order2 && t2 < t1); };
+                    if (gr > 0) ok = ok && down_ok(v1, v0);
+                    if (xd1) ok = ok && down_ok(__ldg(p + ox), xd2 ? __ldg(p + 2 * ox) : INF);
+                    if (zd1) ok = ok && down_ok(__ldg(p + sz), zd2 ? __ldg(p + 2 * sz) : INF);
+                    // an upstream neighbour at or above lo must be first order
+                    if (f.order2) {
+                        if (gr < f.nnr - 1 && !((td - tu) < lo) && v4 < td) ok = false;
+                        if (xu1 && !((txu - tu) < lo) && xu2 && __ldg(p - 2 * ox) < txu) ok = false;
+                        if (zu1 && !((tzu - tu) < lo) && zu2 && __ldg(p - 2 * sz) < tzu) ok = false;
                     }
                 }
                 if (!ok) bits |= 1u << rr;
-                v0 = v1; v1 = v2; v2 = v3; v3 = v4; v4 = at(gr + 3, gx, gz);
+                v0 = v1; v1 = v2; v2 = v3; v3 = v4; v4 = colv(gr + 3);
             }
             a.cert[((size_t)e * ncol + c) * a.cert_nw + w] = bits;
             // queue the tiles of this word's rows that hold a marked node
-            for (int j = 0; j < tiles_r; ++j) {
-                if (!((bits >> (j * a.tr)) & ((a.tr >= 32) ? 0xffffffffu : ((1u << a.tr) - 1u)))) continue;
+            for (int j = 0; j < tiles_r && bits; ++j) {
+                if (!((bits >> (j * a.tr)) & tmask)) continue;
                 const int tri = (w * 32) / a.tr + j;
                 if (tri >= f.ntr) break;
                 const int t = e * f.tiles_per_event + (tri * f.ntx + gx / a.tx) * f.ntz + gz / a.tz;
