@@ -514,29 +514,42 @@ __global__ void __launch_bounds__(256, 4) certify_kernel(const CertifyArgs<R> a)
         auto colv = [&](int gr) -> R { return (gr >= 0 && gr < f.nnr) ? __ldg(col + (size_t)gr * layer) : INF; };
         // the column around the node: v0..v4 = layers gr-2 .. gr+2
         R v0 = INF, v1 = INF, v2 = colv(0), v3 = colv(1), v4 = colv(2);
+        // the lateral neighbours of layer gr (unset outside the grid), read a
+        // layer ahead: upstream first, downstream first and second
+        R nxu, nzu, nxd, nxd2, nzd, nzd2;
+        auto lateral = [&](int gr) {
+            const bool in = gr < f.nnr;
+            const R *p = col + (size_t)(in ? gr : 0) * layer;
+            nxu = in && xu1 ? __ldg(p - ox) : INF;
+            nzu = in && zu1 ? __ldg(p - sz) : INF;
+            nxd = in && xd1 ? __ldg(p + ox) : INF;
+            nxd2 = in && xd2 ? __ldg(p + 2 * ox) : INF;
+            nzd = in && zd1 ? __ldg(p + sz) : INF;
+            nzd2 = in && zd2 ? __ldg(p + 2 * sz) : INF;
+        };
+        lateral(0);
         for (int w = 0; w < a.cert_nw; ++w) {
             unsigned bits = 0;
             for (int rr = 0; rr < 32; ++rr) {
                 const int gr = w * 32 + rr;
                 if (gr >= f.nnr) break;
                 bool ok = true;
+                const R txu = nxu, tzu = nzu, txd = nxd, txd2 = nxd2, tzd = nzd, tzd2 = nzd2;
+                lateral(gr + 1);
                 if (!(gr == f.nnr - 1 && frozen_col)) {
                     const R *p = col + (size_t)gr * layer;
                     const R T = v2;
                     // upstream first neighbours: down (r+1) and the lateral ones
                     const R td = gr < f.nnr - 1 ? v3 : INF;
-                    const R txu = xu1 ? __ldg(p - ox) : INF;
-                    const R tzu = zu1 ? __ldg(p - sz) : INF;
                     const R tu = fm_min(td, fm_min(txu, tzu));
                     ok = T < INF && tu < INF;
                     const R B = T - tu;
                     const R hi = B + B * margin, lo = B - B * margin;
                     // a downstream neighbour passes when its key is at least hi
-                    // and it is first order (its second neighbour not earlier)
+                    // and it is first order (its second neighbour not earlier);
+                    // one outside the grid reads unset and passes
                     auto down_ok = [&](R t1, R t2) { return (t1 - tu) >= hi && !(f.order2 && t2 < t1); };
-                    if (gr > 0) ok = ok && down_ok(v1, v0);
-                    if (xd1) ok = ok && down_ok(__ldg(p + ox), xd2 ? __ldg(p + 2 * ox) : INF);
-                    if (zd1) ok = ok && down_ok(__ldg(p + sz), zd2 ? __ldg(p + 2 * sz) : INF);
+                    ok = ok && down_ok(v1, v0) && down_ok(txd, txd2) && down_ok(tzd, tzd2);
                     // an upstream neighbour at or above lo must be first order
                     if (f.order2) {
                         if (gr < f.nnr - 1 && !((td - tu) < lo) && v4 < td) ok = false;
