@@ -515,10 +515,45 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     CK(cudaMemsetAsync(ctx->d_count[1], 0, sizeof(int), s));
     CK(cudaMemsetAsync(ctx->d_stats, 0, 3 * sizeof(unsigned long long), s));
     CK(cudaMemsetAsync(ctx->d_trace, 0, 2 * sizeof(unsigned long long) * fm3dt_ctx::kTraceRounds, s));
+    // Certification of the events swept exactly once (all but the near-tie
+    // events, which had extra sweeps): their first round recomputes only the
+    // nodes it marks, on the tiles it appends to list 0
+    auto certify = [&](const int *events, int n, cudaStream_t st) {
+        auto fill = [&](auto &ca, const auto &f) {
+            ca.f = f;
+            ca.events = events; ca.nev = n;
+            ca.dir = ctx->d_dir;
+            ca.cert = ctx->d_cert; ca.cert_nw = ctx->cert_nw;
+            ca.tr = ts.tr; ca.tx = ts.tx; ca.tz = ts.tz;
+            ca.flag = ctx->d_flag; ca.list = ctx->d_list[0]; ca.count = ctx->d_count[0];
+        };
+        if (ctx->prec == FM3DT_FP64) {
+            CertifyArgs<double> ca{};
+            fill(ca, f64);
+            launch_certify_f64(ca, st);
+        } else {
+            CertifyArgs<float> ca{};
+            fill(ca, f32);
+            launch_certify_f32(ca, st);
+        }
+        ctx->launches += 1;
+    };
+    const bool certify_alone = FM_CERTIFY && do_sweep && streaming && !verified && !overlap && !others.empty();
     if (!verified) {
         CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
         if (overlap) {
             // the first round is launched below, in two parts
+        } else if (certify_alone) {
+            // the near-tie events' tiles first (this sets the count), then the
+            // other events' marked tiles appended
+            if (!ties.empty())
+                launch_initial_tiles((int)ties.size(), ctx->d_events, tpe, first, cnt, ctx->d_list[0],
+                                     ctx->d_count[0], ctx->d_flag, s);
+            else
+                CK(cudaMemsetAsync(ctx->d_count[0], 0, sizeof(int), s));
+            CK(cudaMemcpyAsync(ctx->d_events_b, others.data(), others.size() * sizeof(int), cudaMemcpyHostToDevice,
+                               s));
+            certify(ctx->d_events_b, (int)others.size(), s);
         } else if (mode == kPoint)
             launch_initial_tiles_box(nev, tpe, ntx, ntz, ts.tr, ts.tx, ts.tz, ctx->d_box_init, ctx->d_list[0],
                                      ctx->d_count[0], ctx->d_flag, s);
@@ -659,23 +694,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             // the other events were swept once: only the tiles holding a node
             // the certification cannot clear, from those nodes
             CK(cudaMemsetAsync(ctx->d_count[0], 0, sizeof(int), s));
-            auto certify = [&](auto &ca, const auto &f) {
-                ca.f = f;
-                ca.events = ctx->d_events_b; ca.nev = (int)others.size();
-                ca.dir = ctx->d_dir;
-                ca.cert = ctx->d_cert; ca.cert_nw = ctx->cert_nw;
-                ca.tr = ts.tr; ca.tx = ts.tx; ca.tz = ts.tz;
-                ca.flag = ctx->d_flag; ca.list = ctx->d_list[0]; ca.count = ctx->d_count[0];
-            };
-            if (ctx->prec == FM3DT_FP64) {
-                CertifyArgs<double> ca{};
-                certify(ca, f64);
-                launch_certify_f64(ca, s);
-            } else {
-                CertifyArgs<float> ca{};
-                certify(ca, f32);
-                launch_certify_f32(ca, s);
-            }
+            certify(ctx->d_events_b, (int)others.size(), s);
             launch_round(0, ctx->d_list[0], ctx->d_count[0], ctx->d_list[1], ctx->d_count[1], s);
         } else {
             launch_initial_tiles((int)others.size(), ctx->d_events_b, tpe, first, cnt, ctx->d_list[0],
@@ -718,7 +737,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             CK(cudaEventRecord(ctx->round_events[2 * k], s));
             // the first round's tile count is known on the host: one CTA per
             // tile, so blocks free up as they finish
-            if (rounds == 0 && FM_ROUND0_PER_TILE && !verified && mode != kPoint)
+            if (rounds == 0 && FM_ROUND0_PER_TILE && !verified && mode != kPoint && !certify_alone)
                 grid_override = (int)std::min<long long>((long long)nev * cnt, 1LL << 30);
             launch_round(rounds, ctx->d_list[cur], ctx->d_count[cur], ctx->d_list[nxt], ctx->d_count[nxt], s);
             grid_override = 0;

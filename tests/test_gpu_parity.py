@@ -242,9 +242,9 @@ def test_two_part_first_round_bitwise(gpu_lib, prec, cfg, scale):
     """A batch with at least 32 events that are not near ties takes the
     two-part schedule: the near-tie events swept and their first round run on
     a second stream, the others swept once, certified, and recomputed only
-    where the certification fails.  It gives the same fields bit for bit as
-    the same events in batches of 8 (one sweep pass, every tile in the first
-    round), and they are a fixed point."""
+    where the certification fails.  Batches of 8 certify their singly swept
+    events on one stream.  Both give the same fields bit for bit as rounds
+    without a sweep (nothing certified), and they are a fixed point."""
     import fm3dt
     baz = np.concatenate([np.linspace(0.0, 352.5, 48), [0.4, 90.3, 179.6, 270.2]])
     events = np.stack([np.linspace(32.0, 88.0, len(baz)), baz], axis=1)
@@ -253,17 +253,21 @@ def test_two_part_first_round_bitwise(gpu_lib, prec, cfg, scale):
     n = len(params)
     with fm3dt.Solver(w.header, precision=prec, max_events=n) as s:
         s.set_velocity(w.velv)
-        s.set_tuning(1, 16, 0, 1)                     # (8, 8, 32) tiles, streaming sweep
-        ref = []
+        s.set_tuning(1, 16, 0, 0)                     # (8, 8, 32) tiles, rounds only
+        st = s.solve_planewave(params)
+        assert st["converged"] == 1
+        ref = np.concatenate([s.get_times(e) for e in range(n)])
+        s.set_tuning(1, 16, 0, 1)                     # streaming sweep first
+        small = []
         for e0 in range(0, n, 8):
             st = s.solve_planewave(params[e0:e0 + 8])
             assert st["converged"] == 1
-            ref += [s.get_times(e) for e in range(len(params[e0:e0 + 8]))]
-        ref = np.concatenate(ref)
+            small += [s.get_times(e) for e in range(len(params[e0:e0 + 8]))]
+        assert np.array_equal(np.concatenate(small), ref)
         st = s.solve_planewave(params)
         assert st["converged"] == 1
         # the certification left most of the other events' tiles out of the
-        # first round (the batches of 8 visit every tile)
+        # first round
         tiles0 = s.round_trace()[0][0]
         got = np.concatenate([s.get_times(e) for e in range(n)])
         assert np.array_equal(got, ref)
