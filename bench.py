@@ -159,19 +159,21 @@ def measured_peak_hbm():
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per node of
-# each single-precision solver kernel, from one ncu capture of a smaller case
-# of the same kernels (96^3, 64 events): the first round's launch (every tile
-# staged) and one mid-sweep launch; the bench scales it to its own launches
-# by the nodes they process.
-KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.15, "stream_sweep_kernel": 31.8}
+# each single-precision solver kernel, from ncu captures of smaller cases of
+# the same kernels: a first round with every tile staged (96^3, 64 events)
+# and a full mid-sweep launch of a main sweep in four height segments (128^3,
+# 64 events); the bench scales it to its own launches by the nodes they
+# process.
+KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.15, "stream_sweep_kernel": 30.6}
 
 # Warp instructions per node of the same kernels, from ncu's
-# smsp__inst_executed.sum summed over every launch of three solves of that
-# case: per node swept (main and near-tie sweeps), and per node staged by
-# the rounds (first round and tail rounds together).  The kernels are bound
-# by instruction issue, so the bench also reports the issue rate they reach
-# against the SMs' peak of four warp instructions per cycle.
-KERNEL_WARP_INST_PER_NODE = {"round_kernel": 25.28, "stream_sweep_kernel": 20.15}
+# smsp__inst_executed.sum summed over every launch of three solves: per node
+# swept on the 128^3 grid with sweeps in four height segments (16 events),
+# and per node staged by the rounds on the 96^3 case (64 events: first
+# rounds after certification and tail rounds together).  The kernels are
+# bound by instruction issue, so the bench also reports the issue rate they
+# reach against the SMs' peak of four warp instructions per cycle.
+KERNEL_WARP_INST_PER_NODE = {"round_kernel": 41.6, "stream_sweep_kernel": 23.15}
 
 
 def _oracle_event(args):
