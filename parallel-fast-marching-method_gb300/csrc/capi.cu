@@ -201,6 +201,9 @@ int stream_segments(const fm3dt_ctx *ctx, int nitems, int nbx, int nbz, int sgri
 {
     const int nnr = ctx->g.nnr;
     constexpr double kLaunchSteps = 4.0;
+    // an item fills its ring (five layers and the first prefetch) before its
+    // first step: about six steps' worth of loads
+    constexpr int kFillSteps = 6;
     // blocks per lateral hyperplane (x' + z' = d)
     std::vector<long long> lat(nbx + nbz - 1, 0);
     for (int d = 0; d < nbx + nbz - 1; ++d)
@@ -217,7 +220,7 @@ int stream_segments(const fm3dt_ctx *ctx, int nitems, int nbx, int nbz, int sgri
                 if (d >= 0 && d < nbx + nbz - 1) cnt += lat[d];
             }
             const long long items = cnt * (long long)nitems;
-            t += (double)((items + sgrid - 1) / sgrid) * (seg_len + ramp) + kLaunchSteps;
+            t += (double)((items + sgrid - 1) / sgrid) * (seg_len + ramp + kFillSteps) + kLaunchSteps;
         }
         if (nseg == 1 || t < best_t) {
             best = nseg;
