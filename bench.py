@@ -168,12 +168,13 @@ KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.15, "stream_sweep_kernel": 30.6}
 
 # Warp instructions per node of the same kernels, from ncu's
 # smsp__inst_executed.sum summed over every launch of three solves: per node
-# swept on the 128^3 grid with sweeps in four height segments (16 events),
+# swept on the 128^3 grid with sweeps in two height segments (16 events; the
+# 128^3 x 256 workload's main sweeps use two),
 # and per node staged by the rounds on the 96^3 case (64 events: first
 # rounds after certification and tail rounds together).  The kernels are
 # bound by instruction issue, so the bench also reports the issue rate they
 # reach against the SMs' peak of four warp instructions per cycle.
-KERNEL_WARP_INST_PER_NODE = {"round_kernel": 41.6, "stream_sweep_kernel": 23.15}
+KERNEL_WARP_INST_PER_NODE = {"round_kernel": 41.6, "stream_sweep_kernel": 20.15}
 
 
 def _oracle_event(args):
