@@ -259,6 +259,7 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
     round_kernel(const __grid_constant__ RoundArgs<R> a)
 {
     using TL = Tile<R, TR, TX, TZ>;
+    static_assert(32 % TR == 0, "a column's rows of a tile lie in one certification word");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     R *box = reinterpret_cast<R *>(smem_raw);
     __shared__ __align__(8) unsigned long long s_bar;
