@@ -285,7 +285,7 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 // Solve schedule (compile-time tuning; the measured best on this GPU):
 //   FM_TIE_SWEEPS          extra sweeps of near-tie events (reversed, forward, ...)
 //   FM_ROUND0_PER_TILE     first round with one CTA per tile when its tile count is known
-//   FM_OVERLAP_TIES        near-tie sweeps beside the other events' first round ...
+//   FM_OVERLAP_TIES        near-tie events' sweeps and first round beside the other events' ...
 //   FM_OVERLAP_MIN_EVENTS  ... when at least this many other events are in the batch
 //   FM_CERTIFY             the other events' first round only where the certification
 //                          of their single sweep fails
@@ -653,11 +653,13 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         return FM3DT_OK;
     };
     if (overlap) {
-        // first round, in two parts that run side by side: the other events'
-        // tiles on the context stream from the end of the main sweep, one CTA
-        // per tile so that blocks free up as they finish; the near-tie events'
-        // extra sweeps and then their tiles on stream2, whose higher priority
-        // gets its blocks scheduled first; both queue onto list 1
+        // the solve in two parts that run side by side, both queueing onto
+        // list 1 for the next round: on stream2, whose higher priority gets
+        // its blocks scheduled first, the near-tie events' main sweep, their
+        // extra sweeps and their first round (every tile); on the context
+        // stream, the other events' main sweep, their certification and their
+        // first round on the tiles it marks (or, without the certification,
+        // every tile, one CTA per tile so that blocks free up as they finish)
         cudaEvent_t fork, join, r0, r1;
         CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
