@@ -71,11 +71,16 @@ typedef struct {
     int64_t node_passes;      /* node updates (tile nodes x in-tile passes) */
     int64_t tile_nodes;       /* grid nodes staged by all tile activations */
     double ms;                /* device time of the whole solve */
-    double round_ms;          /* device time inside the tile-round kernels */
+    double round_ms;          /* device time of the rounds: from the end of the sweep interval
+                                 to the last round (in batches solved in two parts it also
+                                 covers the near-tie events' extra sweeps and the
+                                 certification, which run beside the first round) */
     int round_launches;       /* tile-round kernel launches */
-    int sweep_launches;       /* directional-sweep kernel launches */
-    double sweep_ms;          /* device time of the directional sweep */
-    int64_t sweep_nodes;      /* grid nodes staged by the sweep */
+    int sweep_launches;       /* directional-sweep kernel launches (all passes) */
+    double sweep_ms;          /* device time of the sweep interval: the main sweep (in
+                                 batches solved in two parts, until the other events' main
+                                 sweep ends) plus any re-sweeps */
+    int64_t sweep_nodes;      /* grid nodes staged by all sweep passes */
 } fm3dt_status;
 
 typedef struct fm3dt_ctx fm3dt_ctx;
