@@ -341,7 +341,10 @@ def run_ours(a):
         "round_kernel": (round_ms, staged, round_launches, staged),
         sweep_name: (sweep_ms, main_nodes, sweep_launches, sweep_nodes),
     }
-    if a.prec == "f32" and all(k in KERNEL_WARP_INST_PER_NODE for k in kernels):
+    # (the single-precision counts also weigh the double-precision kernels:
+    # the same octant work per node; the rounds' interval holds sweeps too, so
+    # device time cannot tell them apart)
+    if all(k in KERNEL_WARP_INST_PER_NODE for k in kernels):
         work = {k: KERNEL_WARP_INST_PER_NODE[k] * v[3] for k, v in kernels.items()}
     else:
         work = {k: v[0] for k, v in kernels.items()}
