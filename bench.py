@@ -1,31 +1,35 @@
 #!/usr/bin/env python
-"""Benchmark of the batched forward traveltime solve on GB300.
+"""Benchmark of the batched forward traveltime iteration on GB300.
 
 Metric: batched eikonal solves/s (whole job, all GPUs) with p50/p99 step
 latency, at <= 1e-5 relative receiver-time error against the plain FP64 GPU
-path (checked on a subset of events, untimed).
+path (checked on 64 events, untimed).
 
-Workload (default): 128 x 128 x 128 (r, theta, phi) propagation grid, 12 x 14
-x 14 B-spline velocity nodes with +-3% Gaussian node noise, 256 teleseismic
-plane-wave events (distance 30-90 deg, back-azimuth 0-360 deg), 300 surface
-receivers, single-precision offset stencils.  Synthetic, seeded inputs (the
-reference publishes no benchmark and its boundary-time file is not
-available).
+Workload (default): the tomography grid -- 192 x 224 x 224 (r, theta, phi)
+propagation nodes, 16 x 20 x 20 B-spline velocity nodes with a +-5%
+checkerboard, 500 teleseismic plane-wave events (distance 30-90 deg,
+back-azimuth 0-360 deg), 300 surface receivers, single-precision offset
+stencils.  Synthetic, seeded inputs (the reference publishes no benchmark and
+its boundary-time file is not available).
 
-One step = one batched solve of all events of this rank (boundary injection +
-tile rounds until convergence).  `value` uses boundary frames already
-resident in HBM; `e2e` goes through the public C ABI with pinned host
-buffers: boundary frames host->device and receiver times device->host inside
-every step.  The traveltime fields (2.1 GB per step) are larger than L2, so
-no flush is needed between steps.
+One step = one forward iteration of all events of this rank: boundary
+injection and the solve to convergence, receiver times, and rays with their
+Frechet rows (CSR) -- what one tomography iteration needs before the
+subspace step (``--step solve`` times the solve alone).  `value` uses
+boundary frames, receivers and outputs in HBM (the device-memory entry
+points); `e2e` goes through the host entry points with pinned host buffers:
+boundary frames and receivers host->device, receiver times and the Frechet
+rows device->host inside every step.  The traveltime fields (19 GB per step)
+are larger than L2, so no flush is needed between steps.
 
 Multi-GPU (torchrun): events shard across ranks (each rank solves its own
 batch of the same size, weak scaling); no data-path collective, a gloo
 barrier and a max-reduce of the timings only.
 
 --impl reference: times the CPU oracle (a C restatement of the reference's
-serial fast marching, fm3dt_parallel.f90 local_fmm) on all host cores on a
-bounded sample of the same workload.
+serial fast marching, fm3dt_parallel.f90 local_fmm, with srtimes and
+parallel_rpaths) on all host cores, one event per core per step, on the same
+workload.
 """
 from __future__ import annotations
 
@@ -54,14 +58,16 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--config", type=int, default=3)
+    ap.add_argument("--step", choices=["forward", "solve"], default="forward",
+                    help="forward: solve + receiver times + rays and Frechet rows; solve: the solve alone")
     ap.add_argument("--scale", type=int, default=0, help="override the grid edge (small profiling cases)")
     ap.add_argument("--events", type=int, default=0)
     ap.add_argument("--prec", choices=["f32", "f64"], default="f32")
     ap.add_argument("--shape", type=int, default=-1, help="tile shape index (-1: autotune)")
     ap.add_argument("--passes", type=int, default=0)
     ap.add_argument("--sweep-shape", type=int, default=-1, help="sweep tile shape index (-1: same as --shape)")
-    ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline, FP64 check and e2e leg")
+    ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline, FP64 checks and e2e leg")
     ap.add_argument("--duration", type=float, default=30.0, help="config 4: seconds of Poisson arrivals")
     ap.add_argument("--sweep-mode", type=int, default=1,
                     help="with --shape: 1 sweep then rounds, 2 sweep + verifying sweep, 0 no sweep")
@@ -177,67 +183,136 @@ KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.15, "stream_sweep_kernel": 30.6}
 KERNEL_WARP_INST_PER_NODE = {"round_kernel": 41.6, "stream_sweep_kernel": 20.15}
 
 
+def workload_config(cfg, step, h, nev, nrc, prec):
+    """The `config` object of both arms' lines (the same keys and values)."""
+    nnr, nnx, nnz = h.nn
+    what = ("solve + receiver times + rays and Frechet rows" if step == "forward" else "solve")
+    return {"workload": f"config{cfg}: batched teleseismic plane-wave events, {nnr}x{nnx}x{nnz} (r,theta,phi) "
+                        f"grid, {h.nv[0]}x{h.nv[1]}x{h.nv[2]} velocity nodes, {nev} events per GPU, {nrc} "
+                        f"receivers; one step = {what} of every event",
+            "grid": [nnr, nnx, nnz], "velocity_nodes": list(h.nv), "events_per_gpu": nev, "receivers": nrc,
+            "step": step, "precision": "FP32 offset" if prec == "f32" else "FP64",
+            "l2": "inputs larger than L2 (traveltime fields %.1f GB per step)" %
+                  (nev * nnr * nnx * nnz * (4 if prec == "f32" else 8) / 1e9)}
+
+
+_ORC_CACHE = {}
+
+
+def _oracle_setup(cfg, scale, nev):
+    """Per worker process, once per workload: grid, gridded velocity,
+    receivers and boundary frames (not timed)."""
+    key = (cfg, scale, nev)
+    if key not in _ORC_CACHE:
+        import numpy as np
+        import oracle as O
+        from fm3dt import synth
+        w = synth.config(cfg, scale=scale or None, nev=nev)
+        h = w.header
+        g = O.grid_from_header(h.nv, h.vorig, h.vstep, h.nn, h.norig, h.nstep, h.earth)
+        veln, _ = O.gridder(g, w.velv)
+        rcx, rcz = O.latlon_to_rad(w.rec_lat, w.rec_lon)
+        rcr = np.asarray(w.rec_elev, dtype=np.float64)
+        _ORC_CACHE[key] = (w, g, veln, rcr, rcx, rcz)
+    return _ORC_CACHE[key]
+
+
 def _oracle_event(args):
-    """One serial fast-marching solve of one event (spawned worker)."""
-    cfg, scale, ev_index, nev = args
+    """One event on one core (spawned worker): serial fast marching, receiver
+    times and rays with Frechet rows (step forward) or the march alone (step
+    solve).  Returns the compute seconds; the setup is cached per worker."""
+    cfg, scale, ev_index, nev, step = args
     import oracle as O
     from fm3dt import synth
-    w = synth.config(cfg, scale=scale or None, nev=nev)
-    h = w.header
-    g = O.grid_from_header(h.nv, h.vorig, h.vstep, h.nn, h.norig, h.nstep, h.earth)
-    veln, _ = O.gridder(g, w.velv)
-    p = synth.planewave_params(h, *w.events[ev_index])
+    w, g, veln, rcr, rcx, rcz = _oracle_setup(cfg, scale, nev)
+    p = synth.planewave_params(w.header, *w.events[ev_index])
     fr = O.planewave_frame(g, O.PlaneWave(*p))
     t = time.perf_counter()
-    O.fmm(g, veln, fr, 1)
+    ttn, _ = O.fmm(g, veln, fr, 1)
+    if step == "forward":
+        O.srtimes(g, ttn, rcr, rcx, rcz)
+        O.rays(g, ttn, veln, rcr, rcx, rcz)
     return time.perf_counter() - t
 
 
-def cpu_sample(cfg, scale, nev, n_events, cores):
-    """Events across `cores` spawned processes; returns (solves/s, wall s)."""
-    import multiprocessing as mp
-    import oracle
-    oracle.build()
-    ctx = mp.get_context("spawn")
-    jobs = [(cfg, scale, i % nev, nev) for i in range(n_events)]
-    with ctx.Pool(cores) as pool:
-        pool.map(_oracle_event, jobs[:cores])          # warm the workers (imports, build check)
-        t = time.perf_counter()
-        pool.map(_oracle_event, jobs)
-        wall = time.perf_counter() - t
-    return n_events / wall, wall
+def _oracle_warm(args):
+    """Warm-up of a worker: imports, the oracle library and the workload's
+    setup (not timed)."""
+    cfg, scale, nev = args
+    _oracle_setup(cfg, scale, nev)
+    return 0.0
+
+
+class CpuPool:
+    """`cores` spawned worker processes, one event per core per step.  A
+    step's time is the slowest worker's compute time (all run at once)."""
+
+    def __init__(self, cfg, scale, nev, step, cores):
+        import multiprocessing as mp
+        import oracle
+        oracle.build()
+        self.cfg, self.scale, self.nev, self.step, self.cores = cfg, scale, nev, step, cores
+        self.pool = mp.get_context("spawn").Pool(cores)
+        self.pool.map(_oracle_warm, [(cfg, scale, nev)] * cores, chunksize=1)
+        self.next = 0
+
+    def sample(self):
+        """One step: `cores` events at once; returns (solves/s, step seconds)."""
+        jobs = [(self.cfg, self.scale, (self.next + i) % self.nev, self.nev, self.step) for i in range(self.cores)]
+        self.next += self.cores
+        secs = self.pool.map(_oracle_event, jobs, chunksize=1)
+        t = max(secs)
+        return self.cores / t, t
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part", "hardware")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 
 def run_reference(a):
     ws, rank, local = dist_env()
     if rank != 0:
         return 0
-    cfg, scale = a.config, a.scale
     from fm3dt import synth
-    w = synth.config(cfg, scale=scale or None, nev=a.events or None)
+    w = synth.config(a.config, scale=a.scale or None, nev=a.events or None)
     nev = len(w.events)
     cores = os.cpu_count() or 1
-    per_step = cores
+    pool = CpuPool(a.config, a.scale, nev, a.step, cores)
     for _ in range(a.warmup):
-        cpu_sample(cfg, scale, nev, per_step, cores)
-    vals, walls = [], []
+        pool.sample()
+    vals, secs = [], []
     for _ in range(a.steps):
-        v, wall = cpu_sample(cfg, scale, nev, per_step, cores)
+        v, t = pool.sample()
         vals.append(v)
-        walls.append(wall)
-    total = sum(walls)
-    value = a.steps * per_step / total
-    n = w.header.nn
+        secs.append(t)
+    pool.close()
+    total = sum(secs)
+    value = a.steps * cores / total
+    lat = sorted(1000.0 * t for t in secs)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": a.gpus,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000.0 * total / a.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"config{cfg}: {n[0]}x{n[1]}x{n[2]} grid, plane-wave events, serial fast marching "
-                               f"per event, events spread over {cores} host cores", "grid": list(n)},
+        "config": workload_config(a.config, a.step, w.header, nev, len(w.rec_elev), a.prec),
+        "p50_ms": lat[len(lat) // 2], "p99_ms": lat[-1],
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": f"{per_step} events per step x {a.steps} steps, one event per core "
-                                   f"(oracle C restatement of local_fmm; the Fortran/MPI reference cannot be "
-                                   f"built: no Fortran or MPI toolchain)"},
+                         "cpu_model": cpu_model(), "nproc": os.cpu_count(),
+                         "sample": f"{cores} events per step (one per core, at once) x {a.steps} steps; per event "
+                                   f"the oracle's serial fast marching (C restatement of local_fmm)"
+                                   + (", srtimes and parallel_rpaths" if a.step == "forward" else "") +
+                                   "; the step's time is its slowest core's compute time (set-up excluded); the "
+                                   "Fortran/MPI reference cannot be built: no Fortran or MPI toolchain"},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -260,6 +335,7 @@ def run_ours(a):
     h = w.header
     nev = len(w.events)
     nnr, nnx, nnz = h.nn
+    forward = a.step == "forward"
     # shard: the job holds ws x nev events; each rank solves its own share of
     # them (weak scaling), with no collective until the final gather
     mine = list(range(nev))
@@ -273,11 +349,19 @@ def run_ours(a):
     frames = synth.planewave_frames(h, params)
     rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat, w.rec_lon)
     rcr = np.ascontiguousarray(w.rec_elev, dtype=np.float64)
+    rcx = np.ascontiguousarray(rcx)
+    rcz = np.ascontiguousarray(rcz)
+    nrc = len(rcr)
+    nrows = nev * nrc
     prec = fm3dt.FP32_OFFSET if a.prec == "f32" else fm3dt.FP64
 
     solver = fm3dt.Solver(h, fom=1, precision=prec, max_events=nev)
     solver.set_velocity(w.velv)
     d_frames = torch.from_numpy(frames).cuda()
+    d_rec = [torch.from_numpy(x).cuda() for x in (rcr, rcx, rcz)]
+    rec_ptrs = [x.data_ptr() for x in d_rec]
+    d_times = torch.empty((nev, nrc), dtype=torch.float32, device="cuda")
+    d_rowptr = torch.empty(nrows + 1, dtype=torch.int64, device="cuda")
     torch.cuda.synchronize()
     fptr = d_frames.data_ptr()
     solver.set_sweep_segments(*a.segments)
@@ -288,20 +372,53 @@ def run_ours(a):
         solver.set_sweep_shape(sweep_shape)
         tuned = (a.shape, a.passes or 64, sweep_shape, None)
     else:
-        tuned = autotune.autotune(solver, fptr, nev, device=True)
+        # (tuned on up to 128 of the events: the choice never changes results)
+        tuned = autotune.autotune(solver, fptr, min(nev, 128), device=True)
     shape = fm3dt.tile_shapes()[tuned[0]]
     sweep_shape_dims = fm3dt.sweep_shapes()[tuned[2]]
 
-    for _ in range(a.warmup):
+    # the Frechet arrays, sized by one untimed forward pass
+    cap = 0
+    d_cols = d_vals = None
+    if forward:
         solver.solve_ptr(nev, fptr, True)
+        cap = solver.rays_frechet_device(nrc, *rec_ptrs, d_rowptr.data_ptr(), 1, 1, 0, strict=False)
+        cap = int(cap * 1.05) + 1024
+        d_cols = torch.empty(cap, dtype=torch.int32, device="cuda")
+        d_vals = torch.empty(cap, dtype=torch.float32, device="cuda")
+
+    phase = {"solve": [], "receivers": [], "rays": []}
+
+    def step_device():
+        t0 = time.perf_counter()
+        st = solver.solve_ptr(nev, fptr, True)
+        t1 = time.perf_counter()
+        if forward:
+            solver.receiver_times_device(nrc, *rec_ptrs, d_times.data_ptr())
+            t2 = time.perf_counter()
+            solver.rays_frechet_device(nrc, *rec_ptrs, d_rowptr.data_ptr(), d_cols.data_ptr(), d_vals.data_ptr(),
+                                       cap)
+            t3 = time.perf_counter()
+            phase["receivers"].append(1000.0 * (t2 - t1))
+            phase["rays"].append(1000.0 * (t3 - t2))
+        phase["solve"].append(1000.0 * (t1 - t0))
+        return st
+
+    for _ in range(a.warmup):
+        step_device()
+    for v in phase.values():
+        v.clear()
     clocks = Clocks(local if ws > 1 else 0) if rank == 0 else None
     d.barrier()
     torch.cuda.synchronize()
     l0 = solver.launch_count
     t0 = time.perf_counter()
-    sts = []
+    sts, lat = [], []
     for _ in range(a.steps):
-        sts.append(solver.solve_ptr(nev, fptr, True))
+        ts = time.perf_counter()
+        sts.append(step_device())
+        torch.cuda.synchronize()
+        lat.append(1000.0 * (time.perf_counter() - ts))
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     d.barrier()
@@ -311,10 +428,10 @@ def run_ours(a):
     trace_ms = [round(float(x), 4) for x in solver.round_trace_ms()]
     clk = clocks.stop() if clocks else None
     dev_ms = sum(s["ms"] for s in sts)
-    step_s = max(wall, dev_ms / 1000.0)
+    step_s = wall if forward else max(wall, dev_ms / 1000.0)
     step_s = d.max(step_s)
     value = ws * nev * a.steps / step_s
-    lat = sorted(s["ms"] for s in sts)
+    lat.sort()
     p50 = lat[len(lat) // 2]
     p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
     # The two solver kernels: the rounds (nodes of staged tiles) and the
@@ -353,8 +470,8 @@ def run_ours(a):
     achieved = k_nodes * B_NODE[a.prec] / (k_ms / 1000.0) / 1e9 if k_ms > 0 else 0.0
     peak, peak_kind = measured_peak_hbm()
     per_launch = all_nodes * B_NODE[a.prec] / max(1, k_launches)
-    # DRAM bytes per node processed, from the ncu capture of the small case
-    # (profiles/solver_kernels_small_case.md), times the nodes one launch
+    # DRAM bytes per node processed, from an ncu capture of a smaller case of
+    # the same kernel (KERNEL_DRAM_BYTES_PER_NODE), times the nodes one launch
     # processes here on average
     traffic = (KERNEL_DRAM_BYTES_PER_NODE[top] * all_nodes / max(1, k_launches)
                if top in KERNEL_DRAM_BYTES_PER_NODE and a.prec == "f32" else None)
@@ -369,58 +486,55 @@ def run_ours(a):
                  "inst_per_node": KERNEL_WARP_INST_PER_NODE[top], "sm_mhz": mhz}
 
     extras = {}
+    if forward:
+        extras["forward_ms_per_step"] = {k: statistics.median(v) for k, v in phase.items() if v}
+        extras["frechet_entries_per_step"] = int(d_rowptr[-1].item())
     if not a.no_extras:
-        # e2e through the public API with pinned host buffers
+        # e2e through the host entry points with pinned host buffers: frames
+        # and receivers in, receiver times and Frechet rows out, every step
         h_frames = torch.from_numpy(frames).pin_memory()
-        h_out = torch.empty((nev, len(rcr)), dtype=torch.float32).pin_memory()
-        solver.solve_ptr(nev, h_frames.data_ptr(), False)
-        solver.receiver_times_into(rcr, rcx, rcz, h_out.data_ptr())
-        d.barrier()
-        t0 = time.perf_counter()
-        for _ in range(a.steps):
+        h_out = torch.empty((nev, nrc), dtype=torch.float32).pin_memory()
+        h_rowptr = torch.empty(nrows + 1, dtype=torch.int64).pin_memory() if forward else None
+        h_cols = torch.empty(max(cap, 1), dtype=torch.int32).pin_memory() if forward else None
+        h_vals = torch.empty(max(cap, 1), dtype=torch.float32).pin_memory() if forward else None
+
+        def step_host():
             solver.solve_ptr(nev, h_frames.data_ptr(), False)
             solver.receiver_times_into(rcr, rcx, rcz, h_out.data_ptr())
+            if forward:
+                return solver.rays_frechet_into(rcr, rcx, rcz, h_rowptr.data_ptr(), h_cols.data_ptr(),
+                                                h_vals.data_ptr(), cap)
+            return 0
+
+        step_host()
+        d.barrier()
+        t0 = time.perf_counter()
+        entries = 0
+        for _ in range(a.steps):
+            entries = step_host()
         e2e_s = d.max(time.perf_counter() - t0)
         extras["e2e"] = {"value": ws * nev * a.steps / e2e_s, "unit": "solves/s",
-                         "h2d_bytes_per_step": int(frames.nbytes + 3 * rcr.nbytes),
-                         "d2h_bytes_per_step": int(h_out.numel() * 4)}
+                         "h2d_bytes_per_step": int(frames.nbytes + (2 if forward else 1) * 3 * rcr.nbytes),
+                         "d2h_bytes_per_step": int(h_out.numel() * 4 +
+                                                   ((nrows + 1) * 8 + entries * 8 if forward else 0))}
         trr32 = h_out.numpy().astype(np.float64).copy()
         # the job's one collective: receiver times of every rank's events to
         # rank 0 (host gather, after the timed region)
         got = shard.gather_to_root((mine, h_out.numpy().copy()), getattr(d, "dist", None))
         if rank == 0:
             extras["gathered_events"] = int(shard.merge_times(ws * nev, got).shape[0])
-        # error against the plain FP64 GPU path on a subset of events (untimed)
-        k = min(nev, 8)
-        with fm3dt.Solver(h, fom=1, precision=fm3dt.FP64, max_events=k) as s64:
-            s64.set_velocity(w.velv)
-            s64.solve(frames[:k])
-            t64 = s64.receiver_times(rcr, rcx, rcz).astype(np.float64)
-            # plain single-event FP64 path: solves/s, one event per solve
-            s64.solve(frames[:1])
-            t = time.perf_counter()
-            n1 = 3
-            for i in range(n1):
-                s64.solve(frames[i:i + 1])
-            plain = n1 / (time.perf_counter() - t)
-        rel = float(np.max(np.abs(trr32[:k] - t64) / t64))
-        ab = float(np.max(np.abs(trr32[:k] - t64)))
-        extras["error_vs_plain_fp64"] = {"max_rel": rel, "max_abs_s": ab, "events_checked": k}
-        extras["plain_fp64_single_event"] = {"value": plain, "unit": "solves/s"}
-        extras["speedup_vs_plain_fp64"] = value / ws / plain
+        if rank == 0:
+            extras.update(fp64_checks(a, h, w, fptr, frames, rcr, rcx, rcz, rec_ptrs, trr32, solver, d_rowptr,
+                                      d_cols, d_vals, cap, forward, value / ws))
 
+    # (tuning details and solver counters sit outside `config`, which both
+    # arms print alike)
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1000.0 * step_s / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": a.prec, "data": "synthetic",
-        "config": {"workload": f"config{a.config}: batched teleseismic plane-wave events, "
-                               f"{nnr}x{nnx}x{nnz} (r,theta,phi) grid, {nev} events per GPU, "
-                               f"{len(rcr)} receivers, {'FP32 offset' if a.prec == 'f32' else 'FP64'} stencils",
-                   "grid": [nnr, nnx, nnz], "events_per_gpu": nev, "receivers": len(rcr),
-                   "tile_shape": list(shape), "max_passes": tuned[1],
-                   "sweep_tile_shape": list(sweep_shape_dims),
-                   "l2": "inputs larger than L2 (traveltime fields %.1f GB per step)" %
-                         (nev * nnr * nnx * nnz * (4 if a.prec == 'f32' else 8) / 1e9)},
+        "config": workload_config(a.config, a.step, h, nev, nrc, a.prec),
+        "tuning": {"tile_shape": list(shape), "max_passes": tuned[1], "sweep_tile_shape": list(sweep_shape_dims)},
         "p50_ms": p50, "p99_ms": p99,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -445,15 +559,125 @@ def run_ours(a):
         line["clocks"] = clk
     if rank == 0 and ws == 1 and not a.no_extras:
         cores = os.cpu_count() or 1
-        v, wall = cpu_sample(a.config, a.scale, nev, cores, cores)
+        pool = CpuPool(a.config, a.scale, nev, a.step, cores)
+        v, t = pool.sample()
+        pool.close()
         line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
-                                "sample": f"{cores} events of this workload, one per core, serial fast "
-                                          f"marching (oracle restatement of local_fmm), {wall:.1f} s"}
+                                "cpu_model": cpu_model(), "nproc": os.cpu_count(),
+                                "sample": f"{cores} events of this workload at once, one per core: the oracle's "
+                                          f"serial fast marching (restatement of local_fmm)"
+                                          + (", srtimes and parallel_rpaths" if forward else "") +
+                                          f"; {t:.1f} s for the slowest core (set-up excluded)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     solver.close()
     d.close()
     return 0
+
+
+def fp64_checks(a, h, w, fptr, frames, rcr, rcx, rcz, rec_ptrs, trr32, solver, d_rowptr, d_cols, d_vals, cap,
+                forward, value_per_gpu):
+    """Untimed against the run: the plain FP64 GPU path on the same workload.
+    (1) the plain single-event FP64 path, one event per call (>= 10 calls);
+    (2) the batched FP64 path on 64 events; (3) the FP32 line's receiver
+    times, ray end points and Frechet rows against (2) on those events."""
+    import numpy as np
+    import torch
+    import fm3dt
+    nev = len(frames)
+    nrc = len(rcr)
+    k = min(nev, 64)
+    out = {}
+    d_t64 = torch.empty((k, nrc), dtype=torch.float32, device="cuda")
+    d_rp64 = torch.empty(k * nrc + 1, dtype=torch.int64, device="cuda")
+    d_end64 = torch.empty((k * nrc, 3), dtype=torch.float64, device="cuda")
+    with fm3dt.Solver(h, fom=1, precision=fm3dt.FP64, max_events=k) as s64:
+        s64.set_velocity(w.velv)
+        s64.solve_ptr(k, fptr, True)
+        cap64 = s64.rays_frechet_device(nrc, *rec_ptrs, d_rp64.data_ptr(), 1, 1, 0, strict=False) + 1024
+        d_c64 = torch.empty(cap64, dtype=torch.int32, device="cuda")
+        d_v64 = torch.empty(cap64, dtype=torch.float32, device="cuda")
+
+        def step64():
+            s64.solve_ptr(k, fptr, True)
+            s64.receiver_times_device(nrc, *rec_ptrs, d_t64.data_ptr())
+            if forward:
+                s64.rays_frechet_device(nrc, *rec_ptrs, d_rp64.data_ptr(), d_c64.data_ptr(), d_v64.data_ptr(),
+                                        cap64, d_end64.data_ptr())
+
+        step64()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(2):
+            step64()
+        torch.cuda.synchronize()
+        out["fp64_batched"] = {"value": 2 * k / (time.perf_counter() - t), "unit": "solves/s", "events": k,
+                               "step": a.step}
+        t64 = d_t64.cpu().numpy().astype(np.float64)
+        rel = float(np.max(np.abs(trr32[:k] - t64) / t64))
+        ab = float(np.max(np.abs(trr32[:k] - t64)))
+        out["error_vs_plain_fp64"] = {"max_rel": rel, "max_abs_s": ab, "events_checked": k,
+                                      "receivers": nrc, "pairs_checked": k * nrc}
+        if forward:
+            # the FP32 line's rays and rows for the same events
+            d_end32 = torch.empty((nev * nrc, 3), dtype=torch.float64, device="cuda")
+            solver.rays_frechet_device(nrc, *rec_ptrs, d_rowptr.data_ptr(), d_cols.data_ptr(), d_vals.data_ptr(),
+                                       cap, d_end32.data_ptr())
+            e32 = d_end32[:k * nrc].cpu().numpy()
+            e64 = d_end64.cpu().numpy()
+            dn = np.array([h.nstep[0], math.radians(h.nstep[1]), math.radians(h.nstep[2])])
+            cells = float(np.max(np.abs(e32 - e64) / dn[None, :]))
+            rows = _row_differences(d_rowptr, d_cols, d_vals, d_rp64, d_c64, d_v64, k * nrc)
+            out["rays_vs_plain_fp64"] = {"endpoint_max_cells": cells, "frechet_row": rows}
+    # plain single-event FP64 path: one event per call, solve + receivers (+ rays)
+    n1 = 10
+    with fm3dt.Solver(h, fom=1, precision=fm3dt.FP64, max_events=1) as s1:
+        s1.set_velocity(w.velv)
+        fbytes = frames[0].nbytes
+
+        def one(i):
+            s1.solve_ptr(1, fptr + i * fbytes, True)
+            s1.receiver_times_device(nrc, *rec_ptrs, d_t64.data_ptr())
+            if forward:
+                s1.rays_frechet_device(nrc, *rec_ptrs, d_rp64.data_ptr(), d_c64.data_ptr(), d_v64.data_ptr(), cap64)
+
+        one(0)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for i in range(n1):
+            one(i % nev)
+        torch.cuda.synchronize()
+        plain = n1 / (time.perf_counter() - t)
+    out["plain_fp64_single_event"] = {"value": plain, "unit": "solves/s", "calls": n1, "step": a.step}
+    out["speedup_vs_plain_fp64"] = value_per_gpu / plain
+    return out
+
+
+def _row_differences(rp32, c32, v32, rp64, c64, v64, nrows):
+    """Per-row Frechet differences between two CSR matrices (first nrows rows):
+    the largest entry difference over the row's largest entry, and the 2-norm
+    ratio; their median, 99th percentile and maximum, and the share of rows
+    within 1e-4 by both."""
+    import numpy as np
+    import scipy.sparse as sp
+    n32 = int(rp32[nrows].item())
+    n64 = int(rp64[nrows].item())
+    nmp = int(max(c32[:n32].max().item(), c64[:n64].max().item()))
+    A = sp.csr_matrix((v32[:n32].cpu().numpy().astype(np.float64), c32[:n32].cpu().numpy() - 1,
+                       rp32[:nrows + 1].cpu().numpy()), shape=(nrows, nmp))
+    B = sp.csr_matrix((v64[:n64].cpu().numpy().astype(np.float64), c64[:n64].cpu().numpy() - 1,
+                       rp64[:nrows + 1].cpu().numpy()), shape=(nrows, nmp))
+    D = (A - B).tocsr()
+    bmax = np.asarray(abs(B).max(axis=1).todense()).ravel()
+    dmax = np.asarray(abs(D).max(axis=1).todense()).ravel()
+    bl2 = np.sqrt(np.asarray(B.multiply(B).sum(axis=1)).ravel())
+    dl2 = np.sqrt(np.asarray(D.multiply(D).sum(axis=1)).ravel())
+    ok = bmax > 0
+    rmax = dmax[ok] / bmax[ok]
+    rl2 = dl2[ok] / bl2[ok]
+    q = lambda x: {"p50": float(np.percentile(x, 50)), "p99": float(np.percentile(x, 99)), "max": float(x.max())}
+    return {"max_entry_rel": q(rmax), "l2_rel": q(rl2), "rows": int(ok.sum()),
+            "rows_within_1e-4": float(np.mean((rmax <= 1e-4) & (rl2 <= 1e-4)))}
 
 
 def run_serving(a):

@@ -154,8 +154,12 @@ int fm3dt_receiver_times(fm3dt_ctx *ctx, int nrc, const double *rcr, const doubl
  * Limits: nrc <= 4096 and nev * nrc <= 262144 per call, else FM3DT_EINVAL.
  * The first call on a device looks up that array's device address (once per
  * device, with the device current); make that first call before capturing
- * any stream.  All calls share the array: calls whose GPU work overlaps
- * (other streams or contexts on the same device) race on it. */
+ * any stream.  The looked-up address is kept for the life of the process and
+ * is not refreshed after cudaDeviceReset: a host that resets a device must not
+ * call this entry point on that device again.  All calls share the array:
+ * calls whose GPU work overlaps (other streams or contexts on the same device)
+ * race on it.  A receiver outside the grid (or with a non-finite coordinate)
+ * gives FM3DT_ERANGE and leaves `out` unwritten, as fm3dt_receiver_times does. */
 int fm3dt_receiver_times_noalloc(fm3dt_ctx *ctx, int nrc, const double *rcr, const double *rcx,
                                  const double *rcz, float *out);
 
@@ -170,10 +174,28 @@ int fm3dt_receiver_times_noalloc(fm3dt_ctx *ctx, int nrc, const double *rcr, con
  * cols/vals; if the rows need more, FM3DT_ERANGE is returned with
  * row_ptr[nev*nrc] = the required count.  endpoints (nullable): nev*nrc*3
  * doubles (height km, colat rad, lon rad).  Pass cols = vals = NULL and
- * cap = 0 to trace rays only. */
+ * cap = 0 to trace rays only.  FM3DT_ERANGE if a receiver lies outside the
+ * grid (or has a non-finite coordinate) or a ray's B-spline support leaves
+ * the velocity grid. */
 int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double *rcx,
                        const double *rcz, int64_t *row_ptr, int32_t *cols, float *vals,
                        int64_t cap, double *endpoints);
+
+/* Device-memory forms of fm3dt_receiver_times and fm3dt_rays_frechet, for a
+ * tomography loop that keeps receivers, times and the Frechet matrix on the
+ * GPU between iterations (the reference writes them to rtravel.out and
+ * frechet.out, F:6503-6599, 7174-7176).  Every array argument is a device
+ * pointer except *total.  fm3dt_receiver_times_device writes nev x nrc floats
+ * to d_out.  fm3dt_rays_frechet_device writes nev*nrc+1 row pointers to
+ * d_row_ptr (formed on the device), the entry count to *total, and the rows
+ * to d_cols/d_vals when *total <= cap (FM3DT_ERANGE otherwise, rows not
+ * written); d_endpoints is nullable; d_cols = d_vals = NULL traces rays only.
+ * Both return after the GPU work has finished. */
+int fm3dt_receiver_times_device(fm3dt_ctx *ctx, int nrc, const double *d_rcr, const double *d_rcx,
+                                const double *d_rcz, float *d_out);
+int fm3dt_rays_frechet_device(fm3dt_ctx *ctx, int nrc, const double *d_rcr, const double *d_rcx,
+                              const double *d_rcz, int64_t *d_row_ptr, int32_t *d_cols, float *d_vals,
+                              int64_t cap, int64_t *total, double *d_endpoints);
 
 /* Copies the solved traveltime field of one event to the host: nnr*nnx*nnz
  * doubles, phi fastest (absolute seconds in both precisions; unreached nodes

@@ -42,6 +42,29 @@ int fail(fm3dt_ctx *ctx, int code, const std::string &msg)
             return fail(ctx, FM3DT_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
     } while (0)
 
+// Device buffers of one call, allocated on the context's stream and freed
+// (stream-ordered) on every return path.
+struct DeviceScratch {
+    cudaStream_t s;
+    std::vector<void *> bufs;
+    explicit DeviceScratch(cudaStream_t st) : s(st) {}
+    DeviceScratch(const DeviceScratch &) = delete;
+    DeviceScratch &operator=(const DeviceScratch &) = delete;
+    template <typename T>
+    cudaError_t alloc(T **p, size_t n)
+    {
+        *p = nullptr;
+        if (n == 0) return cudaSuccess;
+        cudaError_t e = cudaMallocAsync((void **)p, n * sizeof(T), s);
+        if (e == cudaSuccess) bufs.push_back((void *)*p);
+        return e;
+    }
+    ~DeviceScratch()
+    {
+        for (void *p : bufs) cudaFreeAsync(p, s);
+    }
+};
+
 // fm3dt_parallel.f90:61 initialises the double-precision pi from a
 // default-kind (single precision) literal; the converted angles use that value.
 double ref_pi() { return (double)3.1415926535898f; }
@@ -792,6 +815,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         st->sweep_launches = sweep_launches;
         st->sweep_nodes = sweep_nodes;
     }
+    if (kerr == 2) return fail(ctx, FM3DT_ECUDA, "a tile copy (TMA) destination was not 128-byte aligned");
     if (kerr) return fail(ctx, FM3DT_ECUDA, "a tile copy (TMA) did not complete in time");
     if (!done) return fail(ctx, FM3DT_ENOCONV, "solver round limit reached before convergence");
     return FM3DT_OK;
@@ -1030,14 +1054,14 @@ int fm3dt_solve_point(fm3dt_ctx *ctx, int nev, const double *src, int refine, in
     ctx->launches += 1;
     if (!refine) {
         PointSource *d_src = nullptr;
-        CK(cudaMallocAsync(&d_src, nev * sizeof(PointSource), s));
+        DeviceScratch sc(s);
+        CK(sc.alloc(&d_src, (size_t)nev));
         CK(cudaMemcpyAsync(d_src, ps.data(), nev * sizeof(PointSource), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->d_box, box.data(), box.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->d_box_init, box.data(), box.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         launch_point_analytic(g, ctx->prec, ctx->d_veln, nev, d_src, ctx->d_box, ctx->d_T, s);
         ctx->launches += 1;
         CKL();
-        CK(cudaFreeAsync(d_src, s));
     } else {
         CK(cudaStreamSynchronize(s));
         for (int e = 0; e < nev; ++e) {
@@ -1090,11 +1114,11 @@ int fm3dt_solve_point(fm3dt_ctx *ctx, int nev, const double *src, int refine, in
             CK(cudaMemcpyAsync(fc->d_box, fb, sizeof fb, cudaMemcpyHostToDevice, fc->stream));
             CK(cudaMemcpyAsync(fc->d_box_init, fb, sizeof fb, cudaMemcpyHostToDevice, fc->stream));
             PointSource *d_src = nullptr;
-            CK(cudaMallocAsync(&d_src, sizeof(PointSource), fc->stream));
+            DeviceScratch sc(fc->stream);
+            CK(sc.alloc(&d_src, 1));
             CK(cudaMemcpyAsync(d_src, &ps[e], sizeof(PointSource), cudaMemcpyHostToDevice, fc->stream));
             launch_point_analytic(fg, fc->prec, fc->d_veln, 1, d_src, fc->d_box, fc->d_T, fc->stream);
             fc->launches += 4;
-            CK(cudaFreeAsync(d_src, fc->stream));
             fm3dt_status fst{};
             rc = solve_common(fc, 1, &fst, kPoint);
             ctx->launches += fc->launches;
@@ -1122,68 +1146,68 @@ int fm3dt_receiver_times(fm3dt_ctx *ctx, int nrc, const double *rcr, const doubl
     const Geom &g = ctx->g;
     std::vector<RecCell> cells(nrc);
     for (int i = 0; i < nrc; ++i) {
-        // F:7066-7097 with the last-subdomain clamp of F:7069-7070
         RecCell c;
-        c.irr = (int)std::floor((g.rgor - rcr[i]) / g.dnr) + 1;
-        c.irx = (int)std::floor((rcx[i] - g.rgox) / g.dnx) + 1;
-        c.irz = (int)std::floor((rcz[i] - g.rgoz) / g.dnz) + 1;
-        c.pad = 0;
-        if (c.irx == g.nnx) c.irx--;
-        if (c.irz == g.nnz) c.irz--;
-        if (c.irr < 1 || c.irr >= g.nnr || c.irx < 1 || c.irx >= g.nnx || c.irz < 1 || c.irz >= g.nnz)
+        if (!locate_receiver(g, rcr[i], rcx[i], rcz[i], c))
             return fail(ctx, FM3DT_ERANGE, "receiver " + std::to_string(i + 1) + " lies outside the grid");
-        c.drx = (rcx[i] - g.rgox) - (double)(c.irx - 1) * g.dnx;
-        c.drz = (rcz[i] - g.rgoz) - (double)(c.irz - 1) * g.dnz;
-        c.drr = (g.rgor - rcr[i]) - (double)(c.irr - 1) * g.dnr;
         cells[i] = c;
     }
     RecCell *d_cells = nullptr;
     float *d_out = nullptr;
     const int nev = ctx->nev_solved;
-    CK(cudaMallocAsync(&d_cells, nrc * sizeof(RecCell), ctx->stream));
-    CK(cudaMallocAsync(&d_out, (size_t)nev * nrc * sizeof(float), ctx->stream));
+    DeviceScratch sc(ctx->stream);
+    CK(sc.alloc(&d_cells, (size_t)nrc));
+    CK(sc.alloc(&d_out, (size_t)nev * nrc));
     CK(cudaMemcpyAsync(d_cells, cells.data(), nrc * sizeof(RecCell), cudaMemcpyHostToDevice, ctx->stream));
     launch_receivers(g, ctx->prec, ctx->d_T, ctx->d_base, nev, nrc, d_cells, d_out, ctx->stream);
     ctx->launches += 1;
     CKL();
     CK(cudaMemcpyAsync(out, d_out, (size_t)nev * nrc * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaFreeAsync(d_cells, ctx->stream));
-    CK(cudaFreeAsync(d_out, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return FM3DT_OK;
 }
 
-int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double *rcx, const double *rcz,
-                       int64_t *row_ptr, int32_t *cols, float *vals, int64_t cap, double *endpoints)
+int fm3dt_receiver_times_device(fm3dt_ctx *ctx, int nrc, const double *d_rcr, const double *d_rcx,
+                                const double *d_rcz, float *d_out)
 {
-    if (!ctx || nrc < 0 || (nrc > 0 && (!rcr || !rcx || !rcz))) return FM3DT_EINVAL;
+    if (!ctx || nrc < 0 || (nrc > 0 && (!d_rcr || !d_rcx || !d_rcz || !d_out))) return FM3DT_EINVAL;
     if (ctx->nev_solved < 1) return fail(ctx, FM3DT_ESTATE, "no solved events");
-    if (!ctx->have_velocity) return fail(ctx, FM3DT_ESTATE, "no velocity model");
-    if (ctx->last_point)
-        return fail(ctx, FM3DT_ESTATE, "rays are traced through teleseismic (boundary-frame) solves only");
-    const bool want_rows = cols != nullptr && vals != nullptr;
-    if (want_rows && !row_ptr) return FM3DT_EINVAL;
     if (nrc == 0) return FM3DT_OK;
+    cudaStream_t s = ctx->stream;
+    DeviceScratch sc(s);
+    int *d_bad = nullptr;
+    CK(sc.alloc(&d_bad, 1));
+    CK(cudaMemsetAsync(d_bad, 0x7f, sizeof(int), s));           // 0x7f7f7f7f: none
+    launch_receivers_located(ctx->g, ctx->prec, ctx->d_T, ctx->d_base, ctx->nev_solved, nrc, d_rcr, d_rcx, d_rcz,
+                             d_bad, d_out, s);
+    ctx->launches += 1;
+    CKL();
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (bad != 0x7f7f7f7f)
+        return fail(ctx, FM3DT_ERANGE, "receiver " + std::to_string(bad + 1) + " lies outside the grid");
+    return FM3DT_OK;
+}
+
+// Rays of every solved event from receivers in device memory.  Traces the
+// rays (end points to d_end when not null) and, when rows are wanted, forms
+// the row pointers on the device (d_row_ptr, nrows + 1) and returns the entry
+// count in *total; the caller then compacts the rows with rays_compact.
+static int rays_trace(fm3dt_ctx *ctx, DeviceScratch &sc, int nrc, const double *d_rcr, const double *d_rcx,
+               const double *d_rcz, bool want_rows, double *d_end, int64_t *d_row_ptr, int64_t *total,
+               float **d_fdm_out)
+{
     const Geom &g = ctx->g;
     const int nev = ctx->nev_solved;
     const int nrows = nev * nrc;
     const size_t nmp = (size_t)(g.nvr + 2) * (g.nvx + 2) * (g.nvz + 2);
     cudaStream_t s = ctx->stream;
-    double *d_rec = nullptr, *d_end = nullptr;
-    int *d_steps = nullptr, *d_status = nullptr;
     float *d_fdm = nullptr;
-    int64_t *d_counts = nullptr, *d_rowptr = nullptr;
-    int32_t *d_cols = nullptr;
-    float *d_vals = nullptr;
-    CK(cudaMallocAsync(&d_rec, 3 * (size_t)nrc * sizeof(double), s));
-    CK(cudaMallocAsync(&d_end, 3 * (size_t)nrows * sizeof(double), s));
-    CK(cudaMallocAsync(&d_steps, (size_t)nrows * sizeof(int), s));
-    CK(cudaMallocAsync(&d_status, (size_t)nrows * sizeof(int), s));
-    CK(cudaMemcpyAsync(d_rec, rcr, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(d_rec + nrc, rcx, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(d_rec + 2 * nrc, rcz, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
+    int *d_flags = nullptr;
+    CK(sc.alloc(&d_flags, 2));
+    CK(cudaMemsetAsync(d_flags, 0x7f, 2 * sizeof(int), s));     // 0x7f7f7f7f: no ray flagged
     if (want_rows) {
-        CK(cudaMallocAsync(&d_fdm, (size_t)nrows * nmp * sizeof(float), s));
+        CK(sc.alloc(&d_fdm, (size_t)nrows * nmp));
         CK(cudaMemsetAsync(d_fdm, 0, (size_t)nrows * nmp * sizeof(float), s));
     }
     RayArgs ra;
@@ -1193,43 +1217,105 @@ int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double 
     ra.veln = ctx->d_veln;
     ra.nev = nev;
     ra.nrc = nrc;
-    ra.rcr = d_rec;
-    ra.rcx = d_rec + nrc;
-    ra.rcz = d_rec + 2 * nrc;
+    ra.rcr = d_rcr;
+    ra.rcx = d_rcx;
+    ra.rcz = d_rcz;
     ra.fdm = d_fdm;
     ra.endpoints = d_end;
-    ra.nsteps = d_steps;
-    ra.status = d_status;
+    ra.nsteps = nullptr;
+    ra.flags = d_flags;
     launch_rays(ra, s);
     ctx->launches += 1;
     CKL();
-    std::vector<int> status(nrows);
-    CK(cudaMemcpyAsync(status.data(), d_status, nrows * sizeof(int), cudaMemcpyDeviceToHost, s));
+    *total = 0;
+    if (want_rows) {
+        int64_t *d_counts = nullptr, *d_chunks = nullptr;
+        CK(sc.alloc(&d_counts, (size_t)nrows));
+        CK(sc.alloc(&d_chunks, (size_t)scan_chunks(nrows)));
+        launch_row_counts(d_fdm, nrows, (int)nmp, d_counts, s);
+        launch_row_scan(d_counts, nrows, d_row_ptr, d_chunks, s);
+        ctx->launches += 4;
+        CKL();
+        CK(cudaMemcpyAsync(total, d_row_ptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    }
+    int flags[2] = {0, 0};
+    CK(cudaMemcpyAsync(flags, d_flags, sizeof flags, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (flags[1] != 0x7f7f7f7f)
+        return fail(ctx, FM3DT_ERANGE, "ray " + std::to_string(flags[1]) + ": receiver " +
+                                           std::to_string(flags[1] % nrc + 1) + " lies outside the grid");
+    if (flags[0] != 0x7f7f7f7f)
+        return fail(ctx, FM3DT_ERANGE, "ray " + std::to_string(flags[0]) +
+                                           ": B-spline support outside the velocity grid");
+    *d_fdm_out = d_fdm;
+    return FM3DT_OK;
+}
+
+static int rays_compact(fm3dt_ctx *ctx, const float *d_fdm, int nrows, const int64_t *d_row_ptr, int32_t *d_cols,
+                 float *d_vals)
+{
+    const Geom &g = ctx->g;
+    const size_t nmp = (size_t)(g.nvr + 2) * (g.nvx + 2) * (g.nvz + 2);
+    launch_row_compact(d_fdm, nrows, (int)nmp, d_row_ptr, d_cols, d_vals, ctx->stream);
+    ctx->launches += 1;
+    CKL();
+    return FM3DT_OK;
+}
+
+static int rays_ready(fm3dt_ctx *ctx)
+{
+    if (ctx->nev_solved < 1) return fail(ctx, FM3DT_ESTATE, "no solved events");
+    if (!ctx->have_velocity) return fail(ctx, FM3DT_ESTATE, "no velocity model");
+    if (ctx->last_point)
+        return fail(ctx, FM3DT_ESTATE, "rays are traced through teleseismic (boundary-frame) solves only");
+    return FM3DT_OK;
+}
+
+int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double *rcx, const double *rcz,
+                       int64_t *row_ptr, int32_t *cols, float *vals, int64_t cap, double *endpoints)
+{
+    if (!ctx || nrc < 0 || (nrc > 0 && (!rcr || !rcx || !rcz))) return FM3DT_EINVAL;
+    int rc = rays_ready(ctx);
+    if (rc != FM3DT_OK) return rc;
+    const bool want_rows = cols != nullptr && vals != nullptr;
+    if (want_rows && !row_ptr) return FM3DT_EINVAL;
+    if (nrc == 0) return FM3DT_OK;
+    for (int i = 0; i < nrc; ++i) {
+        RecCell c;
+        if (!locate_receiver(ctx->g, rcr[i], rcx[i], rcz[i], c))
+            return fail(ctx, FM3DT_ERANGE, "receiver " + std::to_string(i + 1) + " lies outside the grid");
+    }
+    const int nrows = ctx->nev_solved * nrc;
+    cudaStream_t s = ctx->stream;
+    DeviceScratch sc(s);
+    double *d_rec = nullptr, *d_end = nullptr;
+    int64_t *d_rowptr = nullptr;
+    CK(sc.alloc(&d_rec, 3 * (size_t)nrc));
+    if (endpoints) CK(sc.alloc(&d_end, 3 * (size_t)nrows));
+    if (want_rows) CK(sc.alloc(&d_rowptr, (size_t)nrows + 1));
+    CK(cudaMemcpyAsync(d_rec, rcr, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_rec + nrc, rcx, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_rec + 2 * nrc, rcz, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
+    int64_t total = 0;
+    float *d_fdm = nullptr;
+    rc = rays_trace(ctx, sc, nrc, d_rec, d_rec + nrc, d_rec + 2 * nrc, want_rows, d_end, d_rowptr, &total, &d_fdm);
+    if (rc != FM3DT_OK) return rc;
     if (endpoints)
         CK(cudaMemcpyAsync(endpoints, d_end, 3 * (size_t)nrows * sizeof(double), cudaMemcpyDeviceToHost, s));
-    int rc = FM3DT_OK;
     if (want_rows) {
-        CK(cudaMallocAsync(&d_counts, (size_t)nrows * sizeof(int64_t), s));
-        launch_row_counts(d_fdm, nrows, (int)nmp, d_counts, s);
-        ctx->launches += 1;
-        CKL();
-        std::vector<int64_t> counts(nrows);
-        CK(cudaMemcpyAsync(counts.data(), d_counts, nrows * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        row_ptr[0] = 0;
-        for (int q = 0; q < nrows; ++q) row_ptr[q + 1] = row_ptr[q] + counts[q];
-        const int64_t total = row_ptr[nrows];
+        CK(cudaMemcpyAsync(row_ptr, d_rowptr, ((size_t)nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         if (total > cap) {
-            rc = fail(ctx, FM3DT_ERANGE, "Frechet rows need " + std::to_string(total) + " entries, capacity " +
-                                             std::to_string(cap));
-        } else if (total > 0) {
-            CK(cudaMallocAsync(&d_rowptr, (size_t)(nrows + 1) * sizeof(int64_t), s));
-            CK(cudaMallocAsync(&d_cols, (size_t)total * sizeof(int32_t), s));
-            CK(cudaMallocAsync(&d_vals, (size_t)total * sizeof(float), s));
-            CK(cudaMemcpyAsync(d_rowptr, row_ptr, (nrows + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
-            launch_row_compact(d_fdm, nrows, (int)nmp, d_rowptr, d_cols, d_vals, s);
-            ctx->launches += 1;
-            CKL();
+            CK(cudaStreamSynchronize(s));
+            return fail(ctx, FM3DT_ERANGE, "Frechet rows need " + std::to_string(total) + " entries, capacity " +
+                                               std::to_string(cap));
+        }
+        if (total > 0) {
+            int32_t *d_cols = nullptr;
+            float *d_vals = nullptr;
+            CK(sc.alloc(&d_cols, (size_t)total));
+            CK(sc.alloc(&d_vals, (size_t)total));
+            rc = rays_compact(ctx, d_fdm, nrows, d_rowptr, d_cols, d_vals);
+            if (rc != FM3DT_OK) return rc;
             CK(cudaMemcpyAsync(cols, d_cols, (size_t)total * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
             CK(cudaMemcpyAsync(vals, d_vals, (size_t)total * sizeof(float), cudaMemcpyDeviceToHost, s));
         }
@@ -1237,22 +1323,40 @@ int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double 
         for (int q = 0; q <= nrows; ++q) row_ptr[q] = 0;
     }
     CK(cudaStreamSynchronize(s));
-    cudaFreeAsync(d_rec, s);
-    cudaFreeAsync(d_end, s);
-    cudaFreeAsync(d_steps, s);
-    cudaFreeAsync(d_status, s);
-    if (d_fdm) cudaFreeAsync(d_fdm, s);
-    if (d_counts) cudaFreeAsync(d_counts, s);
-    if (d_rowptr) cudaFreeAsync(d_rowptr, s);
-    if (d_cols) cudaFreeAsync(d_cols, s);
-    if (d_vals) cudaFreeAsync(d_vals, s);
-    CK(cudaStreamSynchronize(s));
-    if (rc == FM3DT_OK)
-        for (int q = 0; q < nrows; ++q)
-            if (status[q])
-                return fail(ctx, FM3DT_ERANGE, "ray " + std::to_string(q) +
-                                                   ": B-spline support outside the velocity grid");
-    return rc;
+    return FM3DT_OK;
+}
+
+int fm3dt_rays_frechet_device(fm3dt_ctx *ctx, int nrc, const double *d_rcr, const double *d_rcx,
+                              const double *d_rcz, int64_t *d_row_ptr, int32_t *d_cols, float *d_vals, int64_t cap,
+                              int64_t *total, double *d_endpoints)
+{
+    if (!ctx || nrc < 0 || (nrc > 0 && (!d_rcr || !d_rcx || !d_rcz))) return FM3DT_EINVAL;
+    int rc = rays_ready(ctx);
+    if (rc != FM3DT_OK) return rc;
+    const bool want_rows = d_cols != nullptr && d_vals != nullptr;
+    if (want_rows && (!d_row_ptr || !total)) return FM3DT_EINVAL;
+    if (total) *total = 0;
+    if (nrc == 0) return FM3DT_OK;
+    const int nrows = ctx->nev_solved * nrc;
+    DeviceScratch sc(ctx->stream);
+    int64_t n = 0;
+    float *d_fdm = nullptr;
+    rc = rays_trace(ctx, sc, nrc, d_rcr, d_rcx, d_rcz, want_rows, d_endpoints, d_row_ptr, &n, &d_fdm);
+    if (rc != FM3DT_OK) return rc;
+    if (!want_rows) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        return FM3DT_OK;
+    }
+    *total = n;
+    if (n > cap)
+        return fail(ctx, FM3DT_ERANGE, "Frechet rows need " + std::to_string(n) + " entries, capacity " +
+                                           std::to_string(cap));
+    if (n > 0) {
+        rc = rays_compact(ctx, d_fdm, nrows, d_row_ptr, d_cols, d_vals);
+        if (rc != FM3DT_OK) return rc;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FM3DT_OK;
 }
 
 int fm3dt_get_times(fm3dt_ctx *ctx, int event, double *ttn)
@@ -1260,13 +1364,13 @@ int fm3dt_get_times(fm3dt_ctx *ctx, int event, double *ttn)
     if (!ctx || !ttn) return FM3DT_EINVAL;
     if (event < 0 || event >= ctx->nev_solved) return fail(ctx, FM3DT_EINVAL, "event not solved");
     double *d_out = nullptr;
-    CK(cudaMallocAsync(&d_out, ctx->N * sizeof(double), ctx->stream));
+    DeviceScratch sc(ctx->stream);
+    CK(sc.alloc(&d_out, ctx->N));
     const double base = ctx->prec == FM3DT_FP64 ? 0.0 : ctx->h_base[event];
     launch_to_absolute(ctx->g, ctx->prec, ctx->d_T, (size_t)event * ctx->N, base, d_out, ctx->stream);
     ctx->launches += 1;
     CKL();
     CK(cudaMemcpyAsync(ttn, d_out, ctx->N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaFreeAsync(d_out, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return FM3DT_OK;
 }
@@ -1297,14 +1401,14 @@ int fm3dt_set_times(fm3dt_ctx *ctx, int event, int nev_total, const double *ttn)
     if ((int)ctx->h_base.size() < nev_total) ctx->h_base.resize(nev_total, 0.0);
     ctx->h_base[event] = base;
     double *d_in = nullptr;
-    CK(cudaMallocAsync(&d_in, ctx->N * sizeof(double), ctx->stream));
+    DeviceScratch sc(ctx->stream);
+    CK(sc.alloc(&d_in, ctx->N));
     CK(cudaMemcpyAsync(d_in, ttn, ctx->N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     launch_from_absolute(ctx->g, ctx->prec, d_in, base, ctx->d_T, (size_t)event * ctx->N, ctx->stream);
     ctx->launches += 1;
     CKL();
     CK(cudaMemcpyAsync(ctx->d_base + event, &ctx->h_base[event], sizeof(double), cudaMemcpyHostToDevice,
                        ctx->stream));
-    CK(cudaFreeAsync(d_in, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->nev_solved = nev_total;
     return FM3DT_OK;

@@ -185,8 +185,37 @@ void launch_point_sample(int prec, const void *Tf, int nnx_f, int nnz_f, int ref
 
 // receivers.cu
 struct RecCell { int irr, irx, irz, pad; double drr, drx, drz; };
+// Cell of a receiver and its offsets in it (F:7066-7097, with the
+// last-subdomain clamp of F:7069-7070).  The cell indices are formed and
+// range-checked in double precision before any conversion to int, so a NaN,
+// infinite or huge coordinate is rejected (false) instead of converting with
+// undefined behaviour.
+__host__ __device__ inline bool locate_receiver(const Geom &g, double rcr, double rcx, double rcz, RecCell &c)
+{
+    const double fr = floor((g.rgor - rcr) / g.dnr) + 1.0;
+    double fx = floor((rcx - g.rgox) / g.dnx) + 1.0;
+    double fz = floor((rcz - g.rgoz) / g.dnz) + 1.0;
+    if (fx == (double)g.nnx) fx -= 1.0;
+    if (fz == (double)g.nnz) fz -= 1.0;
+    // (every comparison with NaN is false)
+    if (!(fr >= 1.0 && fr < (double)g.nnr && fx >= 1.0 && fx < (double)g.nnx && fz >= 1.0 && fz < (double)g.nnz))
+        return false;
+    c.irr = (int)fr;
+    c.irx = (int)fx;
+    c.irz = (int)fz;
+    c.pad = 0;
+    c.drx = (rcx - g.rgox) - (double)(c.irx - 1) * g.dnx;
+    c.drz = (rcz - g.rgoz) - (double)(c.irz - 1) * g.dnz;
+    c.drr = (g.rgor - rcr) - (double)(c.irr - 1) * g.dnr;
+    return true;
+}
 void launch_receivers(const Geom &g, int prec, const void *T, const double *base, int nev, int nrc,
                       const RecCell *cells, float *out, cudaStream_t st);
+// receivers located on the device (rcr/rcx/rcz in device memory); *bad gets
+// the lowest index of a receiver outside the grid (atomicMin; preset it)
+void launch_receivers_located(const Geom &g, int prec, const void *T, const double *base, int nev, int nrc,
+                              const double *rcr, const double *rcx, const double *rcz, int *bad, float *out,
+                              cudaStream_t st);
 
 // rays.cu
 struct RayArgs {
@@ -197,11 +226,16 @@ struct RayArgs {
     int nev, nrc;
     const double *rcr, *rcx, *rcz;
     float *fdm;                 // [E*nrc][nmp] dense rows, or nullptr
-    double *endpoints;          // [E*nrc][3]
-    int *nsteps;                // [E*nrc]
-    int *status;                // [E*nrc] 0 ok, 1 B-spline support outside grid
+    double *endpoints;          // [E*nrc][3], or nullptr
+    int *nsteps;                // [E*nrc], or nullptr
+    // first ray (atomicMin) whose B-spline support left the velocity grid [0]
+    // and whose receiver lies outside the propagation grid [1]; INT_MAX if none
+    int *flags;
 };
 void launch_rays(const RayArgs &a, cudaStream_t st);
+// row_ptr (nrows+1) from per-row counts; chunk_tmp holds scan_chunks(nrows) values
+int scan_chunks(int nrows);
+void launch_row_scan(const int64_t *counts, int nrows, int64_t *row_ptr, int64_t *chunk_tmp, cudaStream_t st);
 void launch_row_counts(const float *fdm, int nrows, int nmp, int64_t *counts, cudaStream_t st);
 void launch_row_compact(const float *fdm, int nrows, int nmp, const int64_t *row_ptr, int32_t *cols,
                         float *vals, cudaStream_t st);

@@ -83,14 +83,20 @@ __global__ void rays_kernel(RayArgs a)
         };
         int st = 0;
         double rgr = a.rcr[i], rgx = a.rcx[i], rgz = a.rcz[i];
-        int ipr = (int)floor((g.rgor - rgr) / g.dnr) + 1;
-        int ipx = (int)floor((rgx - g.rgox) / g.dnx) + 1;
-        int ipz = (int)floor((rgz - g.rgoz) / g.dnz) + 1;
-        if (ipr == g.nnr) ipr--;   // F:7320-7333
-        if (ipx == g.nnx) ipx--;
-        if (ipz == g.nnz) ipz--;
+        // the start cell (F:7320-7333), formed and checked in double precision
+        // so that a non-finite or huge coordinate is rejected, not converted
+        double fpr = floor((g.rgor - rgr) / g.dnr) + 1.0;
+        double fpx = floor((rgx - g.rgox) / g.dnx) + 1.0;
+        double fpz = floor((rgz - g.rgoz) / g.dnz) + 1.0;
+        if (fpr == (double)g.nnr) fpr -= 1.0;
+        if (fpx == (double)g.nnx) fpx -= 1.0;
+        if (fpz == (double)g.nnz) fpz -= 1.0;
+        const bool inside = fpr >= 1.0 && fpr < (double)g.nnr && fpx >= 1.0 && fpx < (double)g.nnx &&
+                            fpz >= 1.0 && fpz < (double)g.nnz;
+        int ipr = inside ? (int)fpr : 0, ipx = inside ? (int)fpx : 0, ipz = inside ? (int)fpz : 0;
         int steps = 0;
-        if (!(ipr < 1 || ipr >= g.nnr || ipx < 1 || ipx >= g.nnx || ipz < 1 || ipz >= g.nnz)) {
+        if (!inside && a.flags) atomicMin(&a.flags[1], q);
+        if (inside) {
             for (int jstep = 1; jstep <= maxrp; ++jstep) {
                 ++steps;
                 double dtr = 0.0;
@@ -265,13 +271,13 @@ __global__ void rays_kernel(RayArgs a)
                 if (stop) break;
             }
         }
+        if (st && a.flags) atomicMin(&a.flags[0], q);
         if (a.endpoints) {
             a.endpoints[3 * (size_t)q] = rgr;
             a.endpoints[3 * (size_t)q + 1] = rgx;
             a.endpoints[3 * (size_t)q + 2] = rgz;
         }
         if (a.nsteps) a.nsteps[q] = steps;
-        if (a.status) a.status[q] = st;
     }
 }
 
@@ -330,6 +336,87 @@ __global__ void row_compact_kernel(const float *__restrict__ fdm, int nrows, int
             __syncthreads();
         }
     }
+}
+
+// Row pointers from row counts: row_ptr[0] = 0, row_ptr[i+1] = row_ptr[i] +
+// counts[i].  Each block scans a chunk of kScanChunk rows and writes its total;
+// one block then turns the totals into chunk offsets in order (any number of
+// chunks, with a running carry) and the chunks add their offset.
+constexpr int kScanThreads = 1024;
+constexpr int kScanChunk = kScanThreads;
+
+__device__ int64_t block_exclusive_scan(int64_t v, int64_t *total)
+{
+    __shared__ int64_t warp_sums[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int64_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        int64_t w = lane < nw ? warp_sums[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nw) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    const int64_t before = (wid > 0 ? warp_sums[wid - 1] : 0) + x - v;
+    *total = warp_sums[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return before;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_chunks_kernel(const int64_t *__restrict__ counts, int n,
+                                                                   int64_t *__restrict__ row_ptr,
+                                                                   int64_t *__restrict__ chunk_tot)
+{
+    const int i = blockIdx.x * kScanChunk + threadIdx.x;
+    const int64_t v = i < n ? counts[i] : 0;
+    int64_t tot;
+    const int64_t ex = block_exclusive_scan(v, &tot);
+    if (i < n) row_ptr[i + 1] = ex + v;          // inclusive within the chunk
+    if (threadIdx.x == 0) chunk_tot[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_totals_kernel(int64_t *__restrict__ chunk_tot, int nchunks)
+{
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int c0 = 0; c0 < nchunks; c0 += kScanThreads) {
+        const int c = c0 + threadIdx.x;
+        const int64_t v = c < nchunks ? chunk_tot[c] : 0;
+        int64_t tot;
+        const int64_t ex = block_exclusive_scan(v, &tot);
+        if (c < nchunks) chunk_tot[c] = carry + ex;  // offset of chunk c
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+}
+
+__global__ void scan_add_kernel(int n, int64_t *__restrict__ row_ptr, const int64_t *__restrict__ chunk_off)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) row_ptr[0] = 0;
+    if (i < n) row_ptr[i + 1] += chunk_off[i / kScanChunk];
+}
+
+int scan_chunks(int nrows) { return (nrows + kScanChunk - 1) / kScanChunk; }
+
+void launch_row_scan(const int64_t *counts, int nrows, int64_t *row_ptr, int64_t *chunk_tmp, cudaStream_t st)
+{
+    if (nrows <= 0) return;
+    const int nc = scan_chunks(nrows);
+    scan_chunks_kernel<<<nc, kScanThreads, 0, st>>>(counts, nrows, row_ptr, chunk_tmp);
+    scan_totals_kernel<<<1, kScanThreads, 0, st>>>(chunk_tmp, nc);
+    scan_add_kernel<<<(nrows + 255) / 256, 256, 0, st>>>(nrows, row_ptr, chunk_tmp);
 }
 
 void launch_rays(const RayArgs &a, cudaStream_t st)

@@ -4,6 +4,7 @@
 // trr of the reference (each partial sum rounded to float, F:7098-7106).
 // The cell and its offsets are located on the host (F:7066-7097).
 // Compiled without FMA contraction.
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -78,9 +79,12 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 // Same cell location (F:7066-7097, last-subdomain clamp F:7069-7070) and the
 // same single-precision accumulation as the table-driven kernel above.
+// (also the kernel of fm3dt_receiver_times_device, whose receivers are in
+// device memory)
 template <typename R>
 __global__ void receivers_noalloc_kernel(Geom g, const R *__restrict__ T, const double *__restrict__ base, int nev,
-                                         int nrc, const double *__restrict__ coords, int *__restrict__ bad,
+                                         int nrc, const double *__restrict__ rcr, const double *__restrict__ rcx,
+                                         const double *__restrict__ rcz, int *__restrict__ bad,
                                          float *__restrict__ out)
 {
     const size_t N = (size_t)g.nnx * g.nnz * g.nnr;
@@ -88,20 +92,13 @@ __global__ void receivers_noalloc_kernel(Geom g, const R *__restrict__ T, const 
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
          q += (long long)gridDim.x * blockDim.x) {
         const int e = (int)(q / nrc), i = (int)(q - (long long)e * nrc);
-        const double rcr = coords[i], rcx = coords[nrc + i], rcz = coords[2 * nrc + i];
-        const int irr = (int)floor((g.rgor - rcr) / g.dnr) + 1;
-        int irx = (int)floor((rcx - g.rgox) / g.dnx) + 1;
-        int irz = (int)floor((rcz - g.rgoz) / g.dnz) + 1;
-        if (irx == g.nnx) irx--;
-        if (irz == g.nnz) irz--;
-        if (irr < 1 || irr >= g.nnr || irx < 1 || irx >= g.nnx || irz < 1 || irz >= g.nnz) {
+        RecCell c;
+        if (!locate_receiver(g, rcr[i], rcx[i], rcz[i], c)) {
             atomicMin(bad, i);
-            out[q] = 0.0f;
             continue;
         }
-        const double drx = (rcx - g.rgox) - (double)(irx - 1) * g.dnx;
-        const double drz = (rcz - g.rgoz) - (double)(irz - 1) * g.dnz;
-        const double drr = (g.rgor - rcr) - (double)(irr - 1) * g.dnr;
+        const int irr = c.irr, irx = c.irx, irz = c.irz;
+        const double drr = c.drr, drx = c.drx, drz = c.drz;
         const R *Te = T + (size_t)e * N;
         const double b = base[e];
         float acc = 0.0f;
@@ -119,6 +116,21 @@ __global__ void receivers_noalloc_kernel(Geom g, const R *__restrict__ T, const 
     }
 }
 
+void launch_receivers_located(const Geom &g, int prec, const void *T, const double *base, int nev, int nrc,
+                              const double *rcr, const double *rcx, const double *rcz, int *bad, float *out,
+                              cudaStream_t st)
+{
+    const long long n = (long long)nev * nrc;
+    const int blocks = (int)std::min<long long>((n + 127) / 128, 1LL << 20);
+    if (blocks <= 0) return;
+    if (prec == FM3DT_FP64)
+        receivers_noalloc_kernel<double><<<blocks, 128, 0, st>>>(g, (const double *)T, base, nev, nrc, rcr, rcx, rcz,
+                                                                 bad, out);
+    else
+        receivers_noalloc_kernel<float><<<blocks, 128, 0, st>>>(g, (const float *)T, base, nev, nrc, rcr, rcx, rcz,
+                                                                bad, out);
+}
+
 }  // namespace fm3dt
 
 namespace {
@@ -129,7 +141,9 @@ void *g_noalloc_base[kNoAllocMaxDevices] = {};
 
 // Device address of the scratch array on the current device.  The host-side
 // symbol is only a stand-in, so the address is looked up once per device
-// (with that device current) and cached.
+// (with that device current) and cached.  The cache is not dropped when the
+// host resets a device (cudaDeviceReset); after a reset the cached address
+// belongs to the destroyed context.
 cudaError_t noalloc_scratch(void **out)
 {
     int dev = 0;
@@ -176,28 +190,25 @@ extern "C" int fm3dt_receiver_times_noalloc(fm3dt_ctx *ctx, int nrc, const doubl
     if (e == cudaSuccess) e = cudaMemcpyAsync(coords + 2 * nrc, rcz, nrc * sizeof(double), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0x7f, sizeof(int), s);     // 0x7f7f7f7f: no bad receiver
     if (e == cudaSuccess) {
-        const long long n = (long long)nev * nrc;
-        const int blocks = (int)((n + 127) / 128);
-        if (ctx->prec == FM3DT_FP64)
-            receivers_noalloc_kernel<double><<<blocks, 128, 0, s>>>(ctx->g, (const double *)ctx->d_T, ctx->d_base,
-                                                                    nev, nrc, coords, bad, dout);
-        else
-            receivers_noalloc_kernel<float><<<blocks, 128, 0, s>>>(ctx->g, (const float *)ctx->d_T, ctx->d_base,
-                                                                   nev, nrc, coords, bad, dout);
+        launch_receivers_located(ctx->g, ctx->prec, ctx->d_T, ctx->d_base, nev, nrc, coords, coords + nrc,
+                                 coords + 2 * nrc, bad, dout, s);
         e = cudaGetLastError();
         ctx->launches += 1;
     }
+    // the status word first: on a bad receiver `out` is left untouched, like
+    // fm3dt_receiver_times, which checks every receiver before any work
     int first_bad = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, (size_t)nev * nrc * sizeof(float), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&first_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && first_bad != 0x7f7f7f7f) {
+        ctx->err = "receiver " + std::to_string(first_bad + 1) + " lies outside the grid";
+        return FM3DT_ERANGE;
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, (size_t)nev * nrc * sizeof(float), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         ctx->err = std::string("fm3dt_receiver_times_noalloc: ") + cudaGetErrorString(e);
         return FM3DT_ECUDA;
-    }
-    if (first_bad != 0x7f7f7f7f) {
-        ctx->err = "receiver " + std::to_string(first_bad + 1) + " lies outside the grid";
-        return FM3DT_ERANGE;
     }
     return FM3DT_OK;
 }

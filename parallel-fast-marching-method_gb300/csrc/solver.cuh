@@ -260,8 +260,11 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
 {
     using TL = Tile<R, TR, TX, TZ>;
     static_assert(32 % TR == 0, "a column's rows of a tile lie in one certification word");
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    R *box = reinterpret_cast<R *>(smem_raw);
+    // (the TMA destination: 128-byte aligned; a name of its own, since every
+    // extern __shared__ declaration of one name in a translation unit must
+    // agree on the alignment)
+    extern __shared__ __align__(128) unsigned char round_smem[];
+    R *box = reinterpret_cast<R *>(round_smem);
     __shared__ __align__(8) unsigned long long s_bar;
     __shared__ int s_abort;
     int phase = 0;
@@ -278,11 +281,18 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
     if (tid == 0) s_upd = 0;
 
     __shared__ int s_dirty_faces;
+    // a TMA destination must start on a 128-byte boundary: check the box (and
+    // the slowness after it, at a multiple of 128 bytes for every tile shape)
+    // before the first copy, and report instead of issuing a misaligned one
+    static_assert((Tile<R, TR, TX, TZ>::OFF_S * sizeof(R)) % 128 == 0, "slowness box alignment");
+    const bool tma = a.tma && (smem_u32(box) & 127u) == 0;
     if (tid == 0) {
         s_abort = 0;
-        if (a.tma) mbar_init(&s_bar);
+        if (a.tma && !tma) atomicExch(a.err, 2);
+        if (tma) mbar_init(&s_bar);
     }
     __syncthreads();
+    if (a.tma && !tma) return;
     for (int item = blockIdx.x; item < count; item += gridDim.x) {
         if (tid == 0) {
             const int w = a.cur_list[item];
@@ -302,7 +312,7 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
         const int tri = t / (f.ntz * f.ntx);
         const int r0 = tri * TR, x0 = txi * TX, z0 = tzi * TZ;
         R *Te = f.T + (size_t)e * N;
-        if (a.tma) {
+        if (tma) {
             // outside the grid the copy fills NaN, which the stencil never
             // uses: an out-of-grid first neighbour is masked, and a NaN second
             // neighbour fails t2 < t1 like +inf
@@ -446,7 +456,7 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
         }
         // every thread's accesses to the box come before the next copy's
         // writes (generic proxy, then async proxy)
-        if (a.tma) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (tma) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
     }
     if (my_upd) atomicAdd(&s_upd, my_upd);
@@ -590,8 +600,8 @@ template <typename R, int TR, int TX, int TZ>
 __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::sweep)) sweep_kernel(SweepArgs<R> a)
 {
     using TL = Tile<R, TR, TX, TZ>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    R *box = reinterpret_cast<R *>(smem_raw);
+    extern __shared__ __align__(16) unsigned char sweep_smem[];
+    R *box = reinterpret_cast<R *>(sweep_smem);
     const FieldArgs<R> &f = a.f;
     const int tid = threadIdx.x;
     const int tz = tid % TZ, tx = tid / TZ;

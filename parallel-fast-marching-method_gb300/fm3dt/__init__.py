@@ -56,7 +56,7 @@ class Status(C.Structure):
 EXPORTS = [
     "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_resume",
     "fm3dt_solve_planewave", "fm3dt_solve_point",
-    "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
+    "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_receiver_times_device", "fm3dt_rays_frechet_device", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
     "fm3dt_set_tuning", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_round_trace_ms", "fm3dt_tile_shapes", "fm3dt_tile_shape",
     "fm3dt_launch_count",
     "fm3dt_last_error", "fm3dt_ctx_destroy",
@@ -86,6 +86,9 @@ def load(path: str | None = None):
     L.fm3dt_receiver_times.argtypes = [vp, C.c_int, dp, dp, dp, C.POINTER(C.c_float)]
     L.fm3dt_rays_frechet.argtypes = [vp, C.c_int, dp, dp, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                      C.POINTER(C.c_float), C.c_int64, dp]
+    L.fm3dt_receiver_times_device.argtypes = [vp, C.c_int, vp, vp, vp, vp]
+    L.fm3dt_rays_frechet_device.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, C.c_int64,
+                                            C.POINTER(C.c_int64), vp]
     L.fm3dt_get_times.argtypes = [vp, C.c_int, dp]
     L.fm3dt_set_times.argtypes = [vp, C.c_int, C.c_int, dp]
     L.fm3dt_get_velocity.argtypes = [vp, dp]
@@ -327,6 +330,40 @@ class Solver:
             self._check(rc)
             n = int(row_ptr[-1])
             return row_ptr, cols[:n], vals[:n], ends
+
+    def receiver_times_device(self, nrc: int, rcr_ptr: int, rcx_ptr: int, rcz_ptr: int, out_ptr: int):
+        """Receiver times with receivers and output (nev x nrc floats) in
+        device memory (raw device addresses)."""
+        self._check(self._L.fm3dt_receiver_times_device(self._ctx, int(nrc), C.c_void_p(rcr_ptr),
+                                                        C.c_void_p(rcx_ptr), C.c_void_p(rcz_ptr),
+                                                        C.c_void_p(out_ptr)))
+
+    def rays_frechet_device(self, nrc: int, rcr_ptr: int, rcx_ptr: int, rcz_ptr: int, row_ptr_ptr: int,
+                            cols_ptr: int, vals_ptr: int, cap: int, ends_ptr: int = 0, strict: bool = True) -> int:
+        """Rays and Frechet rows with every array in device memory (raw
+        device addresses; cols/vals 0 to trace rays only).  Returns the entry
+        count; when it exceeds cap, raises ERANGE (strict) or returns it with
+        the rows unwritten."""
+        total = C.c_int64(0)
+        rc = self._L.fm3dt_rays_frechet_device(
+            self._ctx, int(nrc), C.c_void_p(rcr_ptr), C.c_void_p(rcx_ptr), C.c_void_p(rcz_ptr),
+            C.c_void_p(row_ptr_ptr or None), C.c_void_p(cols_ptr or None), C.c_void_p(vals_ptr or None),
+            int(cap), C.byref(total), C.c_void_p(ends_ptr or None))
+        if rc == ERANGE and total.value > cap and not strict:
+            return int(total.value)       # the caller sizes its arrays and calls again
+        self._check(rc)
+        return int(total.value)
+
+    def rays_frechet_into(self, rcr, rcx, rcz, row_ptr_ptr: int, cols_ptr: int, vals_ptr: int, cap: int,
+                          ends_ptr: int = 0):
+        """Rays and Frechet rows into caller-owned host memory (e.g. pinned):
+        row_ptr nev*nrc+1 int64, cols int32 and vals float32 of capacity cap.
+        Returns the entry count."""
+        self._check(self._L.fm3dt_rays_frechet(
+            self._ctx, len(rcr), _d(rcr), _d(rcx), _d(rcz), C.cast(C.c_void_p(row_ptr_ptr), C.POINTER(C.c_int64)),
+            C.cast(C.c_void_p(cols_ptr), C.POINTER(C.c_int32)), C.cast(C.c_void_p(vals_ptr), C.POINTER(C.c_float)),
+            int(cap), C.cast(C.c_void_p(ends_ptr or None), C.POINTER(C.c_double))))
+        return int(C.cast(C.c_void_p(row_ptr_ptr + 8 * self.nev * len(rcr)), C.POINTER(C.c_int64))[0])
 
     def get_times(self, event: int = 0) -> np.ndarray:
         nnr, nnx, nnz = self.nn

@@ -390,3 +390,58 @@ def test_errors_are_reported(gpu_lib):
             s.receiver_times(np.array([0.0]), np.array([0.1]), np.array([0.1]))
         assert ei.value.code == fm3dt.ERANGE
         assert s.launch_count > 0
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_device_memory_entry_points_equal_host_ones(gpu_lib, prec):
+    """fm3dt_receiver_times_device and fm3dt_rays_frechet_device (receivers
+    and outputs in device memory) give the host entry points' results bit for
+    bit; a capacity below the entry count is refused with the count given."""
+    import torch
+    import fm3dt
+    w = _setup(3, 24, nev=3)
+    params = _params(w)
+    rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat, w.rec_lon)
+    rcr = np.asarray(w.rec_elev, dtype=np.float64)
+    nrc = len(rcr)
+    with fm3dt.Solver(w.header, precision=prec, max_events=3) as s:
+        s.set_velocity(w.velv)
+        s.solve_planewave(params)
+        ref_t = s.receiver_times(rcr, rcx, rcz)
+        ref_ptr, ref_cols, ref_vals, ref_ends = s.rays_frechet(rcr, rcx, rcz)
+        d = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (rcr, rcx, rcz)]
+        out = torch.empty((3, nrc), dtype=torch.float32, device="cuda")
+        s.receiver_times_device(nrc, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), out.data_ptr())
+        assert np.array_equal(out.cpu().numpy(), ref_t)
+        nrows = 3 * nrc
+        row_ptr = torch.zeros(nrows + 1, dtype=torch.int64, device="cuda")
+        cap = int(ref_ptr[-1])
+        cols = torch.zeros(cap, dtype=torch.int32, device="cuda")
+        vals = torch.zeros(cap, dtype=torch.float32, device="cuda")
+        ends = torch.zeros((nrows, 3), dtype=torch.float64, device="cuda")
+        total = s.rays_frechet_device(nrc, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), row_ptr.data_ptr(),
+                                      cols.data_ptr(), vals.data_ptr(), cap, ends.data_ptr())
+        assert total == cap
+        assert np.array_equal(row_ptr.cpu().numpy(), ref_ptr)
+        assert np.array_equal(cols.cpu().numpy(), ref_cols)
+        assert np.array_equal(vals.cpu().numpy(), ref_vals)
+        assert np.array_equal(ends.cpu().numpy(), ref_ends)
+        with pytest.raises(fm3dt.Fm3dtError) as ei:
+            s.rays_frechet_device(nrc, d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(), row_ptr.data_ptr(),
+                                  cols.data_ptr(), vals.data_ptr(), cap - 1)
+        assert ei.value.code == fm3dt.ERANGE
+        assert int(row_ptr[-1].item()) == cap
+        # a receiver outside the grid is refused by both
+        bad = d[1].clone()
+        bad[7] = float("nan")
+        with pytest.raises(fm3dt.Fm3dtError) as ei:
+            s.receiver_times_device(nrc, d[0].data_ptr(), bad.data_ptr(), d[2].data_ptr(), out.data_ptr())
+        assert ei.value.code == fm3dt.ERANGE
+        with pytest.raises(fm3dt.Fm3dtError) as ei:
+            s.rays_frechet_device(nrc, d[0].data_ptr(), bad.data_ptr(), d[2].data_ptr(), 0, 0, 0, 0)
+        assert ei.value.code == fm3dt.ERANGE
+        badh = rcx.copy()
+        badh[7] = np.nan
+        with pytest.raises(fm3dt.Fm3dtError) as ei:
+            s.rays_frechet(rcr, badh, rcz)
+        assert ei.value.code == fm3dt.ERANGE

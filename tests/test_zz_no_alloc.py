@@ -76,3 +76,58 @@ def test_noalloc_limits_and_errors(gpu_lib):
         rc, got = _call(s, w.rec_elev[:5], rcx, rcz)
         assert rc == fm3dt.OK
         assert np.array_equal(got, s.receiver_times(w.rec_elev[:5], rcx, rcz))
+
+
+def test_noalloc_at_the_limits(gpu_lib):
+    """Exactly at both limits (4096 receivers filling the coordinate block,
+    64 x 4096 = 262144 times filling the output block) the results equal
+    fm3dt_receiver_times bit for bit; one time more is refused."""
+    import fm3dt
+    from fm3dt import synth
+    w = synth.config(0, scale=16, nev=1)
+    rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat, w.rec_lon)
+    n = 4096
+    rcr_n, rcx_n, rcz_n = (np.resize(np.asarray(a, dtype=np.float64), n) for a in (w.rec_elev, rcx, rcz))
+    ev = np.resize(np.asarray(w.events[0], dtype=np.float64), (65, 2)).copy()
+    ev[:, 1] += np.arange(65) * 5.0
+    params = np.array([synth.planewave_params(w.header, *e) for e in ev])
+    with fm3dt.Solver(w.header, max_events=65) as s:
+        s.set_velocity(w.velv)
+        s.solve_planewave(params[:64])
+        ref = s.receiver_times(rcr_n, rcx_n, rcz_n)
+        rc, got = _call(s, rcr_n, rcx_n, rcz_n)
+        assert rc == fm3dt.OK, s._L.fm3dt_last_error(s._ctx)
+        assert got.shape == (64, n)
+        assert np.array_equal(got, ref)
+        s.solve_planewave(params)
+        rc, _ = _call(s, rcr_n, rcx_n, rcz_n)
+        assert rc == fm3dt.EINVAL
+        assert b"262144" in s._L.fm3dt_last_error(s._ctx)
+        # fewer receivers for the 65 events fit again
+        rc, got = _call(s, rcr_n[:4000], rcx_n[:4000], rcz_n[:4000])
+        assert rc == fm3dt.OK
+        assert np.array_equal(got, s.receiver_times(rcr_n[:4000], rcx_n[:4000], rcz_n[:4000]))
+
+
+@pytest.mark.parametrize("bad", [np.nan, np.inf, 1e300])
+def test_noalloc_rejects_non_finite_receivers_like_receiver_times(gpu_lib, bad):
+    """A NaN, infinite or huge coordinate is outside the grid for both entry
+    points (FM3DT_ERANGE), and neither writes its output."""
+    import fm3dt
+    from fm3dt import synth
+    w = synth.config(0, scale=16, nev=1)
+    params = np.array([synth.planewave_params(w.header, *w.events[0])])
+    rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat[:6], w.rec_lon[:6])
+    with fm3dt.Solver(w.header) as s:
+        s.set_velocity(w.velv)
+        s.solve_planewave(params)
+        for which in range(3):
+            coords = [np.array(w.rec_elev[:6], dtype=np.float64), rcx.copy(), rcz.copy()]
+            coords[which][4] = bad
+            rc, got = _call(s, *coords)
+            assert rc == fm3dt.ERANGE
+            assert b"receiver 5" in s._L.fm3dt_last_error(s._ctx)
+            assert np.isnan(got).all()          # untouched
+            with pytest.raises(fm3dt.Fm3dtError) as ei:
+                s.receiver_times(*coords)
+            assert ei.value.code == fm3dt.ERANGE
