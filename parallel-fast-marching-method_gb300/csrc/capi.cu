@@ -316,6 +316,11 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 //                          their extra sweeps, beside the other events' main sweep
 //   FM_RESWEEPS            re-sweeps after the first rounds, at most
 //   FM_RESWEEP_FRAC        ... of events with more than this fraction of tiles queued
+//   FM_FRESH_SWEEP         main sweeps from the unset field with upstream-only node
+//                          updates (the same values as the full update there)
+#ifndef FM_FRESH_SWEEP
+#define FM_FRESH_SWEEP 1
+#endif
 #ifndef FM_TIE_SWEEPS
 #define FM_TIE_SWEEPS 2
 #endif
@@ -405,15 +410,21 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     const int sidx = streaming ? ctx->sweep_shape - kNumShapes : 0;
     const int nbx = (g.nnx + kStreamShapes[sidx].sx - 1) / kStreamShapes[sidx].sx;
     const int nbz = (g.nnz + kStreamShapes[sidx].sz - 1) / kStreamShapes[sidx].sz;
-    const int sgrid = streaming ? std::max(1, ctx->prec == FM3DT_FP64 ? occupancy_stream_f64(sidx)
-                                                                     : occupancy_stream_f32(sidx)) * sm_count()
-                                : 1;
+    // resident one-warp CTAs of the streaming sweep (the main sweep's form and
+    // the general form differ in registers)
+    auto stream_grid = [&](bool fresh) {
+        return streaming ? std::max(1, ctx->prec == FM3DT_FP64 ? occupancy_stream_f64(sidx, fresh)
+                                                               : occupancy_stream_f32(sidx, fresh)) * sm_count()
+                         : 1;
+    };
     // One streaming sweep of nitems events (events == null: all), lateral
     // directions flipped by `flip`; with `flag`, changed nodes queue their
-    // tiles (and face neighbours) on list/count for the rounds.
+    // tiles (and face neighbours) on list/count for the rounds.  `fresh`: the
+    // events' main sweep, from their unset fields (upstream-only updates).
     auto stream_pass = [&](int nitems, const int *events, int flip, int nseg, int *flag, int *list,
-                           int *count, cudaStream_t st) -> int {
+                           int *count, cudaStream_t st, bool fresh) -> int {
         sweep_nodes += (int64_t)nitems * (int64_t)ctx->N;
+        const int sgrid = stream_grid(fresh);
         if (nseg <= 0) nseg = stream_segments(ctx, nitems, nbx, nbz, sgrid, kStreamShapes[sidx].sx + kStreamShapes[sidx].sz - 2);
         nseg = std::min(nseg, g.nnr);
         const fm3dt_ctx::Planes *PP = nullptr;
@@ -429,6 +440,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                 a.dir = ctx->d_dir; a.nev = nitems; a.nbx = nbx; a.nbz = nbz;
                 a.events = events;
                 a.flip = flip;
+                a.fresh = fresh ? 1 : 0;
                 a.seg_len = seg_len;
                 a.flag = flag;
                 a.list = list; a.count = count;
@@ -490,7 +502,8 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             const int nitems = pass == 1 ? (int)ties.size() : nev;
             const int rc = stream_pass(nitems, pass == 1 ? ctx->d_events : nullptr, pl.flip,
                                        pass == 1 ? ctx->tie_segments : ctx->sweep_segments,
-                                       pass == 2 ? ctx->d_flag : nullptr, ctx->d_list[0], ctx->d_count[0], s);
+                                       pass == 2 ? ctx->d_flag : nullptr, ctx->d_list[0], ctx->d_count[0], s,
+                                       pass == 0 && FM_FRESH_SWEEP);
             if (rc) return rc;
         }
         CKL();
@@ -662,7 +675,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         CK(cudaMemcpyAsync(ctx->d_events, busy.data(), busy.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         CK(cudaEventRecord(r0, s));
         const int rc = stream_pass((int)busy.size(), ctx->d_events, 0, 0, ctx->d_flag, ctx->d_list[nl],
-                                   ctx->d_count[nl], s);
+                                   ctx->d_count[nl], s, false);
         if (rc) return rc;
         CK(cudaEventRecord(r1, s));
         CKL();
@@ -698,10 +711,10 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             // each part's main sweep: the near-tie events' on stream2 ahead of
             // their extra sweeps, the others' on the context stream
             int rc = stream_pass((int)ties.size(), ctx->d_events, 0, ctx->tie_segments, nullptr, ctx->d_list[0],
-                                 ctx->d_count[0], s2);
+                                 ctx->d_count[0], s2, FM_FRESH_SWEEP);
             if (rc) return rc;
             rc = stream_pass((int)others.size(), ctx->d_events_b, 0, ctx->sweep_segments, nullptr, ctx->d_list[0],
-                             ctx->d_count[0], s);
+                             ctx->d_count[0], s, FM_FRESH_SWEEP);
             if (rc) return rc;
             CK(cudaEventRecord(sw1, s));
             CK(cudaEventRecord(r0, s));
@@ -711,7 +724,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             // their sweeps are the longer chain of the two parts)
             const int rc = stream_pass((int)ties.size(), ctx->d_events, (k & 1) ? 0 : 4,
                                        FM_OVERLAP_MAIN ? ctx->tie_segments : (ctx->tie_segments > 0 ? ctx->tie_segments : 2),
-                                       nullptr, ctx->d_list[0], ctx->d_count[0], s2);
+                                       nullptr, ctx->d_list[0], ctx->d_count[0], s2, false);
             if (rc) return rc;
         }
         launch_initial_tiles((int)ties.size(), ctx->d_events, tpe, first, cnt, ctx->d_list_b, ctx->d_count_b,

@@ -106,6 +106,7 @@ struct StreamArgs {
     const int *events;          // the events swept (indices), or null for events 0..nev-1
     int nev;
     int flip;                   // bit 0 / 1: reverse theta / phi; bit 2: reverse each near-tie lateral direction
+    int fresh;                  // the main sweep from an unset field: upstream-only node updates
     int nbx, nbz;               // column blocks per axis
     int seg_len;                // layers per height segment
     // verification sweep: when flag is set, every node whose value changes
@@ -118,8 +119,8 @@ struct StreamArgs {
 
 void launch_stream_f32(int idx, int grid, const StreamArgs<float> &a, cudaStream_t st);
 void launch_stream_f64(int idx, int grid, const StreamArgs<double> &a, cudaStream_t st);
-int occupancy_stream_f32(int idx);
-int occupancy_stream_f64(int idx);
+int occupancy_stream_f32(int idx, bool fresh);
+int occupancy_stream_f64(int idx, bool fresh);
 
 // After a single sweep from an unset field: mark the nodes a recomputation
 // could change (certification bitmap) and queue their tiles (kCert).

@@ -55,10 +55,10 @@ void launch_stream_f32(int idx, int grid, const StreamArgs<float> &a, cudaStream
 #undef C_
 }
 
-int occupancy_stream_f32(int idx)
+int occupancy_stream_f32(int idx, bool fresh)
 {
     int r = 0;
-#define C_(X, Z) r = StreamKernels<float, X, Z>::occ()
+#define C_(X, Z) r = StreamKernels<float, X, Z>::occ(fresh)
     FM_STREAM_SWITCH(idx, C_)
 #undef C_
     return r;

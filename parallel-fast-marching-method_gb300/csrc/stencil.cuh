@@ -255,4 +255,109 @@ FM_HD R fm_update(R s, const R t1[6], const R t2[6], unsigned inb, const Spacing
     return tmin + best;
 }
 
+// The node update of a sweep from an unset field, where every neighbour
+// downstream of the sweep (up, r-1, and the lateral directions the sweep runs
+// toward) is still unset when the node is computed.  Then only the three
+// upstream neighbours -- down (r+1) and the lateral ones the sweep comes
+// from, here D, X and Z -- can enter an octant, and each of the eight octants
+// is the causal solve of the upstream terms it contains: the octant that
+// takes the upstream side on the axes of a subset S of {D, X, Z} and the
+// downstream side on the others solves S (its downstream terms are +inf,
+// sort last and never pass k < x).  So this returns fm_update's value, bit
+// for bit, with +inf at the downstream neighbours: the same keys, the same
+// stable order within each subset (key, then axis r, theta, phi), the same
+// arithmetic, and an octant counted when its three neighbours lie inside the
+// grid.  It evaluates the seven subsets with four quadratic solves instead of
+// the eight octants' sixteen: the singletons are one FMA each, the three pairs
+// one solve each, and the triple's first two terms are one of the pairs (the
+// same order and the same operations, hence the same bits), so only its
+// three-term solve is added.
+//
+// tD/tD2, tX/tX2, tZ/tZ2: upstream first and second neighbour values;
+// in*: whether each upstream (u) and downstream (d) neighbour lies inside the
+// grid (inD: r+1, inU: r-1).
+template <typename R>
+FM_HD R fm_update_upstream(R s, R tD, R tD2, R tX, R tX2, R tZ, R tZ2, bool inD, bool inU, bool inXu, bool inXd,
+                           bool inZu, bool inZd, const Spacing<R> &sp, int order2)
+{
+    const R INF = Lim<R>::inf();
+    const R tmin = fm_min(fm_min(tD, tX), tZ);
+    if (!(tmin < INF)) return INF;
+    const R s2 = s * s;
+    R k[3], e[3], w[3], x1[3];
+    {
+        const R t1[3] = {tD, tX, tZ}, t2[3] = {tD2, tX2, tZ2};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const bool o2 = order2 && (t2[a] < t1[a]);
+            const R dt = t1[a] - tmin;
+            k[a] = dt;
+            e[a] = o2 ? fm_fma<R>(t1[a] - t2[a], R(1.0 / 3.0), dt) : dt;
+            const R g = o2 ? sp.h[a] * R(2.0 / 3.0) : sp.h[a];
+            w[a] = o2 ? sp.w[a] * R(2.25) : sp.w[a];
+            x1[a] = fm_fma<R>(s, g, e[a]);        // the one-term solution
+        }
+    }
+    // causal solve of the pair (i, j), i before j in axis order, sorted
+    // stably; the two-term step exactly as fm_update's
+    auto pair = [&](int i, int j) -> R {
+        const bool p = k[j] < k[i];
+        const R ks = p ? k[i] : k[j];
+        const R ef = p ? e[j] : e[i], es = p ? e[i] : e[j];
+        const R wf = p ? w[j] : w[i], ws = p ? w[i] : w[j];
+        R x = p ? x1[j] : x1[i];
+        if (ks < x) {
+            const R a = wf + ws;
+            const R wef = wf * ef, wes = ws * es;
+            const R b = wef + wes;
+            const R c = fm_fma<R>(wef, ef, fm_fma<R>(wes, es, -s2));
+            const R disc = fm_fma<R>(b, b, -(a * c));
+            x = Fast<R>::div(b + Fast<R>::sqrt(fm_max<R>(disc, R(0))), a);
+        }
+        return x;
+    };
+    const R pDX = pair(0, 1), pDZ = pair(0, 2), pXZ = pair(1, 2);
+    // the triple, sorted stably by the same comparisons as fm_update's
+    // network (the lateral pair first, then D inserted in front); selects,
+    // not indexed arrays, so that everything stays in registers.  A/B: the
+    // lateral pair in order; F/M/L: first, middle and last of the triple;
+    // i*: which term (0 D, 1 X, 2 Z)
+    const bool pxz = k[2] < k[1];
+    const R kA = pxz ? k[2] : k[1], eA = pxz ? e[2] : e[1], wA = pxz ? w[2] : w[1], xA = pxz ? x1[2] : x1[1];
+    const R kB = pxz ? k[1] : k[2], eB = pxz ? e[1] : e[2], wB = pxz ? w[1] : w[2];
+    const int iA = pxz ? 2 : 1, iB = pxz ? 1 : 2;
+    const bool p1 = kA < k[0];
+    const R kF = p1 ? kA : k[0], eF = p1 ? eA : e[0], wF = p1 ? wA : w[0], xF = p1 ? xA : x1[0];
+    const R kM0 = p1 ? k[0] : kA, eM0 = p1 ? e[0] : eA, wM0 = p1 ? w[0] : wA;
+    const int iM0 = p1 ? 0 : iA;
+    const bool p2 = kB < kM0;
+    const R kM = p2 ? kB : kM0, eM = p2 ? eB : eM0, wM = p2 ? wB : wM0;
+    const R kL = p2 ? kM0 : kB, eL = p2 ? eM0 : eB, wL = p2 ? wM0 : wB;
+    const int iL = p2 ? iM0 : iB;
+    (void)kF;
+    // its first two terms are the pair without L (the same order and the
+    // same operations as that pair's solve)
+    R xt = iL == 2 ? pDX : (iL == 1 ? pDZ : pXZ);
+    if (kM < xF && kL < xt) {
+        const R a = (wF + wM) + wL;
+        const R wef = wF * eF, wem = wM * eM, wel = wL * eL;
+        const R b = (wef + wem) + wel;
+        const R c = fm_fma<R>(wel, eL, fm_fma<R>(wef, eF, fm_fma<R>(wem, eM, -s2)));
+        const R disc = fm_fma<R>(b, b, -(a * c));
+        xt = Fast<R>::div(b + Fast<R>::sqrt(fm_max<R>(disc, R(0))), a);
+    }
+    // subsets whose octant lies inside the grid (upstream side on the axes in
+    // the subset, downstream side on the others)
+    const bool rD = inD, rN = inU, xU = inXu, xN = inXd, zU = inZu, zN = inZd;
+    R best = INF;
+    best = (rD && xN && zN) ? fm_min(best, x1[0]) : best;
+    best = (rN && xU && zN) ? fm_min(best, x1[1]) : best;
+    best = (rN && xN && zU) ? fm_min(best, x1[2]) : best;
+    best = (rD && xU && zN) ? fm_min(best, pDX) : best;
+    best = (rD && xN && zU) ? fm_min(best, pDZ) : best;
+    best = (rN && xU && zU) ? fm_min(best, pXZ) : best;
+    best = (rD && xU && zU) ? fm_min(best, xt) : best;
+    return tmin + best;
+}
+
 }  // namespace fm3dt

@@ -56,7 +56,18 @@ __device__ void stream_mark(const StreamArgs<R> &a, int e, int gr, int gx, int g
     if (zi >= a.tz - 2 && tk < a.ntz - 1) stream_queue(a, w + 1, kFaceZm);
 }
 
-template <typename R, int SX, int SZ>
+// FRESH: the main sweep of a solve, from an unset field (every node except
+// the fixed bottom layer unset).  Each node above the bottom layer then sees
+// its downstream neighbours (up, and the lateral ones the sweep runs toward)
+// still unset -- later lanes of the block and later launches have not
+// written them, and the node's update must not take them -- so it is
+// computed by fm_update_upstream, which gives fm_update's value with those
+// neighbours unset from the three upstream ones alone.  (Items of the same
+// hyperplane may already have written a downstream neighbour in a halo
+// column; the upstream form leaves it out, as a sweep from an unset field
+// would, and the rounds reach the same fixed point either way.)  The bottom
+// layer keeps fm_update: fixed boundary nodes beside an unset one are set.
+template <typename R, int SX, int SZ, bool FRESH>
 __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
 {
     static_assert(SX * SZ == 32, "one warp per column block");
@@ -140,17 +151,28 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
                     const R *Lu2 = ring + ((rp + 2 + RING) & (RING - 1)) * LAYER;
                     const R *Ld1 = ring + ((rp - 1 + RING) & (RING - 1)) * LAYER;
                     const R *Ld2 = ring + ((rp - 2 + RING) & (RING - 1)) * LAYER;
-                    R t1[6], t2[6];
-                    t1[0] = Lu1[c];       t2[0] = Lu2[c];          // r-1 (up)
-                    t1[1] = Ld1[c];       t2[1] = Ld2[c];          // r+1 (down)
-                    t1[2] = L0[c - LZ];   t2[2] = L0[c - 2 * LZ];
-                    t1[3] = L0[c + LZ];   t2[3] = L0[c + 2 * LZ];
-                    t1[4] = L0[c - 1];    t2[4] = L0[c - 2];
-                    t1[5] = L0[c + 1];    t2[5] = L0[c + 2];
-                    const unsigned inb = (gr > 0 ? 1u : 0u) | (gr < f.nnr - 1 ? 2u : 0u) | (gx > 0 ? 4u : 0u) |
-                                         (gx < f.nnx - 1 ? 8u : 0u) | (gz > 0 ? 16u : 0u) |
-                                         (gz < f.nnz - 1 ? 32u : 0u);
-                    const R v = fm_update<R>(pcur.s, t1, t2, inb, pcur.sp, f.order2);
+                    R v;
+                    if (FRESH && rp >= 1) {
+                        // upstream: down, and x-1 / z-1 when the sweep runs
+                        // toward +theta / +phi (else x+1 / z+1)
+                        const int ox = sx ? -LZ : LZ, oz = sz ? -1 : 1;
+                        const bool xlo = gx > 0, xhi = gx < f.nnx - 1, zlo = gz > 0, zhi = gz < f.nnz - 1;
+                        v = fm_update_upstream<R>(pcur.s, Ld1[c], Ld2[c], L0[c + ox], L0[c + 2 * ox], L0[c + oz],
+                                                  L0[c + 2 * oz], true, gr > 0, sx ? xlo : xhi, sx ? xhi : xlo,
+                                                  sz ? zlo : zhi, sz ? zhi : zlo, pcur.sp, f.order2);
+                    } else {
+                        R t1[6], t2[6];
+                        t1[0] = Lu1[c];       t2[0] = Lu2[c];          // r-1 (up)
+                        t1[1] = Ld1[c];       t2[1] = Ld2[c];          // r+1 (down)
+                        t1[2] = L0[c - LZ];   t2[2] = L0[c - 2 * LZ];
+                        t1[3] = L0[c + LZ];   t2[3] = L0[c + 2 * LZ];
+                        t1[4] = L0[c - 1];    t2[4] = L0[c - 2];
+                        t1[5] = L0[c + 1];    t2[5] = L0[c + 2];
+                        const unsigned inb = (gr > 0 ? 1u : 0u) | (gr < f.nnr - 1 ? 2u : 0u) | (gx > 0 ? 4u : 0u) |
+                                             (gx < f.nnx - 1 ? 8u : 0u) | (gz > 0 ? 16u : 0u) |
+                                             (gz < f.nnz - 1 ? 32u : 0u);
+                        v = fm_update<R>(pcur.s, t1, t2, inb, pcur.sp, f.order2);
+                    }
                     const R old = L0[c];
                     if (fbits(v) != fbits(old)) {
                         ring[((rp + RING) & (RING - 1)) * LAYER + c] = v;
@@ -173,12 +195,18 @@ template <typename R, int SX, int SZ>
 struct StreamKernels {
     static void sweep(int grid, const StreamArgs<R> &a, cudaStream_t st)
     {
-        stream_sweep_kernel<R, SX, SZ><<<grid, 32, 0, st>>>(a);
+        if (a.fresh)
+            stream_sweep_kernel<R, SX, SZ, true><<<grid, 32, 0, st>>>(a);
+        else
+            stream_sweep_kernel<R, SX, SZ, false><<<grid, 32, 0, st>>>(a);
     }
-    static int occ()
+    static int occ(bool fresh)
     {
         int nb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stream_sweep_kernel<R, SX, SZ>, 32, 0);
+        if (fresh)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stream_sweep_kernel<R, SX, SZ, true>, 32, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stream_sweep_kernel<R, SX, SZ, false>, 32, 0);
         return nb;
     }
 };

@@ -1,9 +1,11 @@
-// Host check: the solver's node update (stencil.cuh fm_update, as optimised:
+// Host checks.  (1) The solver's node update (stencil.cuh fm_update, as optimised:
 // lateral pairs sorted once per two octants, hardware min/max, outside
 // octants masked by a select) against a plain restatement of the same
 // update (every octant sorted by a full three-comparator stable network,
 // outside octants skipped), bit for bit, on random inputs with ties, unset
 // neighbours, and +inf or NaN outside the grid as the kernels stage them.
+// (2) The main sweep's upstream-only update against fm_update with its
+// downstream neighbours unset, bit for bit.
 //
 //   g++ -O2 -std=c++17 -ffp-contract=off stencil_network_check.cpp -o check && ./check [cases]
 #include <cmath>
@@ -131,6 +133,60 @@ long run(long n, unsigned seed)
     return bad;
 }
 
+// The main sweep's node update (fm_update_upstream, only the three upstream
+// neighbours) against fm_update with +inf at the three downstream neighbours,
+// for every sweep direction: random upstream values with ties and unset
+// ones, random second neighbours (downstream ones too), neighbours outside
+// the grid (+inf there, as the streaming sweep stages them), both orders.
+template <typename R>
+long run_upstream(long n, unsigned seed)
+{
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> U(0.0, 1.0);
+    const R INF = Lim<R>::inf();
+    long bad = 0;
+    for (long it = 0; it < n; ++it) {
+        const bool sx = rng() & 1, sz = rng() & 1;
+        const int dX = sx ? 2 : 3, dZ = sz ? 4 : 5;      // upstream lateral directions
+        const int levels = (int)(rng() % 4);
+        R t1[6], t2[6];
+        for (int d = 0; d < 6; ++d) {
+            const double v1 = levels ? (double)(rng() % (2 + levels)) * 0.5 : U(rng) * 3.0;
+            const double v2 = levels ? (double)(rng() % (2 + levels)) * 0.5 : U(rng) * 3.0;
+            t1[d] = (rng() % 13 == 0) ? INF : R(v1);
+            t2[d] = (rng() % 9 == 0) ? INF : R(v2);
+        }
+        // downstream neighbours unset
+        t1[0] = INF;
+        t1[dX ^ 1] = INF;
+        t1[dZ ^ 1] = INF;
+        unsigned inb = 63u;
+        if (rng() % 3 == 0) inb = (unsigned)(rng() & 63);
+        for (int d = 0; d < 6; ++d)
+            if (!((inb >> d) & 1u)) {
+                t1[d] = INF;
+                t2[d] = INF;
+            }
+        Spacing<R> sp;
+        for (int a = 0; a < 3; ++a) {
+            const double h = 0.5 + U(rng) * 2.5;
+            sp.h[a] = R(h);
+            sp.w[a] = R(1.0 / (h * h));
+        }
+        const R s = R(0.1 + U(rng));
+        const int order2 = (int)(rng() & 1);
+        const R want = fm3dt::fm_update<R>(s, t1, t2, inb, sp, order2);
+        const R got = fm3dt::fm_update_upstream<R>(
+            s, t1[1], t2[1], t1[dX], t2[dX], t1[dZ], t2[dZ], (inb >> 1) & 1u, inb & 1u, (inb >> dX) & 1u,
+            (inb >> (dX ^ 1)) & 1u, (inb >> dZ) & 1u, (inb >> (dZ ^ 1)) & 1u, sp, order2);
+        if (bits(want) != bits(got)) {
+            if (bad < 5) std::printf("upstream mismatch: %.9g vs %.9g\n", (double)want, (double)got);
+            ++bad;
+        }
+    }
+    return bad;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
@@ -138,5 +194,7 @@ int main(int argc, char **argv)
     const long n = argc > 1 ? std::atol(argv[1]) : 200000;
     const long bf = run<float>(n, 1), bd = run<double>(n, 2);
     std::printf("float mismatches %ld / %ld, double mismatches %ld / %ld\n", bf, n, bd, n);
-    return (bf || bd) ? 1 : 0;
+    const long uf = run_upstream<float>(n, 3), ud = run_upstream<double>(n, 4);
+    std::printf("upstream float mismatches %ld / %ld, upstream double mismatches %ld / %ld\n", uf, n, ud, n);
+    return (bf || bd || uf || ud) ? 1 : 0;
 }

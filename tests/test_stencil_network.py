@@ -6,7 +6,9 @@ octants outside the grid with a select.  tests/stencil_network_check.cpp
 restates the update the direct way (eight octants, each sorted by a full
 three-comparator stable network, outside octants skipped) and compares the
 two bit for bit on random inputs with ties, unset neighbours and +inf/NaN
-outside the grid, in both precisions.
+outside the grid, in both precisions.  It also checks the main sweep's
+upstream-only update (fm_update_upstream) against fm_update with the three
+downstream neighbours unset, for every sweep direction.
 """
 import os
 import shutil
@@ -28,3 +30,4 @@ def test_update_equals_plain_restatement(tmp_path):
     r = subprocess.run([str(exe), "200000"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "float mismatches 0" in r.stdout and "double mismatches 0" in r.stdout
+    assert "upstream float mismatches 0" in r.stdout and "upstream double mismatches 0" in r.stdout
