@@ -44,7 +44,7 @@ def build(force: bool = False) -> str:
     src = os.path.join(_HERE, "fm3dt_oracle.c")
     if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
         os.makedirs(os.path.dirname(_LIB_PATH), exist_ok=True)
-        subprocess.check_call(["gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
+        subprocess.check_call(["gcc", "-std=gnu11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
                                "-o", _LIB_PATH, src, "-lm"])
     return _LIB_PATH
 
@@ -61,6 +61,8 @@ def lib():
         L.orc_gridder.argtypes = [C.POINTER(Grid), dp, dp, C.POINTER(C.c_int)]
         L.orc_fmm.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.POINTER(C.c_longlong)]
         L.orc_fixed_point.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.c_int, C.POINTER(C.c_int)]
+        L.orc_fmm_decomposed.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, C.c_int, C.c_int, C.c_int, C.c_int, dp,
+                                         C.POINTER(C.c_int)]
         ub = C.POINTER(C.c_ubyte)
         L.orc_fixed_point_field.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, ub, dp, C.c_int, C.POINTER(C.c_int)]
         L.orc_point_start.argtypes = [C.POINTER(Grid), dp, dp, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -127,6 +129,22 @@ def fmm(g: Grid, veln: np.ndarray, bottom: np.ndarray, fom: int = 1):
     if rc != 0:
         raise RuntimeError(f"orc_fmm failed: {rc}")
     return ttn, pops.value
+
+
+def fmm_decomposed(g: Grid, velv: np.ndarray, bottom: np.ndarray, fom: int = 1, blocks=(2, 2, 2),
+                   max_rounds: int = 100000):
+    """The reference's decomposed run (nr x nx x nz emulated ranks, 2x2x2 in
+    its mpirun -np 9 layout); velv are the velocity nodes (each block grids
+    its own nodes).  Returns (ttn, rounds)."""
+    velv = np.ascontiguousarray(velv, dtype=np.float64)
+    bottom = np.ascontiguousarray(bottom, dtype=np.float64)
+    ttn = np.zeros(g.nnr * g.nnx * g.nnz, dtype=np.float64)
+    rounds = C.c_int(0)
+    rc = lib().orc_fmm_decomposed(C.byref(g), _d(velv), int(fom), _d(bottom), int(blocks[0]), int(blocks[1]),
+                                  int(blocks[2]), int(max_rounds), _d(ttn), C.byref(rounds))
+    if rc != 0:
+        raise RuntimeError(f"orc_fmm_decomposed failed: {rc}")
+    return ttn, rounds.value
 
 
 def fixed_point(g: Grid, veln: np.ndarray, bottom: np.ndarray, fom: int = 1, max_sweeps: int = 10000):

@@ -9,9 +9,10 @@
  * Every routine restates the serial behaviour of the cited Fortran lines with
  * the reference's operation order (left-to-right, no fused multiply-add), so
  * that double-precision results follow the reference's rounding.  Build with
- * -ffp-contract=off.  Subdomain offsets of the MPI code are taken as those of
- * a single subdomain (roffset = xoffset = zoffset = 1), which removes the
- * (offset-1)*spacing terms (they are exactly 0.0).
+ * -ffp-contract=off.  The serial routines take the offsets of a single
+ * subdomain (roffset = xoffset = zoffset = 1: the (offset-1)*spacing terms are
+ * exactly 0.0); orc_fmm_decomposed runs the reference's block split with each
+ * block's own offsets, in the reference's operation order.
  */
 #include "fm3dt_oracle.h"
 
@@ -79,26 +80,34 @@ static int clampi(int v, int lo, int hi, int *hit)
     return v;
 }
 
-int orc_gridder(const orc_grid *g, const double *velv, double *veln, int *nclamped)
+/* The gridder of one (sub)domain of rnum x xnum x znum nodes whose first
+ * node is global node (roff, xoff, zoff) (F:6989-7038, offsets in the
+ * reference's operation order); veln has (znum+3)(xnum+3)(rnum+3) values,
+ * indices -1..n+1. */
+static int gridder_block(const orc_grid *g, const double *velv, int roff, int xoff, int zoff, int rnum, int xnum,
+                         int znum, double *veln, int *nclamped)
 {
     int nclamp = 0;
-    for (int i = -1; i <= g->nnz + 1; ++i) {
-        /* F:6996-6998 with zoffset = 1 */
-        const double zpos = g->rgoz + (double)(i - 1) * g->dnz - g->goz;
+    const size_t VZ3 = (size_t)znum + 3, VX3 = (size_t)xnum + 3;
+    for (int i = -1; i <= znum + 1; ++i) {
+        /* F:6996-6998 */
+        const double zpos = g->rgoz + (double)(zoff - 1) * g->dnz + (double)(i - 1) * g->dnz - g->goz;
         const int zi = (int)floor(zpos / g->dvz) + 1;
         const double distz = zpos - (double)(zi - 1) * g->dvz;
         double wi[4];
         bspline4(distz / g->dvz, wi);
-        for (int j = -1; j <= g->nnx + 1; ++j) {
-            const double xpos = g->rgox + (double)(j - 1) * g->dnx - g->gox;
+        for (int j = -1; j <= xnum + 1; ++j) {
+            const double xpos = g->rgox + (double)(xoff - 1) * g->dnx + (double)(j - 1) * g->dnx - g->gox;
             const int xi = (int)floor(xpos / g->dvx) + 1;
             const double distx = xpos - (double)(xi - 1) * g->dvx;
             double vi[4];
             bspline4(distx / g->dvx, vi);
-            for (int k = -1; k <= g->nnr + 1; ++k) {
+            for (int k = -1; k <= rnum + 1; ++k) {
                 /* F:7015-7016: ri from depth below the velocity origin */
-                const int ri = (int)floor((g->gor - g->rgor + (double)(k - 1) * g->dnr) / g->dvr) + 1;
-                const double distr = -(g->rgor - (double)(k - 1) * g->dnr) + (g->gor - (double)(ri - 1) * g->dvr);
+                const int ri = (int)floor((g->gor - g->rgor + (double)(roff - 1) * g->dnr + (double)(k - 1) * g->dnr) /
+                                          g->dvr) + 1;
+                const double distr = -(g->rgor - (double)(roff - 1) * g->dnr - (double)(k - 1) * g->dnr) +
+                                     (g->gor - (double)(ri - 1) * g->dvr);
                 double ui[4];
                 bspline4(distr / g->dvr, ui);
                 double sumi = 0.0;
@@ -118,7 +127,7 @@ int orc_gridder(const orc_grid *g, const double *velv, double *veln, int *nclamp
                     }
                     sumi = sumi + wi[i1 - 1] * sumj;
                 }
-                veln[VELN(g, i, j, k)] = sumi;
+                veln[(size_t)(i + 1) + VZ3 * ((size_t)(j + 1) + VX3 * (size_t)(k + 1))] = sumi;
             }
         }
     }
@@ -126,12 +135,19 @@ int orc_gridder(const orc_grid *g, const double *velv, double *veln, int *nclamp
     return nclamp ? -1 : 0;
 }
 
+int orc_gridder(const orc_grid *g, const double *velv, double *veln, int *nclamped)
+{
+    return gridder_block(g, velv, 1, 1, 1, g->nnr, g->nnx, g->nnz, veln, nclamped);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Serial fast marching (F:78-155, 535-1098, 6894-6961)                      */
 /* ------------------------------------------------------------------------ */
 typedef struct {
     const orc_grid *g;
-    const double *veln;
+    const double *veln;    /* gridded velocity, indices -1..n+1 of this (sub)domain */
+    int VZ3, VX3;          /* its strides: nnz+3, nnx+3 */
+    int roff, xoff, zoff;  /* global index of the (sub)domain's first node (F:6159-6168); 1 serially */
     int nnr, nnx, nnz;
     int NZ2, NX2;          /* padded strides: indices 0..n+1 like F:6191 */
     double *ttn;           /* padded (nnz+2)(nnx+2)(nnr+2) */
@@ -141,17 +157,33 @@ typedef struct {
 } fmm_state;
 
 #define TI(s, iz, ix, ir) ((size_t)(iz) + (size_t)(s)->NZ2 * ((size_t)(ix) + (size_t)(s)->NX2 * (size_t)(ir)))
+#define SV(s, iz, ix, ir) ((s)->veln[(size_t)((iz) + 1) + (size_t)(s)->VZ3 * ((size_t)((ix) + 1) + (size_t)(s)->VX3 * (size_t)((ir) + 1))])
+
+/* The whole grid as one domain (the serial run: offsets 1). */
+static void state_serial(fmm_state *s, const orc_grid *g, const double *veln)
+{
+    memset(s, 0, sizeof *s);
+    s->g = g;
+    s->veln = veln;
+    s->VZ3 = g->nnz + 3;
+    s->VX3 = g->nnx + 3;
+    s->roff = s->xoff = s->zoff = 1;
+    s->nnr = g->nnr; s->nnx = g->nnx; s->nnz = g->nnz;
+    s->NZ2 = g->nnz + 2; s->NX2 = g->nnx + 2;
+}
 #define TT(s, iz, ix, ir) ((s)->ttn[TI(s, iz, ix, ir)])
 #define NS(s, iz, ix, ir) ((s)->nsts[TI(s, iz, ix, ir)])
 
 static double sq(double x) { return x * x; }
 
-/* node radius and r*sin(colatitude) at the centre node (F:542-543, 642-643) */
+/* node radius and r*sin(colatitude) at the centre node (F:542-543, 642-643),
+ * with the subdomain offsets in the reference's operation order (they add
+ * exact zeros in the serial run) */
 static void centre_geom(const fmm_state *s, int ix, int ir, double *ri, double *risti)
 {
     const orc_grid *g = s->g;
-    *ri = g->rgor - (double)(ir - 1) * g->dnr + g->earth;
-    *risti = *ri * sin(g->rgox + (double)(ix - 1) * g->dnx);
+    *ri = g->rgor - (double)(s->roff - 1) * g->dnr - (double)(ir - 1) * g->dnr + g->earth;
+    *risti = *ri * sin(g->rgox + (double)(s->xoff - 1) * g->dnx + (double)(ix - 1) * g->dnx);
 }
 
 /* fouds1_all: first-order update over the eight octants (F:535-633). */
@@ -161,7 +193,7 @@ static void fouds1(fmm_state *s, int iz, int ix, int ir)
     const double dnr = g->dnr, dnx = g->dnx, dnz = g->dnz;
     double ri, risti;
     centre_geom(s, ix, ir, &ri, &risti);
-    const double slown = 1.0 / s->veln[VELN(g, iz, ix, ir)];
+    const double slown = 1.0 / SV(s, iz, ix, ir);
     int tsw1 = 0;
     double travm = 0.0;
     for (int i = ir - 1; i <= ir + 1; i += 2)
@@ -252,22 +284,24 @@ static int sw2(const fmm_state *s, int nb_alive, int nb2_in, int nb2_alive, doub
  * the given upwind flags (ai/aj/ak: neighbour used; swi/swj/swk == 0: that
  * axis second order).  Returns 1 and the octant time in *trav when some
  * axis is used. */
-static int octant2(const fmm_state *s, int iz, int ix, int ir, int i, int j, int k, int i2, int j2, int k2,
-                   int ai, int aj, int ak, int swi, int swj, int swk, double ri, double risti, double slown,
-                   double *trav)
+/* (ti/ti2, tj/tj2, tk/tk2: the first and second neighbour values of the
+ * octant along r, theta and phi; the second ones are read only on branches
+ * whose switch proved them in range) */
+static int octant2v(const orc_grid *g, double ti, double ti2, double tj, double tj2, double tk, double tk2,
+                    int ai, int aj, int ak, int swi, int swj, int swk, double ri, double risti, double slown,
+                    double *trav)
 {
-    const orc_grid *g = s->g;
     const double dnr = g->dnr, dnx = g->dnx, dnz = g->dnz;
         int swsol = 0;
         double a = 0, b = 0, c = 0, u, v, w, em, en, tref = 0, tdiv = 1.0;
         /* neighbour values; second neighbours are only read on the
          * branches whose switch proved them in range */
-#define TIv TT(s, iz, ix, i)
-#define TI2 TT(s, iz, ix, i2)
-#define TJv TT(s, iz, j, ir)
-#define TJ2 TT(s, iz, j2, ir)
-#define TKv TT(s, k, ix, ir)
-#define TK2 TT(s, k2, ix, ir)
+#define TIv ti
+#define TI2 ti2
+#define TJv tj
+#define TJ2 tj2
+#define TKv tk
+#define TK2 tk2
         if (swi == 0) {
             swsol = 1;
             if (swj == 0) {
@@ -489,13 +523,24 @@ static int octant2(const fmm_state *s, int iz, int ix, int ir, int i, int j, int
     return swsol;
 }
 
+/* One octant of fouds2_all from the (sub)domain's own field (F:710-993). */
+static int octant2(const fmm_state *s, int iz, int ix, int ir, int i, int j, int k, int i2, int j2, int k2,
+                   int ai, int aj, int ak, int swi, int swj, int swk, double ri, double risti, double slown,
+                   double *trav)
+{
+    const int i2in = i2 >= 1 && i2 <= s->nnr, j2in = j2 >= 1 && j2 <= s->nnx, k2in = k2 >= 1 && k2 <= s->nnz;
+    return octant2v(s->g, TT(s, iz, ix, i), i2in ? TT(s, iz, ix, i2) : 0.0, TT(s, iz, j, ir),
+                    j2in ? TT(s, iz, j2, ir) : 0.0, TT(s, k, ix, ir), k2in ? TT(s, k2, ix, ir) : 0.0, ai, aj, ak,
+                    swi, swj, swk, ri, risti, slown, trav);
+}
+
 /* fouds2_all: mixed-order update over the eight octants (F:635-1004). */
 static void fouds2(fmm_state *s, int iz, int ix, int ir)
 {
     const orc_grid *g = s->g;
     double ri, risti;
     centre_geom(s, ix, ir, &ri, &risti);
-    const double slown = 1.0 / s->veln[VELN(g, iz, ix, ir)];
+    const double slown = 1.0 / SV(s, iz, ix, ir);
     int tsw1 = 0;
     double travm = 0.0;
     for (int i = ir - 1; i <= ir + 1; i += 2) {
@@ -603,7 +648,7 @@ static double fp_update(fmm_state *s, int fom, int iz, int ix, int ir)
     const orc_grid *g = s->g;
     double ri, risti;
     centre_geom(s, ix, ir, &ri, &risti);
-    const double slown = 1.0 / s->veln[VELN(g, iz, ix, ir)];
+    const double slown = 1.0 / SV(s, iz, ix, ir);
     double best = INFINITY;
     for (int i = ir - 1; i <= ir + 1; i += 2)
         for (int j = ix - 1; j <= ix + 1; j += 2)
@@ -654,10 +699,7 @@ int orc_fixed_point(const orc_grid *g, const double *veln, int fom, const double
                     int max_sweeps, int *sweeps)
 {
     fmm_state s;
-    memset(&s, 0, sizeof s);
-    s.g = g; s.veln = veln;
-    s.nnr = g->nnr; s.nnx = g->nnx; s.nnz = g->nnz;
-    s.NZ2 = g->nnz + 2; s.NX2 = g->nnx + 2;
+    state_serial(&s, g, veln);
     const size_t npad = (size_t)s.NZ2 * (size_t)s.NX2 * (size_t)(g->nnr + 2);
     s.ttn = (double *)malloc(npad * sizeof(double));
     unsigned char *fixed = (unsigned char *)calloc(npad, 1);
@@ -679,10 +721,7 @@ int orc_fixed_point_field(const orc_grid *g, const double *veln, int fom, const 
                           const unsigned char *fixed_in, double *ttn, int max_sweeps, int *sweeps)
 {
     fmm_state s;
-    memset(&s, 0, sizeof s);
-    s.g = g; s.veln = veln;
-    s.nnr = g->nnr; s.nnx = g->nnx; s.nnz = g->nnz;
-    s.NZ2 = g->nnz + 2; s.NX2 = g->nnx + 2;
+    state_serial(&s, g, veln);
     const size_t npad = (size_t)s.NZ2 * (size_t)s.NX2 * (size_t)(g->nnr + 2);
     s.ttn = (double *)malloc(npad * sizeof(double));
     unsigned char *fixed = (unsigned char *)calloc(npad, 1);
@@ -824,14 +863,31 @@ static void visit(fmm_state *s, int fom, int iz, int ix, int ir)
     }
 }
 
+/* local_fmm (F:78-155): pop the earliest node, freeze it, update its
+ * far and trial neighbours inside the (sub)domain.  Returns the pops. */
+static long long local_fmm(fmm_state *s, int fom)
+{
+    long long pops = 0;
+    while (s->ntr > 0) {
+        const int ir = s->hr[1], ix = s->hx[1], iz = s->hz[1];
+        NS(s, iz, ix, ir) = 0;
+        downtree(s);
+        ++pops;
+        for (int i = ir - 1; i <= ir + 1; i += 2)
+            if (i >= 1 && i <= s->nnr) visit(s, fom, iz, ix, i);
+        for (int i = ix - 1; i <= ix + 1; i += 2)
+            if (i >= 1 && i <= s->nnx) visit(s, fom, iz, i, ir);
+        for (int i = iz - 1; i <= iz + 1; i += 2)
+            if (i >= 1 && i <= s->nnz) visit(s, fom, i, ix, ir);
+    }
+    return pops;
+}
+
 int orc_fmm(const orc_grid *g, const double *veln, int fom, const double *bottom,
             double *ttn, long long *npops)
 {
     fmm_state s;
-    memset(&s, 0, sizeof s);
-    s.g = g; s.veln = veln;
-    s.nnr = g->nnr; s.nnx = g->nnx; s.nnz = g->nnz;
-    s.NZ2 = g->nnz + 2; s.NX2 = g->nnx + 2;
+    state_serial(&s, g, veln);
     const size_t npad = (size_t)s.NZ2 * (size_t)s.NX2 * (size_t)(g->nnr + 2);
     const size_t nint = (size_t)g->nnz * (size_t)g->nnx * (size_t)g->nnr;
     s.ttn = (double *)calloc(npad, sizeof(double));
@@ -865,19 +921,7 @@ int orc_fmm(const orc_grid *g, const double *veln, int fom, const double *bottom
     long long pops = 0;
     if (sw) {
         addtree(&s, jtmin, itmin, rn);
-        /* local_fmm (F:88-154) */
-        while (s.ntr > 0) {
-            const int ir = s.hr[1], ix = s.hx[1], iz = s.hz[1];
-            NS(&s, iz, ix, ir) = 0;
-            downtree(&s);
-            ++pops;
-            for (int i = ir - 1; i <= ir + 1; i += 2)
-                if (i >= 1 && i <= s.nnr) visit(&s, fom, iz, ix, i);
-            for (int i = ix - 1; i <= ix + 1; i += 2)
-                if (i >= 1 && i <= s.nnx) visit(&s, fom, iz, i, ir);
-            for (int i = iz - 1; i <= iz + 1; i += 2)
-                if (i >= 1 && i <= s.nnz) visit(&s, fom, i, ix, ir);
-        }
+        pops = local_fmm(&s, fom);
     }
     for (int ir = 1; ir <= g->nnr; ++ir)
         for (int ix = 1; ix <= g->nnx; ++ix)
@@ -886,6 +930,429 @@ int orc_fmm(const orc_grid *g, const double *veln, int fom, const double *bottom
     if (npops) *npops = pops;
     free(s.ttn); free(s.nsts); free(s.hr); free(s.hx); free(s.hz);
     return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The decomposed run: nr x nx x nz subdomain ranks (F:6127-6168, 6371-6451)  */
+/* ------------------------------------------------------------------------ */
+/* Each block is one of the reference's compute ranks, emulated in turn
+ * inside every bulk-synchronous round: it marches its own nodes with
+ * local_fmm (stencils see only its own nodes), and before each march takes
+ * its neighbours' two boundary layers as ghosts (boundary_communication,
+ * F:6691-6795), re-solves the boundary nodes a ghost can lower with the face
+ * stencils in ghost order and reopens its heap (order_overlap, F:157-416).
+ * The rounds stop when no node of any block moved by more than 1e-5 s
+ * (error_calculate, F:6963-6987; the single-precision literal of F:6403).
+ *
+ * Faces in the reference's order (send_direction(1..6)): left (x-1), right
+ * (x+1), in (z-1), out (z+1), up (r-1), down (r+1). */
+enum { FC_LEFT, FC_RIGHT, FC_IN, FC_OUT, FC_UP, FC_DOWN };
+
+typedef struct {
+    fmm_state s;
+    double *vel;          /* this block's gridded velocity (its own gridder call) */
+    double *prev;         /* ttn_previous_step */
+    double *ghost[6][2];  /* ghost layers 1 and 2 of each face, one plane each */
+    int nb[6];            /* neighbour block, or -1 (no neighbour: MPI_PROC_NULL) */
+    int sw_fmm, dir_send, send_dir[6];
+} dec_block;
+
+/* node of the face plane with plane coordinates (a, b): left/right (iz, ir),
+ * in/out (ix, ir), up/down (iz, ix) */
+static int face_plane_n(const fmm_state *s, int f)
+{
+    return f <= FC_RIGHT ? s->nnz * s->nnr : (f <= FC_OUT ? s->nnx * s->nnr : s->nnz * s->nnx);
+}
+
+static int face_pidx(const fmm_state *s, int f, int iz, int ix, int ir)
+{
+    if (f <= FC_RIGHT) return (iz - 1) + s->nnz * (ir - 1);
+    if (f <= FC_OUT) return (ix - 1) + s->nnx * (ir - 1);
+    return (iz - 1) + s->nnz * (ix - 1);
+}
+
+/* ghost layer next to the face: 2 for left/in/up, 1 for right/out/down */
+static int face_adj(int f) { return (f == FC_LEFT || f == FC_IN || f == FC_UP) ? 2 : 1; }
+
+/* fouds2_left ... fouds2_down (F:1100-2825): a boundary node re-solved with
+ * its ghost neighbour across face f always taken (second order when the
+ * ghost layer next to the face is later than the one behind it), the two
+ * in-plane axes taken by value ("earlier than the node, or the node unset",
+ * second order when the second neighbour is set and earlier), over the four
+ * octants whose in-plane neighbours lie in the block.  The branch table is
+ * fouds2_all's (F:712-982) with the ghost axis always used.  The value is
+ * kept when it does not exceed the old one (or the node was unset), and the
+ * node goes into, or moves up in, the heap. */
+static void fouds2_face(dec_block *B, int f, int iz, int ix, int ir, double old_value)
+{
+    fmm_state *s = &B->s;
+    const orc_grid *g = s->g;
+    double ri, risti;
+    centre_geom(s, ix, ir, &ri, &risti);
+    const double slown = 1.0 / SV(s, iz, ix, ir);
+    const int ga = f >= FC_UP ? 0 : (f <= FC_RIGHT ? 1 : 2);     /* ghost axis: r, theta, phi */
+    const int p = face_pidx(s, f, iz, ix, ir);
+    const int adj = face_adj(f);
+    const double gt = B->ghost[f][adj - 1][p], gt2 = B->ghost[f][2 - adj][p];
+    const int gsw = gt > gt2 ? 0 : -1;
+    const double tc = TT(s, iz, ix, ir);
+    const int n[3] = {s->nnr, s->nnx, s->nnz};
+    const int c[3] = {ir, ix, iz};
+    /* the two in-plane axes */
+    int ax[2], m = 0;
+    for (int a = 0; a < 3; ++a)
+        if (a != ga) ax[m++] = a;
+    int tsw1 = 0;
+    double travm = 0.0;
+    for (int d0 = -1; d0 <= 1; d0 += 2)
+        for (int d1 = -1; d1 <= 1; d1 += 2) {
+            double t[3], t2[3];
+            int used[3], sw[3], inr = 1;
+            t[ga] = gt; t2[ga] = gt2; used[ga] = 1; sw[ga] = gsw;
+            for (int q = 0; q < 2; ++q) {
+                const int a = ax[q], d = q == 0 ? d0 : d1;
+                int pn[3] = {ir, ix, iz}, pn2[3] = {ir, ix, iz};
+                pn[a] = c[a] + d;
+                pn2[a] = c[a] + 2 * d;
+                const double tn = TT(s, pn[2], pn[1], pn[0]);   /* padded: 0 outside the block */
+                const int n2in = pn2[a] >= 1 && pn2[a] <= n[a];
+                const double tn2 = n2in ? TT(s, pn2[2], pn2[1], pn2[0]) : 0.0;
+                int w = (n2in && tn2 != 0.0) ? 0 : -1;
+                const int u = (tn < tc || tc == 0.0) && tn != 0.0;
+                if (u && w == 0) w = tn > tn2 ? 0 : -1;
+                else w = -1;
+                t[a] = tn; t2[a] = tn2; used[a] = u; sw[a] = w;
+                if (pn[a] < 1 || pn[a] > n[a]) inr = 0;
+            }
+            if (!inr) continue;
+            double trav;
+            if (octant2v(g, t[0], t2[0], t[1], t2[1], t[2], t2[2], used[0], used[1], used[2], sw[0], sw[1], sw[2],
+                         ri, risti, slown, &trav)) {
+                if (tsw1) travm = fmin(trav, travm);
+                else { travm = trav; tsw1 = 1; }
+            }
+        }
+    if (!tsw1) return;
+    if (old_value >= travm || old_value == 0.0) {
+        TT(s, iz, ix, ir) = travm;
+        if (NS(s, iz, ix, ir) <= 0) addtree(s, iz, ix, ir);
+        else updtree(s, iz, ix, ir);
+    }
+}
+
+/* order_overlap (F:157-416) */
+static void order_overlap(dec_block *B)
+{
+    fmm_state *s = &B->s;
+    const int nmax = s->nnr * s->nnx * s->nnz + 1;
+    int *ha = (int *)malloc(sizeof(int) * (size_t)(nmax + 1));
+    int *hb = (int *)malloc(sizeof(int) * (size_t)(nmax + 1));
+    double *hk = (double *)malloc(sizeof(double) * (size_t)(nmax + 1));
+    for (int f = 0; f < 6; ++f) {
+        if (B->send_dir[f] != 1) continue;
+        const int adj = face_adj(f);
+        const double *G = B->ghost[f][adj - 1];
+        /* the face's boundary nodes that a ghost can lower (or that are
+         * unset), in a heap keyed by the ghost value next to them, built by
+         * insertion in the reference's loop order */
+        int temp = 0;
+        const int outer = f >= FC_UP ? s->nnx : s->nnr;
+        const int inner = (f == FC_IN || f == FC_OUT) ? s->nnx : s->nnz;
+        for (int i = 1; i <= outer; ++i)
+            for (int j = 1; j <= inner; ++j) {
+                int iz, ix, ir;
+                switch (f) {
+                    case FC_LEFT:  iz = j; ix = 1;      ir = i; break;
+                    case FC_RIGHT: iz = j; ix = s->nnx; ir = i; break;
+                    case FC_IN:    iz = 1;      ix = j; ir = i; break;
+                    case FC_OUT:   iz = s->nnz; ix = j; ir = i; break;
+                    case FC_UP:    iz = j; ix = i; ir = 1; break;
+                    default:       iz = j; ix = i; ir = s->nnr; break;
+                }
+                const double gv = G[face_pidx(s, f, iz, ix, ir)];
+                const double tv = TT(s, iz, ix, ir);
+                if (!(gv < tv || tv == 0.0)) continue;
+                ++temp;
+                ha[temp] = j; hb[temp] = i; hk[temp] = gv;
+                int tpc = temp, tpp = tpc / 2;
+                while (tpp > 0) {
+                    if (gv < hk[tpp]) {
+                        int x = ha[tpc]; ha[tpc] = ha[tpp]; ha[tpp] = x;
+                        x = hb[tpc]; hb[tpc] = hb[tpp]; hb[tpp] = x;
+                        double y = hk[tpc]; hk[tpc] = hk[tpp]; hk[tpp] = y;
+                        tpc = tpp; tpp = tpc / 2;
+                    } else {
+                        tpp = 0;
+                    }
+                }
+            }
+        /* in ghost order: re-solve, then pop (downtree_left ... downtree_down,
+         * F:5747-6009) */
+        while (temp > 0) {
+            const int j = ha[1], i = hb[1];
+            int iz, ix, ir;
+            switch (f) {
+                case FC_LEFT:  iz = j; ix = 1;      ir = i; break;
+                case FC_RIGHT: iz = j; ix = s->nnx; ir = i; break;
+                case FC_IN:    iz = 1;      ix = j; ir = i; break;
+                case FC_OUT:   iz = s->nnz; ix = j; ir = i; break;
+                case FC_UP:    iz = j; ix = i; ir = 1; break;
+                default:       iz = j; ix = i; ir = s->nnr; break;
+            }
+            fouds2_face(B, f, iz, ix, ir, TT(s, iz, ix, ir));
+            if (temp == 1) { temp = 0; break; }
+            ha[1] = ha[temp]; hb[1] = hb[temp]; hk[1] = hk[temp];
+            --temp;
+            int tpp = 1, tpc = 2;
+            while (tpc < temp) {
+                if (hk[tpc] > hk[tpc + 1]) ++tpc;
+                if (hk[tpc] < hk[tpp]) {
+                    int x = ha[tpc]; ha[tpc] = ha[tpp]; ha[tpp] = x;
+                    x = hb[tpc]; hb[tpc] = hb[tpp]; hb[tpp] = x;
+                    double y = hk[tpc]; hk[tpc] = hk[tpp]; hk[tpp] = y;
+                    tpp = tpc; tpc = 2 * tpp;
+                } else {
+                    tpc = temp + 1;
+                }
+            }
+            if (tpc == temp && hk[tpc] < hk[tpp]) {
+                int x = ha[tpc]; ha[tpc] = ha[tpp]; ha[tpp] = x;
+                x = hb[tpc]; hb[tpc] = hb[tpp]; hb[tpp] = x;
+                double y = hk[tpc]; hk[tpc] = hk[tpp]; hk[tpp] = y;
+            }
+        }
+    }
+    free(ha); free(hb); free(hk);
+    /* reopen (F:387-415): nodes between the heap's earliest and latest value
+     * go back into the heap, earlier ones are frozen, later ones far */
+    if (s->ntr >= 1) {
+        B->sw_fmm = 1;
+        const double mini = hval(s, 1);
+        double maxi = 0.0;
+        for (int q = 1; q <= s->ntr; ++q)
+            if (hval(s, q) > maxi) maxi = hval(s, q);
+        for (int ir = 1; ir <= s->nnr; ++ir)
+            for (int ix = 1; ix <= s->nnx; ++ix)
+                for (int iz = 1; iz <= s->nnz; ++iz) {
+                    if (NS(s, iz, ix, ir) > 0) continue;
+                    const double v = TT(s, iz, ix, ir);
+                    if (v > 0.0) {
+                        if (v <= mini) NS(s, iz, ix, ir) = 0;
+                        else if (v >= maxi) NS(s, iz, ix, ir) = -1;
+                        else addtree(s, iz, ix, ir);
+                    } else {
+                        NS(s, iz, ix, ir) = -1;
+                    }
+                }
+    }
+}
+
+/* one axis of the block split (F:6127-6168): sizes n/np (+1 for the first
+ * n mod np ranks), offsets contiguous from 1 */
+static void split_axis(int n, int np, int rank, int *num, int *off)
+{
+    int o = 1;
+    for (int r = 0; r <= rank; ++r) {
+        const int sz = n / np + ((n % np) && r < n % np ? 1 : 0);
+        if (r == rank) { *num = sz; *off = o; }
+        o += sz;
+    }
+}
+
+/* threads for the blocks of a round: one per block unless
+ * ORC_DECOMPOSED_THREADS says otherwise (1 = the blocks in turn) */
+static int dec_threads(int nb)
+{
+    const char *e = getenv("ORC_DECOMPOSED_THREADS");
+    const int t = e ? atoi(e) : nb;
+    return t >= 1 ? t : 1;
+}
+
+int orc_fmm_decomposed(const orc_grid *g, const double *velv, int fom, const double *bottom, int nr, int nx,
+                       int nz, int max_rounds, double *ttn, int *rounds_out)
+{
+    const int nb = nr * nx * nz;
+    if (nr < 1 || nx < 1 || nz < 1 || g->nnr / nr < 2 || g->nnx / nx < 2 || g->nnz / nz < 2) return -2;
+    dec_block *B = (dec_block *)calloc((size_t)nb, sizeof(dec_block));
+    if (!B) return -3;
+    int rc = 0;
+    for (int br = 0; br < nr; ++br)
+        for (int bx = 0; bx < nx; ++bx)
+            for (int bz = 0; bz < nz; ++bz) {
+                dec_block *b = &B[(br * nx + bx) * nz + bz];
+                fmm_state *s = &b->s;
+                int rnum, xnum, znum, roff, xoff, zoff;
+                split_axis(g->nnr, nr, br, &rnum, &roff);
+                split_axis(g->nnx, nx, bx, &xnum, &xoff);
+                split_axis(g->nnz, nz, bz, &znum, &zoff);
+                memset(s, 0, sizeof *s);
+                s->g = g;
+                s->roff = roff; s->xoff = xoff; s->zoff = zoff;
+                s->nnr = rnum; s->nnx = xnum; s->nnz = znum;
+                s->NZ2 = znum + 2; s->NX2 = xnum + 2;
+                s->VZ3 = znum + 3; s->VX3 = xnum + 3;
+                const size_t npad = (size_t)s->NZ2 * (size_t)s->NX2 * (size_t)(rnum + 2);
+                const size_t nint = (size_t)znum * (size_t)xnum * (size_t)rnum;
+                b->vel = (double *)malloc(sizeof(double) * (size_t)(znum + 3) * (size_t)(xnum + 3) * (size_t)(rnum + 3));
+                s->ttn = (double *)calloc(npad, sizeof(double));
+                s->nsts = (int *)malloc(npad * sizeof(int));
+                s->hr = (int *)malloc((nint + 2) * sizeof(int));
+                s->hx = (int *)malloc((nint + 2) * sizeof(int));
+                s->hz = (int *)malloc((nint + 2) * sizeof(int));
+                b->prev = (double *)calloc(nint, sizeof(double));
+                for (int f = 0; f < 6; ++f)
+                    for (int l = 0; l < 2; ++l) b->ghost[f][l] = (double *)calloc((size_t)face_plane_n(s, f), sizeof(double));
+                if (!b->vel || !s->ttn || !s->nsts || !s->hr || !s->hx || !s->hz || !b->prev) { rc = -3; continue; }
+                for (int f = 0; f < 6; ++f)
+                    if (!b->ghost[f][0] || !b->ghost[f][1]) rc = -3;
+                s->veln = b->vel;
+                int ncl = 0;
+                gridder_block(g, velv, roff, xoff, zoff, rnum, xnum, znum, b->vel, &ncl);
+                for (size_t q = 0; q < npad; ++q) s->nsts[q] = -1;
+                b->nb[FC_LEFT] = bx > 0 ? (br * nx + bx - 1) * nz + bz : -1;
+                b->nb[FC_RIGHT] = bx < nx - 1 ? (br * nx + bx + 1) * nz + bz : -1;
+                b->nb[FC_IN] = bz > 0 ? (br * nx + bx) * nz + bz - 1 : -1;
+                b->nb[FC_OUT] = bz < nz - 1 ? (br * nx + bx) * nz + bz + 1 : -1;
+                b->nb[FC_UP] = br > 0 ? ((br - 1) * nx + bx) * nz + bz : -1;
+                b->nb[FC_DOWN] = br < nr - 1 ? ((br + 1) * nx + bx) * nz + bz : -1;
+            }
+    if (rc) goto done;
+    {
+        /* start_fmm (F:6894-6961) on the bottom blocks: load their part of
+         * the frame, freeze positive values; the block (or blocks) holding
+         * the earliest time seed their heap with it and march */
+        double gmin = INFINITY;
+        double bmin[4096];
+        int bi[4096], bj[4096];
+        if (nx * nz > 4096) { rc = -2; goto done; }
+        for (int q = 0; q < nx * nz; ++q) {
+            dec_block *b = &B[(nr - 1) * nx * nz + q];
+            fmm_state *s = &b->s;
+            const int rn = s->nnr;
+            int sw = 0;
+            double ttmin = -100.0;
+            for (int i = 1; i <= s->nnx; ++i)
+                for (int j = 1; j <= s->nnz; ++j) {
+                    const int xg = s->xoff + i - 1, zg = s->zoff + j - 1;
+                    const double rd1 = bottom[(size_t)(zg - 1) + (size_t)g->nnz * (size_t)(xg - 1)];
+                    TT(s, j, i, rn) = rd1;
+                    if (rd1 > 0.0) {
+                        if (sw == 0) { ttmin = rd1; bi[q] = i; bj[q] = j; sw = 1; }
+                        else if (rd1 < ttmin) { ttmin = rd1; bi[q] = i; bj[q] = j; }
+                        NS(s, j, i, rn) = 0;
+                    } else {
+                        TT(s, j, i, rn) = 0.0;
+                    }
+                }
+            bmin[q] = ttmin;
+            if (ttmin != -100.0 && ttmin < gmin) gmin = ttmin;
+        }
+        for (int q = 0; q < nx * nz; ++q) {
+            if (bmin[q] == -100.0 || bmin[q] > gmin) continue;   /* F:6945-6955 */
+            dec_block *b = &B[(nr - 1) * nx * nz + q];
+            addtree(&b->s, bj[q], bi[q], b->s.nnr);
+            local_fmm(&b->s, fom);
+            b->sw_fmm = 1;
+        }
+    }
+    {
+        const double tol = (double)0.00001f;      /* F:6403, a default-kind literal */
+        double err = 0.0;
+        int rounds = 0;
+        for (;;) {
+            /* error_calculate (F:6963-6987): the largest change of any node */
+            err = 0.0;
+            for (int q = 0; q < nb; ++q) {
+                fmm_state *s = &B[q].s;
+                size_t k = 0;
+                for (int ir = 1; ir <= s->nnr; ++ir)
+                    for (int ix = 1; ix <= s->nnx; ++ix)
+                        for (int iz = 1; iz <= s->nnz; ++iz, ++k) {
+                            const double d = fabs(TT(s, iz, ix, ir) - B[q].prev[k]);
+                            if (d > err) err = d;
+                        }
+            }
+            if (!(err > tol)) break;
+            if (rounds >= max_rounds) { rc = -4; break; }
+            ++rounds;
+            for (int q = 0; q < nb; ++q) {
+                fmm_state *s = &B[q].s;
+                size_t k = 0;
+                for (int ir = 1; ir <= s->nnr; ++ir)
+                    for (int ix = 1; ix <= s->nnx; ++ix)
+                        for (int iz = 1; iz <= s->nnz; ++iz, ++k) B[q].prev[k] = TT(s, iz, ix, ir);
+                B[q].dir_send = B[q].sw_fmm;
+                B[q].sw_fmm = 0;
+            }
+            for (int q = 0; q < nb; ++q)
+                for (int f = 0; f < 6; ++f)
+                    if (B[q].nb[f] >= 0) B[q].send_dir[f] = B[B[q].nb[f]].dir_send;
+            /* boundary_communication: the neighbour's two layers next to the
+             * face, layer 1 the farther one for left/in/up */
+            for (int q = 0; q < nb; ++q) {
+                fmm_state *s = &B[q].s;
+                for (int f = 0; f < 6; ++f) {
+                    if (B[q].send_dir[f] != 1) continue;
+                    const fmm_state *o = &B[B[q].nb[f]].s;
+                    for (int l = 1; l <= 2; ++l) {
+                        double *G = B[q].ghost[f][l - 1];
+                        switch (f) {
+                            case FC_LEFT:   /* left's x = n-1, n */
+                            case FC_RIGHT: { /* right's x = 1, 2 */
+                                const int xs = f == FC_LEFT ? o->nnx - 2 + l : l;
+                                for (int ir = 1; ir <= s->nnr; ++ir)
+                                    for (int iz = 1; iz <= s->nnz; ++iz)
+                                        G[face_pidx(s, f, iz, 0, ir)] = TT(o, iz, xs, ir);
+                                break;
+                            }
+                            case FC_IN:
+                            case FC_OUT: {
+                                const int zs = f == FC_IN ? o->nnz - 2 + l : l;
+                                for (int ir = 1; ir <= s->nnr; ++ir)
+                                    for (int ix = 1; ix <= s->nnx; ++ix)
+                                        G[face_pidx(s, f, 0, ix, ir)] = TT(o, zs, ix, ir);
+                                break;
+                            }
+                            default: {
+                                const int rs = f == FC_UP ? o->nnr - 2 + l : l;
+                                for (int ix = 1; ix <= s->nnx; ++ix)
+                                    for (int iz = 1; iz <= s->nnz; ++iz)
+                                        G[face_pidx(s, f, iz, ix, 0)] = TT(o, iz, ix, rs);
+                                break;
+                            }
+                        }
+                    }
+                }
+            }
+            /* the ranks' work of a round is independent given the ghosts:
+             * one thread per block (the reference's one process per rank) */
+#pragma omp parallel for schedule(dynamic, 1) num_threads(dec_threads(nb))
+            for (int q = 0; q < nb; ++q) {
+                order_overlap(&B[q]);
+                local_fmm(&B[q].s, fom);
+            }
+        }
+        if (rounds_out) *rounds_out = rounds;
+        /* the blocks' nodes into the global field */
+        for (int q = 0; q < nb; ++q) {
+            fmm_state *s = &B[q].s;
+            for (int ir = 1; ir <= s->nnr; ++ir)
+                for (int ix = 1; ix <= s->nnx; ++ix)
+                    for (int iz = 1; iz <= s->nnz; ++iz) {
+                        const size_t gz = (size_t)(s->zoff + iz - 2), gx = (size_t)(s->xoff + ix - 2),
+                                     gr = (size_t)(s->roff + ir - 2);
+                        ttn[gz + (size_t)g->nnz * (gx + (size_t)g->nnx * gr)] = TT(s, iz, ix, ir);
+                    }
+        }
+    }
+done:
+    for (int q = 0; q < nb; ++q) {
+        free(B[q].vel); free(B[q].prev);
+        free(B[q].s.ttn); free(B[q].s.nsts); free(B[q].s.hr); free(B[q].s.hx); free(B[q].s.hz);
+        for (int f = 0; f < 6; ++f) { free(B[q].ghost[f][0]); free(B[q].ghost[f][1]); }
+    }
+    free(B);
+    return rc;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -75,6 +75,21 @@ int orc_gridder(const orc_grid *g, const double *velv, double *veln, int *nclamp
 int orc_fmm(const orc_grid *g, const double *veln, int fom, const double *bottom,
             double *ttn, long long *npops);
 
+/* The reference's decomposed run (its mpirun -np 9 layout with nr = nx = nz
+ * = 2, F:6052-6056): the grid split into nr x nx x nz blocks like F:6127-6168,
+ * each block an emulated rank with its own gridder call (F:6172), start_fmm
+ * on the bottom blocks (the block holding the earliest boundary time seeds
+ * and marches), then bulk-synchronous rounds (F:6371-6451): exchange of the
+ * two boundary layers with the neighbours that changed (F:6691-6795),
+ * order_overlap with the face stencils fouds2_left .. fouds2_down and the
+ * reopen pass (F:157-416, 1100-2825, 5747-6009), local_fmm, until no node
+ * moved by more than the single-precision literal 1e-5 s (F:6403,
+ * 6963-6987).  velv (not the gridded velocity): every block grids its own
+ * nodes with its offsets.  Returns 0, -4 after max_rounds, -2 for blocks
+ * thinner than two nodes, -3 out of memory; *rounds the rounds run. */
+int orc_fmm_decomposed(const orc_grid *g, const double *velv, int fom, const double *bottom, int nr, int nx,
+                       int nz, int max_rounds, double *ttn, int *rounds);
+
 /* Fixed point of the reference's stencil: the same octant formulas
  * (fouds1_all / fouds2_all) with the heap's "alive" test restated as
  * "earlier than the node", iterated by Gauss-Seidel sweeps in alternating
