@@ -269,6 +269,44 @@ class CpuPool:
         self.pool.join()
 
 
+def cpu_modes():
+    """The reference's two single-event CPU layouts on the 64^3 plane-wave
+    event (the plain single-event workload), timed with the oracle: (a) the
+    serial march (one rank), (b) the 2 x 2 x 2 decomposed run, its eight
+    blocks on eight threads (the reference's mpirun -np 9 compute ranks).
+    Seconds per solve, median of three."""
+    import numpy as np
+    import oracle as O
+    from fm3dt import synth
+    O.build()
+    w = synth.config(0)
+    h = w.header
+    g = O.grid_from_header(h.nv, h.vorig, h.vstep, h.nn, h.norig, h.nstep, h.earth)
+    veln, _ = O.gridder(g, w.velv)
+    fr = O.planewave_frame(g, O.PlaneWave(*synth.planewave_params(h, *w.events[0])))
+
+    def med(f):
+        ts = []
+        for _ in range(3):
+            t = time.perf_counter()
+            f()
+            ts.append(time.perf_counter() - t)
+        return statistics.median(ts)
+
+    old = os.environ.get("ORC_DECOMPOSED_THREADS")
+    os.environ["ORC_DECOMPOSED_THREADS"] = "8"
+    try:
+        a = med(lambda: O.fmm(g, veln, fr, 1))
+        b = med(lambda: O.fmm_decomposed(g, w.velv, fr, 1, (2, 2, 2)))
+    finally:
+        if old is None:
+            os.environ.pop("ORC_DECOMPOSED_THREADS", None)
+        else:
+            os.environ["ORC_DECOMPOSED_THREADS"] = old
+    return {"workload": "config0: 64x64x64, one plane-wave event", "unit": "s/solve",
+            "a_serial_march": a, "b_decomposed_2x2x2_8_threads": b}
+
+
 def cpu_model():
     try:
         for line in open("/proc/cpuinfo"):
@@ -436,22 +474,26 @@ def run_ours(a):
     p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
     # The two solver kernels: the rounds (nodes of staged tiles) and the
     # directional sweep.  The solver's sweep interval (start of the sweep to
-    # the end of the other events' main sweep) holds only sweep launches:
-    # every event's main sweep, on the context stream and, for the near-tie
-    # events, beside it on the second stream.  The rounds' interval also holds
-    # the near-tie events' extra sweeps, which run beside the first round, so
-    # no interval times the round kernel alone.  The roofline line reports
-    # the kernel with more work (warp instructions per node from the ncu count
-    # x nodes; device time when there is no count) and, for the sweep, the
-    # main sweeps' nodes over the sweep interval: a lower bound, since the
-    # near-tie events' extra sweeps start in that interval too.
+    # the end of the other events' main sweep, plus the re-sweeps) holds only
+    # sweep launches: every event's main sweep, on the context stream and, for
+    # the near-tie events, beside it on the second stream, and the re-sweeps.
+    # The rounds' interval also holds the near-tie events' extra sweeps, which
+    # run beside the first round, so no interval times the round kernel
+    # alone.  The roofline line reports the kernel with more work (warp
+    # instructions per node from the ncu count x nodes; device time when there
+    # is no count) and, for the sweep, the nodes swept inside the sweep
+    # interval over its time: a lower bound, since the near-tie events' extra
+    # sweeps can start in that interval too.
     round_ms = sum(s["round_ms"] for s in sts)
     round_launches = sum(s["round_launches"] for s in sts)
     staged = sum(s["tile_nodes"] for s in sts)
     sweep_ms = sum(s["sweep_ms"] for s in sts)
     sweep_launches = sum(s["sweep_launches"] for s in sts)
     sweep_nodes = sum(s["sweep_nodes"] for s in sts)
-    main_nodes = nev * nnr * nnx * nnz * a.steps if a.sweep_mode == 1 else sweep_nodes
+    # nodes swept inside the sweep interval: every event's main sweep and the
+    # re-sweeps (the near-tie events' extra sweeps fall in the rounds' interval
+    # when the batch is solved in two parts)
+    main_nodes = sum(s["interval_nodes"] for s in sts)
     sweep_name = "stream_sweep_kernel" if sweep_shape_dims[0] == "stream" else "sweep_kernel"
     # name: (interval ms, nodes in it, launches, nodes of all launches)
     kernels = {
@@ -567,7 +609,8 @@ def run_ours(a):
                                 "sample": f"{cores} events of this workload at once, one per core: the oracle's "
                                           f"serial fast marching (restatement of local_fmm)"
                                           + (", srtimes and parallel_rpaths" if forward else "") +
-                                          f"; {t:.1f} s for the slowest core (set-up excluded)"}
+                                          f"; {t:.1f} s for the slowest core (set-up excluded)",
+                                "modes": cpu_modes()}
     if rank == 0:
         print(json.dumps(line), flush=True)
     solver.close()

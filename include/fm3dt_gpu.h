@@ -81,6 +81,9 @@ typedef struct {
                                  batches solved in two parts, until the other events' main
                                  sweep ends) plus any re-sweeps */
     int64_t sweep_nodes;      /* grid nodes staged by all sweep passes */
+    int64_t interval_nodes;   /* of those, the nodes swept inside the sweep interval (the main
+                                 sweeps and any re-sweeps; in batches solved in two parts the
+                                 near-tie events' main sweep counts, their extra sweeps not) */
 } fm3dt_status;
 
 typedef struct fm3dt_ctx fm3dt_ctx;

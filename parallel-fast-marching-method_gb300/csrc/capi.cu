@@ -405,6 +405,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     // 1. directional sweep, one launch per tile hyperplane
     int sweep_launches = 0;
     int64_t sweep_nodes = 0;      // nodes visited by all sweep passes
+    int64_t interval_nodes = 0;   // ... by the passes inside the sweep interval
     bool verified = false;
     const bool streaming = ctx->sweep_shape >= kNumShapes;
     const int sidx = streaming ? ctx->sweep_shape - kNumShapes : 0;
@@ -508,8 +509,10 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         }
         CKL();
         verified = ctx->verify != 0;
+        interval_nodes = sweep_nodes;
     } else if (do_sweep) {
         sweep_nodes = (int64_t)nev * (int64_t)ctx->N;
+        interval_nodes = sweep_nodes;
         const int sshape = ctx->sweep_shape;
         int rc = ensure_planes(ctx, sshape);
         if (rc) return rc;
@@ -677,6 +680,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         const int rc = stream_pass((int)busy.size(), ctx->d_events, 0, 0, ctx->d_flag, ctx->d_list[nl],
                                    ctx->d_count[nl], s, false);
         if (rc) return rc;
+        interval_nodes += (int64_t)busy.size() * (int64_t)ctx->N;
         CK(cudaEventRecord(r1, s));
         CKL();
         CK(cudaMemcpyAsync(ctx->h_count, ctx->d_count[nl], sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -716,6 +720,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             rc = stream_pass((int)others.size(), ctx->d_events_b, 0, ctx->sweep_segments, nullptr, ctx->d_list[0],
                              ctx->d_count[0], s, FM_FRESH_SWEEP);
             if (rc) return rc;
+            interval_nodes += (int64_t)nev * (int64_t)ctx->N;
             CK(cudaEventRecord(sw1, s));
             CK(cudaEventRecord(r0, s));
         }
@@ -827,6 +832,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         st->sweep_ms = do_sweep ? sms + resweep_ms : 0.0;
         st->sweep_launches = sweep_launches;
         st->sweep_nodes = sweep_nodes;
+        st->interval_nodes = interval_nodes;
     }
     if (kerr == 2) return fail(ctx, FM3DT_ECUDA, "a tile copy (TMA) destination was not 128-byte aligned");
     if (kerr) return fail(ctx, FM3DT_ECUDA, "a tile copy (TMA) did not complete in time");

@@ -61,9 +61,12 @@ __device__ float trilinf(const Geom &g, const double *veln, int ipz, int ipx, in
     return vel;
 }
 
+constexpr int kRayBlock = 64;
+
 template <typename R>
-__global__ void rays_kernel(RayArgs a)
+__global__ void __launch_bounds__(kRayBlock) rays_kernel(RayArgs a)
 {
+    __shared__ float ray_acc[64 * kRayBlock];
     const Geom g = a.g;
     const int total = a.nev * a.nrc;
     const size_t NB = (size_t)g.nnx * g.nnz;
@@ -78,6 +81,37 @@ __global__ void rays_kernel(RayArgs a)
         const int e = q / a.nrc, i = q - e * a.nrc;
         const R *Te = (const R *)a.T + (size_t)e * N;
         float *fdm = a.fdm ? a.fdm + nmp * (size_t)q : nullptr;
+        // The row's sums for the velocity cell whose 4 x 4 x 4 B-spline
+        // support the ray is in (one slot per support node, in shared memory,
+        // this thread's slots strided by the block size so that a warp's
+        // threads hit 32 different banks); added to the row when the ray
+        // moves to another cell and at its end.  In the row each node's value
+        // is the REAL(4) sum of its terms in ray order, grouped per cell visit.
+        float *acc = ray_acc + threadIdx.x;
+        int acc_r = -1, acc_x = -1, acc_z = -1;
+        for (int t = 0; t < 64; ++t) acc[t * kRayBlock] = 0.0f;
+        auto flush = [&]() {
+            if (acc_r < 0) return;
+            const size_t zstride = (size_t)(g.nvr + 2) * (size_t)(g.nvx + 2);
+            // a row of four nodes (along phi) at a time: four independent
+            // loads, then the four sums stored
+#pragma unroll 1
+            for (int nm = 0; nm < 16; ++nm) {
+                const int n = nm >> 2, m = nm & 3;
+                float *p = fdm + (size_t)(acc_r - 1 + n) +
+                           (size_t)(g.nvr + 2) * ((size_t)(acc_x - 1 + m) + (size_t)(g.nvx + 2) * (size_t)(acc_z - 1));
+                const float o0 = p[0], o1 = p[zstride], o2 = p[2 * zstride], o3 = p[3 * zstride];
+                float *c = acc + (nm * 4) * kRayBlock;
+                p[0] = c[0] + o0;
+                p[zstride] = c[kRayBlock] + o1;
+                p[2 * zstride] = c[2 * kRayBlock] + o2;
+                p[3 * zstride] = c[3 * kRayBlock] + o3;
+                c[0] = 0.0f;
+                c[kRayBlock] = 0.0f;
+                c[2 * kRayBlock] = 0.0f;
+                c[3 * kRayBlock] = 0.0f;
+            }
+        };
         auto TD = [&](int iz, int ix, int ir) -> double {
             return (double)Te[((size_t)(ir - 1) * g.nnx + (ix - 1)) * g.nnz + (iz - 1)];
         };
@@ -253,16 +287,22 @@ __global__ void rays_kernel(RayArgs a)
                             st = 1;
                             continue;
                         }
-                        const size_t zstride = (size_t)(g.nvr + 2) * (size_t)(g.nvx + 2);
+                        // a sub-segment in another support cell: the current
+                        // cell's sums go to the row first
+                        if (ivrt != acc_r || ivxt != acc_x || ivzt != acc_z) {
+                            flush();
+                            acc_r = ivrt; acc_x = ivxt; acc_z = ivzt;
+                        }
+#pragma unroll 1
                         for (int n = 0; n < 4; ++n)
+#pragma unroll
                             for (int m = 0; m < 4; ++m) {
-                                float *rowp = fdm + (size_t)(ivrt - 1 + n) +
-                                              (size_t)(g.nvr + 2) * ((size_t)(ivxt - 1 + m) + (size_t)(g.nvx + 2) * (size_t)(ivzt - 1));
                                 const float uv = ui[n] * vi[m] * iv2, uvo = uio[n] * vio[m] * iv2o;
+#pragma unroll
                                 for (int l = 0; l < 4; ++l) {
                                     const float a1 = -(uv * wi[l] + uvo * wio[l]) * hd;
-                                    float *p = rowp + zstride * (size_t)l;
-                                    *p = a1 + *p;
+                                    float &c = acc[((n * 4 + m) * 4 + l) * kRayBlock];
+                                    c = a1 + c;
                                 }
                             }
                     }
@@ -271,6 +311,7 @@ __global__ void rays_kernel(RayArgs a)
                 if (stop) break;
             }
         }
+        if (fdm) flush();
         if (st && a.flags) atomicMin(&a.flags[0], q);
         if (a.endpoints) {
             a.endpoints[3 * (size_t)q] = rgr;
@@ -422,7 +463,7 @@ void launch_row_scan(const int64_t *counts, int nrows, int64_t *row_ptr, int64_t
 void launch_rays(const RayArgs &a, cudaStream_t st)
 {
     const int total = a.nev * a.nrc;
-    const int block = 64;
+    const int block = kRayBlock;
     const int blocks = (total + block - 1) / block;
     if (blocks <= 0) return;
     if (a.prec == FM3DT_FP64)

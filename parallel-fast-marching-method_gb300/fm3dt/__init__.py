@@ -47,7 +47,7 @@ class Status(C.Structure):
     _fields_ = [("rounds", C.c_int), ("converged", C.c_int), ("tile_updates", C.c_int64),
                 ("node_passes", C.c_int64), ("tile_nodes", C.c_int64), ("ms", C.c_double),
                 ("round_ms", C.c_double), ("round_launches", C.c_int), ("sweep_launches", C.c_int),
-                ("sweep_ms", C.c_double), ("sweep_nodes", C.c_int64)]
+                ("sweep_ms", C.c_double), ("sweep_nodes", C.c_int64), ("interval_nodes", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -134,3 +134,38 @@ def test_tomography_grid_event_full_size(gpu_lib, orc):
     from fm3dt import synth
     w = synth.config(3, nev=500)
     _end_to_end(orc, 3, w.events[:1], precisions=(0, 1))
+
+
+@pytest.mark.parametrize("cfg,nev", [(0, 1), (1, 2)])
+def test_against_the_reference_decomposed_run(gpu_lib, orc, cfg, nev):
+    """What the reference's own production run (mpirun -np 9: 2 x 2 x 2
+    blocks, oracle.fmm_decomposed) would print, against the GPU.  The
+    decomposed run is a different discretisation near block faces and edges
+    (first-order terms where a second neighbour lies in another block; edge
+    nodes re-solved by the face stencils only), so it differs from the
+    serial march -- which the GPU equals -- by more than the 1e-5 bar:
+    measured 7.3e-2 s / 1.0e-4 relative at receivers on the 64^3 event,
+    2.8e-2 to 3.7e-2 s / 5.7e-5 on 128^3 events.  The test states that gap
+    and bounds it at twice the measured relative size."""
+    import fm3dt
+    from fm3dt import synth
+    w = synth.config(cfg, nev=nev)
+    h = w.header
+    params = np.array([synth.planewave_params(h, *ev) for ev in w.events])
+    g = orc.grid_from_header(h.nv, h.vorig, h.vstep, h.nn, h.norig, h.nstep, h.earth)
+    rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat, w.rec_lon)
+    rcr = np.asarray(w.rec_elev, dtype=np.float64)
+    with fm3dt.Solver(h, fom=1, precision=fm3dt.FP64, max_events=len(params)) as s:
+        s.set_velocity(w.velv)
+        s.solve_planewave(params)
+        gt = s.receiver_times(rcr, rcx, rcz).astype(np.float64)
+    worst_rel = worst_abs = 0.0
+    for e, p in enumerate(params):
+        frame = orc.planewave_frame(g, orc.PlaneWave(*p))
+        dec, rounds = orc.fmm_decomposed(g, w.velv, frame, 1, (2, 2, 2))
+        assert rounds <= 8
+        rt = orc.srtimes(g, dec, rcr, rcx, rcz).astype(np.float64)
+        worst_rel = max(worst_rel, float(np.max(np.abs(gt[e] - rt) / rt)))
+        worst_abs = max(worst_abs, float(np.max(np.abs(gt[e] - rt))))
+    print(f"\nconfig {cfg} {h.nn}: GPU vs the 2x2x2 run at receivers: {worst_abs:.3e} s, {worst_rel:.2e} relative")
+    assert worst_rel <= 2.5e-4 and worst_abs <= 0.15
