@@ -73,6 +73,10 @@ def parse():
                     help="with --shape: 1 sweep then rounds, 2 sweep + verifying sweep, 0 no sweep")
     ap.add_argument("--segments", type=int, nargs=2, default=(0, 0),
                     help="streaming sweep height segments (all events, near-tie events); 0 = automatic")
+    ap.add_argument("--schedule", type=float, nargs=4, default=None,
+                    metavar=("TIE_SWEEPS", "TIE_RATIO", "RESWEEPS", "RESWEEP_FRAC"),
+                    help="with --shape: the solve schedule (negative keeps the default); without --shape the "
+                         "autotuner picks it")
     return ap.parse_args()
 
 
@@ -408,7 +412,9 @@ def run_ours(a):
         sweep_shape = a.sweep_shape if a.sweep_shape >= 0 else a.shape
         solver.set_tuning(a.shape, a.passes or 64, 0, a.sweep_mode)
         solver.set_sweep_shape(sweep_shape)
-        tuned = (a.shape, a.passes or 64, sweep_shape, None)
+        if a.schedule:
+            solver.set_schedule(int(a.schedule[0]), a.schedule[1], int(a.schedule[2]), a.schedule[3])
+        tuned = (a.shape, a.passes or 64, sweep_shape, None, tuple(a.schedule) if a.schedule else None)
     else:
         # (tuned on up to 128 of the events: the choice never changes results)
         tuned = autotune.autotune(solver, fptr, min(nev, 128), device=True)
@@ -576,7 +582,9 @@ def run_ours(a):
         "warmup": a.warmup, "ms_per_step": 1000.0 * step_s / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": a.prec, "data": "synthetic",
         "config": workload_config(a.config, a.step, h, nev, nrc, a.prec),
-        "tuning": {"tile_shape": list(shape), "max_passes": tuned[1], "sweep_tile_shape": list(sweep_shape_dims)},
+        "tuning": {"tile_shape": list(shape), "max_passes": tuned[1], "sweep_tile_shape": list(sweep_shape_dims),
+                   "schedule": dict(zip(("tie_sweeps", "tie_ratio", "resweeps", "resweep_frac"), tuned[4]))
+                   if tuned[4] else "default"},
         "p50_ms": p50, "p99_ms": p99,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -220,6 +220,15 @@ int fm3dt_set_times(fm3dt_ctx *ctx, int event, int nev_total, const double *ttn)
  * rounds with every tile).  None of these changes the converged field. */
 int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rounds, int sweep);
 
+/* Solve schedule (a negative value keeps the current one): extra sweeps of the
+ * near-tie events, alternating reversed and forward (0..16, default 2); the
+ * near-tie band, a lateral component below tie_ratio times the other (0..1,
+ * default 0.1: within ~6 degrees of an axis); re-sweeps after the first rounds
+ * (0..16, default 4) of the events with more than resweep_frac of their tiles
+ * still queued (default 0.01).  None of these changes the converged field;
+ * the best values depend on the model's heterogeneity. */
+int fm3dt_set_schedule(fm3dt_ctx *ctx, int tie_sweeps, double tie_ratio, int resweeps, double resweep_frac);
+
 /* Shape of the directional sweep (independent of the rounds' shape): a tile
  * shape index 0..count-1 of fm3dt_tile_shapes (tile sweep), or count +
  * 0 / 1 for the streaming sweep, one warp per 4x8 / 2x16 block of

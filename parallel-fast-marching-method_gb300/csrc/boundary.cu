@@ -73,17 +73,12 @@ __global__ void finalize_kernel(Geom g, const double *__restrict__ frames, R *__
     }
 }
 
-// Lateral components within this ratio of each other count as a near tie.
-#ifndef FM_TIE_RATIO
-#define FM_TIE_RATIO 0.1
-#endif
-
 // One block per event: the dominant lateral propagation direction of the
 // boundary frame (sign of its summed theta and phi differences over pairs of
 // fixed nodes), which orders the solver's sweep.  bit 0: times grow with
 // theta (sweep +theta), bit 1: times grow with phi; bits 2 and 3: theta /
 // phi is a near tie (sweep it both ways).
-__global__ void directions_kernel(Geom g, const double *__restrict__ frames, int *__restrict__ dir)
+__global__ void directions_kernel(Geom g, const double *__restrict__ frames, int *__restrict__ dir, double tie_ratio)
 {
     const int e = blockIdx.x;
     const long long nb = (long long)g.nnx * g.nnz;
@@ -106,11 +101,12 @@ __global__ void directions_kernel(Geom g, const double *__restrict__ frames, int
     if (threadIdx.x == 0) {
         double ax = 0.0, az = 0.0;
         for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) { ax += rx[w]; az += rz[w]; }
-        // bits 2 / 3: the wave runs within ~6 degrees of the phi / theta
-        // axis, so its theta / phi direction is ambiguous under heterogeneity
-        // and a second sweep with that direction reversed is worth its cost
+        // bits 2 / 3: the wave's theta / phi component is below tie_ratio
+        // times the other (0.1: within ~6 degrees of an axis), so its theta /
+        // phi direction is ambiguous under heterogeneity and sweeps with that
+        // direction reversed are worth their cost
         const double mx = fabs(ax), mz = fabs(az);
-        dir[e] = (ax >= 0.0 ? 1 : 0) | (az >= 0.0 ? 2 : 0) | (mx < FM_TIE_RATIO * mz ? 4 : 0) | (mz < FM_TIE_RATIO * mx ? 8 : 0);
+        dir[e] = (ax >= 0.0 ? 1 : 0) | (az >= 0.0 ? 2 : 0) | (mx < tie_ratio * mz ? 4 : 0) | (mz < tie_ratio * mx ? 8 : 0);
     }
 }
 
@@ -176,9 +172,10 @@ void launch_finalize_frames(const Geom &g, int nev, int prec, const double *fram
         finalize_kernel<float><<<nev, 512, 0, st>>>(g, frames, (float *)T, frozen, base, 1);
 }
 
-void launch_sweep_directions(const Geom &g, int nev, const double *frames, int *dir, cudaStream_t st)
+void launch_sweep_directions(const Geom &g, int nev, const double *frames, int *dir, double tie_ratio,
+                             cudaStream_t st)
 {
-    directions_kernel<<<nev, 256, 0, st>>>(g, frames, dir);
+    directions_kernel<<<nev, 256, 0, st>>>(g, frames, dir, tie_ratio);
 }
 
 void launch_fill_inf(void *T, size_t n, int prec, cudaStream_t st)

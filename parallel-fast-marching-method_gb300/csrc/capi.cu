@@ -305,8 +305,10 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
     return &ctx->tmap[shape];
 }
 
-// Solve schedule (compile-time tuning; the measured best on this GPU):
-//   FM_TIE_SWEEPS          extra sweeps of near-tie events (reversed, forward, ...)
+// Solve schedule.  Per context, at run time (fm3dt_set_schedule; the
+// autotuner picks them per workload): the near-tie events' extra sweeps and
+// band, the re-sweeps after the first rounds and their threshold.
+// Compile-time (the measured best on this GPU):
 //   FM_ROUND0_PER_TILE     first round with one CTA per tile when its tile count is known
 //   FM_OVERLAP_TIES        near-tie events' sweeps and first round beside the other events' ...
 //   FM_OVERLAP_MIN_EVENTS  ... when at least this many other events are in the batch
@@ -314,15 +316,10 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 //                          of their single sweep fails
 //   FM_OVERLAP_MAIN        the near-tie events' main sweep on stream2 too, ahead of
 //                          their extra sweeps, beside the other events' main sweep
-//   FM_RESWEEPS            re-sweeps after the first rounds, at most
-//   FM_RESWEEP_FRAC        ... of events with more than this fraction of tiles queued
 //   FM_FRESH_SWEEP         main sweeps from the unset field with upstream-only node
 //                          updates (the same values as the full update there)
 #ifndef FM_FRESH_SWEEP
 #define FM_FRESH_SWEEP 1
-#endif
-#ifndef FM_TIE_SWEEPS
-#define FM_TIE_SWEEPS 2
 #endif
 #ifndef FM_ROUND0_PER_TILE
 #define FM_ROUND0_PER_TILE 1
@@ -338,12 +335,6 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #endif
 #ifndef FM_OVERLAP_MAIN
 #define FM_OVERLAP_MAIN 1
-#endif
-#ifndef FM_RESWEEPS
-#define FM_RESWEEPS 4
-#endif
-#ifndef FM_RESWEEP_FRAC
-#define FM_RESWEEP_FRAC 0.01
 #endif
 
 // How a solve starts: from boundary frames (initialisation, sweep, rounds),
@@ -369,7 +360,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     if (mode == kFrames) {
         launch_fill_inf(ctx->d_T, (size_t)nev * ctx->N, ctx->prec, s);
         launch_finalize_frames(g, nev, ctx->prec, ctx->d_frames, ctx->d_T, ctx->d_frozen, ctx->d_base, s);
-        launch_sweep_directions(g, nev, ctx->d_frames, ctx->d_dir, s);
+        launch_sweep_directions(g, nev, ctx->d_frames, ctx->d_dir, ctx->tie_ratio, s);
         ctx->launches += 3;
         CKL();
     }
@@ -479,7 +470,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         // and contexts that solve side by side, as a service runs them, lose
         // more to the priority stream than they gain)
         overlap = FM_OVERLAP_TIES && !ctx->verify && !ties.empty() && (int)others.size() >= FM_OVERLAP_MIN_EVENTS &&
-                  FM_TIE_SWEEPS > 0;
+                  ctx->tie_sweeps > 0;
         if (!ties.empty())
             CK(cudaMemcpyAsync(ctx->d_events, ties.data(), ties.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         // pass 0 sweeps every event from the boundary, pass 1 the near-tie
@@ -489,11 +480,11 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
             CK(cudaMemsetAsync(ctx->d_count[0], 0, sizeof(int), s));
         }
-        // (FM_TIE_SWEEPS sweeps of the near-tie events, alternating reversed
+        // (ctx->tie_sweeps sweeps of the near-tie events, alternating reversed
         // and forward, stand for pass 1)
         struct PassPlan { int pass, flip; };
         std::vector<PassPlan> plan{{0, 0}};
-        for (int k = 0; k < FM_TIE_SWEEPS; ++k) plan.push_back({1, (k & 1) ? 0 : 4});
+        for (int k = 0; k < ctx->tie_sweeps; ++k) plan.push_back({1, (k & 1) ? 0 : 4});
         plan.push_back({2, 0});
         for (const PassPlan &pl : plan) {
             const int pass = pl.pass;
@@ -633,11 +624,11 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     double round_ms = 0.0, resweep_ms = 0.0;
     ctx->round_ms_trace.clear();
     // after the first round of a swept solve, the events that still change
-    // on many tiles are swept again (FM_RESWEEPS times at most): corrections
+    // on many tiles are swept again (ctx->resweeps times at most): corrections
     // that the first round made deep in the grid then reach the top in one
     // pass instead of one tile layer per round; the sweep queues the tiles
     // it changes for the next round
-    int resweeps_left = (do_sweep && streaming && !verified) ? FM_RESWEEPS : 0;
+    int resweeps_left = (do_sweep && streaming && !verified) ? ctx->resweeps : 0;
     int grid_override = 0;   // launch grid other than the persistent one (0: persistent)
     auto launch_round = [&](int round, int *cur_list, int *cur_count, int *next_list, int *next_count,
                             cudaStream_t st) {
@@ -663,14 +654,14 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         if (resweeps_left <= 0) return FM3DT_OK;
         --resweeps_left;
         const int queued = *ctx->h_count;
-        if (!((double)queued > FM_RESWEEP_FRAC * (double)nev * (double)tpe)) return FM3DT_OK;
+        if (!((double)queued > ctx->resweep_frac * (double)nev * (double)tpe)) return FM3DT_OK;
         std::vector<int> lst(queued);
         CK(cudaMemcpy(lst.data(), ctx->d_list[nl], (size_t)queued * sizeof(int), cudaMemcpyDeviceToHost));
         std::vector<int> per(nev, 0);
         for (int w : lst) per[w / tpe] += 1;
         std::vector<int> busy;
         for (int e = 0; e < nev; ++e)
-            if ((double)per[e] > FM_RESWEEP_FRAC * (double)tpe) busy.push_back(e);
+            if ((double)per[e] > ctx->resweep_frac * (double)tpe) busy.push_back(e);
         if (busy.empty()) return FM3DT_OK;
         cudaEvent_t r0, r1;
         CK(cudaEventCreate(&r0));
@@ -724,7 +715,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             CK(cudaEventRecord(sw1, s));
             CK(cudaEventRecord(r0, s));
         }
-        for (int k = 0; k < FM_TIE_SWEEPS; ++k) {
+        for (int k = 0; k < ctx->tie_sweeps; ++k) {
             // (height segments by the time model for the near-tie events alone:
             // their sweeps are the longer chain of the two parts)
             const int rc = stream_pass((int)ties.size(), ctx->d_events, (k & 1) ? 0 : 4,
@@ -1444,6 +1435,19 @@ int fm3dt_set_tuning(fm3dt_ctx *ctx, int tile_shape, int max_passes, int max_rou
         ctx->sweep = sweep ? 1 : 0;
         ctx->verify = sweep == 2 ? 1 : 0;
     }
+    return FM3DT_OK;
+}
+
+int fm3dt_set_schedule(fm3dt_ctx *ctx, int tie_sweeps, double tie_ratio, int resweeps, double resweep_frac)
+{
+    if (!ctx) return FM3DT_EINVAL;
+    if (tie_sweeps > 16 || resweeps > 16 || tie_ratio > 1.0 || resweep_frac > 1.0 || tie_ratio != tie_ratio ||
+        resweep_frac != resweep_frac)
+        return fail(ctx, FM3DT_EINVAL, "schedule: tie_sweeps and resweeps <= 16, ratios <= 1");
+    if (tie_sweeps >= 0) ctx->tie_sweeps = tie_sweeps;
+    if (tie_ratio >= 0.0) ctx->tie_ratio = tie_ratio;
+    if (resweeps >= 0) ctx->resweeps = resweeps;
+    if (resweep_frac >= 0.0) ctx->resweep_frac = resweep_frac;
     return FM3DT_OK;
 }
 

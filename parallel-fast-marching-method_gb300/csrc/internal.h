@@ -166,7 +166,8 @@ void launch_planewave_frames(const Geom &g, const PlaneWaveGeom &pg, int nev, co
 void launch_finalize_frames(const Geom &g, int nev, int prec, const double *frames, void *T,
                             uint8_t *frozen, double *base, cudaStream_t st);
 void launch_fill_inf(void *T, size_t n, int prec, cudaStream_t st);
-void launch_sweep_directions(const Geom &g, int nev, const double *frames, int *dir, cudaStream_t st);
+void launch_sweep_directions(const Geom &g, int nev, const double *frames, int *dir, double tie_ratio,
+                             cudaStream_t st);
 // (events: the event of each of the nev entries; null = 0..nev-1)
 void launch_initial_tiles(int nev, const int *events, int tiles_per_event, int first_tile, int count_per_event,
                           int *list, int *count, int *flag, cudaStream_t st);
@@ -291,6 +292,12 @@ struct fm3dt_ctx {
     struct Planes { int shape = -1; int nseg = 1; int *d_tiles = nullptr; std::vector<int> off, cnt; };
     std::vector<Planes> block_planes;   // streaming sweeps, by (shape, height segments)
     int sweep_segments = 0;       // height segments of the streaming sweep (0: automatic)
+    // solve schedule (fm3dt_set_schedule): extra sweeps of the near-tie events,
+    // the near-tie band, re-sweeps after the first rounds and their threshold
+    int tie_sweeps = 2;
+    double tie_ratio = 0.1;
+    int resweeps = 4;
+    double resweep_frac = 0.01;
     int tie_segments = 0;         // the same for the reversed sweep of near-tie events
     int *h_dir = nullptr;         // pinned [maxev] sweep directions of the last solve
     int *d_events = nullptr;      // [maxev] the near-tie events of the last solve

@@ -105,17 +105,21 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
         // ring slot
         constexpr int PER = (LAYER + 31) / 32;
         R buf[PER];
-        auto fetch_layer = [&](int rp) {
-            const int gr = f.nnr - 1 - rp;
+        // this lane's share of a layer: offsets in a grid layer (phi
+        // fastest), -1 outside the grid; the same for every layer of the item
+        const size_t lstride = (size_t)f.nnx * f.nnz;
+        int loff[PER];
 #pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                const int q = lane + 32 * k;
-                const int qx = x0 + q / LZ - 2, qz = z0 + q % LZ - 2;
-                R v = INF;
-                if (q < LAYER && rp >= 0 && rp < f.nnr && qx >= 0 && qx < f.nnx && qz >= 0 && qz < f.nnz)
-                    v = __ldcg(Te + ((size_t)gr * f.nnx + qx) * f.nnz + qz);
-                buf[k] = v;
-            }
+        for (int k = 0; k < PER; ++k) {
+            const int q = lane + 32 * k;
+            const int qx = x0 + q / LZ - 2, qz = z0 + q % LZ - 2;
+            loff[k] = (q < LAYER && qx >= 0 && qx < f.nnx && qz >= 0 && qz < f.nnz) ? qx * f.nnz + qz : -1;
+        }
+        auto fetch_layer = [&](int rp) {
+            const bool rin = rp >= 0 && rp < f.nnr;
+            const R *src = Te + (size_t)(f.nnr - 1 - (rin ? rp : 0)) * lstride;
+#pragma unroll
+            for (int k = 0; k < PER; ++k) buf[k] = (rin && loff[k] >= 0) ? __ldcg(src + loff[k]) : INF;
         };
         auto store_layer = [&](int rp) {
             R *dst = ring + ((rp + RING) & (RING - 1)) * LAYER;

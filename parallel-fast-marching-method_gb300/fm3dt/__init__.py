@@ -57,7 +57,7 @@ EXPORTS = [
     "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_resume",
     "fm3dt_solve_planewave", "fm3dt_solve_point",
     "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_receiver_times_device", "fm3dt_rays_frechet_device", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
-    "fm3dt_set_tuning", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_round_trace_ms", "fm3dt_tile_shapes", "fm3dt_tile_shape",
+    "fm3dt_set_tuning", "fm3dt_set_schedule", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_round_trace_ms", "fm3dt_tile_shapes", "fm3dt_tile_shape",
     "fm3dt_launch_count",
     "fm3dt_last_error", "fm3dt_ctx_destroy",
 ]
@@ -94,6 +94,7 @@ def load(path: str | None = None):
     L.fm3dt_get_velocity.argtypes = [vp, dp]
     L.fm3dt_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
     L.fm3dt_set_sweep_shape.argtypes = [vp, C.c_int]
+    L.fm3dt_set_schedule.argtypes = [vp, C.c_int, C.c_double, C.c_int, C.c_double]
     L.fm3dt_set_sweep_segments.argtypes = [vp, C.c_int, C.c_int]
     L.fm3dt_round_trace.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.fm3dt_round_trace_ms.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
@@ -211,6 +212,13 @@ class Solver:
 
     def set_tuning(self, shape: int = 0, max_passes: int = 0, max_rounds: int = 0, sweep: int = -1):
         self._check(self._L.fm3dt_set_tuning(self._ctx, int(shape), int(max_passes), int(max_rounds), int(sweep)))
+
+    def set_schedule(self, tie_sweeps: int = -1, tie_ratio: float = -1.0, resweeps: int = -1,
+                     resweep_frac: float = -1.0):
+        """Near-tie extra sweeps and band, re-sweeps and their threshold
+        (negative: keep); see fm3dt_set_schedule."""
+        self._check(self._L.fm3dt_set_schedule(self._ctx, int(tie_sweeps), float(tie_ratio), int(resweeps),
+                                               float(resweep_frac)))
 
     def set_sweep_shape(self, shape: int):
         self._check(self._L.fm3dt_set_sweep_shape(self._ctx, int(shape)))

@@ -1,11 +1,17 @@
 """Autotuner of the tile solver.
 
 Tunes, on a sample batch, (1) the shape of the directional sweep (tile or
-streaming) and
+streaming),
 (2) the tile shape and in-tile pass cap of the fast-iterative rounds (the
-shape also fixes the CTA size: one thread per column), keeping the fastest
-device time.  The converged field does not depend on any of these choices
-(the fixed point is unique), so tuning never changes results.
+shape also fixes the CTA size: one thread per column), and (3) the solve
+schedule -- how many extra sweeps, alternately reversed and forward, the
+near-tie events get and how wide the near-tie band is -- keeping the fastest
+device time.  The schedule depends most on the model: on a smooth one
+(Gaussian node noise) two extra sweeps of the events within ~6 degrees of an
+axis are best; on a checkerboard, whose fast cells carry head waves across
+the sweep direction, five or six of them over a band twice as wide halve the
+rounds.  The converged field does not depend on any of these choices (the
+fixed point is unique), so tuning never changes results.
 """
 from __future__ import annotations
 
@@ -14,6 +20,8 @@ import numpy as np
 from . import sweep_shapes, tile_shapes
 
 PASS_CAPS = (16, 64)
+# (extra sweeps of the near-tie events, near-tie band)
+SCHEDULES = ((2, 0.1), (3, 0.15), (4, 0.15), (5, 0.15), (5, 0.2), (6, 0.2))
 
 
 def _time(solver, frames_ptr, nev, device, repeats):
@@ -22,7 +30,9 @@ def _time(solver, frames_ptr, nev, device, repeats):
 
 
 def autotune(solver, frames_ptr: int, nev: int, device: bool = True, repeats: int = 1):
-    """Returns (round_shape, max_passes, sweep_shape, ms) and applies it."""
+    """Returns (round_shape, max_passes, sweep_shape, ms, schedule) and applies
+    it; schedule = (tie_sweeps, tie_ratio, resweeps, resweep_frac), negative
+    values being the defaults kept."""
     nshapes = len(tile_shapes())
     round_shape, cap = 0, PASS_CAPS[0]
     solver.set_tuning(round_shape, cap, 0, 1)
@@ -41,4 +51,11 @@ def autotune(solver, frames_ptr: int, nev: int, device: bool = True, repeats: in
             if best is None or ms < best[2]:
                 best = (shape, c, ms)
     solver.set_tuning(best[0], best[1], 0, 1)
-    return best[0], best[1], best_sweep[0], best[2]
+    best_sched = None
+    for ts, tr in SCHEDULES:
+        solver.set_schedule(ts, tr, -1, -1.0)
+        ms = _time(solver, frames_ptr, nev, device, repeats)
+        if best_sched is None or ms < best_sched[2]:
+            best_sched = (ts, tr, ms)
+    solver.set_schedule(best_sched[0], best_sched[1], -1, -1.0)
+    return best[0], best[1], best_sweep[0], min(best[2], best_sched[2]), (best_sched[0], best_sched[1], -1, -1.0)

@@ -445,3 +445,34 @@ def test_device_memory_entry_points_equal_host_ones(gpu_lib, prec):
         with pytest.raises(fm3dt.Fm3dtError) as ei:
             s.rays_frechet(rcr, badh, rcz)
         assert ei.value.code == fm3dt.ERANGE
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_schedule_does_not_change_the_field(gpu_lib, prec):
+    """The solve schedule (near-tie extra sweeps and band, re-sweeps and their
+    threshold) only changes how fast the fixed point is reached: on a batch
+    large enough for the two-part schedule, every schedule gives the same
+    fields bit for bit; out-of-range values are refused."""
+    import fm3dt
+    baz = np.concatenate([np.linspace(0.0, 352.5, 40), [0.4, 90.3, 179.6, 270.2]])
+    events = np.stack([np.linspace(32.0, 88.0, len(baz)), baz], axis=1)
+    w = _setup(3, 30, events=events)
+    params = _params(w)
+    n = len(params)
+    with fm3dt.Solver(w.header, precision=prec, max_events=n) as s:
+        s.set_velocity(w.velv)
+        ref = None
+        for sched in ((2, 0.1, 4, 0.01), (0, 0.1, 0, 0.01), (5, 0.25, 2, 0.005), (8, 0.2, 6, 0.02),
+                      (3, 0.0, 16, 0.0)):
+            s.set_schedule(*sched)
+            st = s.solve_planewave(params)
+            assert st["converged"] == 1
+            out = np.concatenate([s.get_times(e) for e in range(n)])
+            if ref is None:
+                ref = out
+            else:
+                assert np.array_equal(out, ref), sched
+        for bad in ((17, -1.0, -1, -1.0), (-1, 1.5, -1, -1.0), (-1, float("nan"), -1, -1.0)):
+            with pytest.raises(fm3dt.Fm3dtError) as ei:
+                s.set_schedule(*bad)
+            assert ei.value.code == fm3dt.EINVAL
