@@ -72,10 +72,12 @@ class Tomography:
     """In-process sub.sh.  ``header``: grids; ``velv_ref``: the starting
     model as the forward solver reads it (gridi.vtx velocities, float64);
     ``cm_sd``: gridi.vtx's second column; ``survey``: sources and receivers;
-    ``params``: subinv.in values."""
+    ``params``: subinv.in values; ``schedule``: the solver's solve schedule
+    (tie_sweeps, tie_ratio, resweeps, resweep_frac; see
+    ``Solver.set_schedule``), None for the library's defaults."""
 
     def __init__(self, header, velv_ref, cm_sd, survey: Survey, params: SI.Params, precision=None,
-                 subinv_precision=SI.FP32, batch: int = 512, fom: int = 1):
+                 subinv_precision=SI.FP32, batch: int = 512, fom: int = 1, schedule=None):
         import fm3dt
         import torch
         self.header = header
@@ -89,6 +91,8 @@ class Tomography:
         nmax = max(int(np.max(survey.nsrc)), 1)
         self.batch = min(batch, nmax)
         self.solver = fm3dt.Solver(header, fom=fom, precision=prec, max_events=self.batch)
+        if schedule is not None:
+            self.solver.set_schedule(*schedule)
         # boundary frames resident in device memory for every iteration
         self.d_frames = [torch.from_numpy(np.ascontiguousarray(f, dtype=np.float64)).cuda() for f in survey.frames]
         self.rec = []
