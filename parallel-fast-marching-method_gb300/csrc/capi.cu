@@ -337,116 +337,9 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #define FM_OVERLAP_MAIN 1
 #endif
 
-#ifndef FM_TAIL_GRAPH
-#define FM_TAIL_GRAPH 1
+#ifndef FM_SWEEP_GRAPHS
+#define FM_SWEEP_GRAPHS 1
 #endif
-
-// One thread after each round of the tail graph: counts the round (if it had
-// tiles), records convergence, and ends the graph's loop when the round
-// queued nothing or the round cap is reached.  tail[0]: rounds, tail[1]: 1
-// when converged.
-__global__ void tail_round_done_kernel(cudaGraphConditionalHandle h, const int *cnt_in, const int *cnt_out,
-                                       int *tail, int max_rounds)
-{
-    int r = tail[0];
-    if (*cnt_in > 0) ++r;
-    tail[0] = r;
-    const bool empty = *cnt_out == 0;
-    if (empty) tail[1] = 1;
-    if (empty || r >= max_rounds) cudaGraphSetConditional(h, 0);
-}
-
-// The tail rounds as a graph: a conditional while node whose body runs two
-// rounds (list 0 -> 1, then 1 -> 0), each followed by its count check.  Built
-// once per key and replayed; the loop ends on the device (at the latest at the
-// round cap), so the host waits once for the whole tail instead of once per
-// chunk of rounds.
-template <typename RA64, typename RA32>
-int run_tail_graph(fm3dt_ctx *ctx, cudaStream_t s, int start_round, int max_rounds, int grid, bool point,
-                   int shape, RA32 a32, RA64 a64, int *rounds_out, bool *done_out, double *round_ms)
-{
-    const long long key[7] = {ctx->prec, shape, ctx->max_passes, grid, max_rounds, point ? 1 : 0,
-                              ctx->prec == FM3DT_FP64 ? a64.tma : a32.tma};
-    if (!ctx->tail.valid || memcmp(key, ctx->tail.key, sizeof key) != 0) {
-        if (ctx->tail.exec) {
-            cudaGraphExecDestroy(ctx->tail.exec);
-            ctx->tail.exec = nullptr;
-        }
-        ctx->tail.valid = false;
-        cudaGraph_t g = nullptr;
-        CK(cudaGraphCreate(&g, 0));
-        cudaGraphConditionalHandle h;
-        cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
-        cudaGraphNodeParams cp{};
-        cudaGraphNode_t node;
-        cudaGraph_t body = nullptr;
-        if (e == cudaSuccess) {
-            cp.type = cudaGraphNodeTypeConditional;
-            cp.conditional.handle = h;
-            cp.conditional.type = cudaGraphCondTypeWhile;
-            cp.conditional.size = 1;
-            e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
-        }
-        if (e == cudaSuccess) {
-            body = cp.conditional.phGraph_out[0];
-            e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-        }
-        if (e == cudaSuccess) {
-            for (int half = 0; half < 2; ++half) {
-                const int cur = half, nxt = half ^ 1;
-                cudaMemsetAsync(ctx->d_count[nxt], 0, sizeof(int), s);
-                if (ctx->prec == FM3DT_FP64) {
-                    a64.trace = ctx->d_trace; a64.round_dev = ctx->d_tail; a64.round = 0;
-                    a64.cur_list = ctx->d_list[cur]; a64.cur_count = ctx->d_count[cur];
-                    a64.next_list = ctx->d_list[nxt]; a64.next_count = ctx->d_count[nxt];
-                    launch_round_f64(shape, grid, a64, s);
-                } else {
-                    a32.trace = ctx->d_trace; a32.round_dev = ctx->d_tail; a32.round = 0;
-                    a32.cur_list = ctx->d_list[cur]; a32.cur_count = ctx->d_count[cur];
-                    a32.next_list = ctx->d_list[nxt]; a32.next_count = ctx->d_count[nxt];
-                    launch_round_f32(shape, grid, a32, s);
-                }
-                tail_round_done_kernel<<<1, 1, 0, s>>>(h, ctx->d_count[cur], ctx->d_count[nxt], ctx->d_tail,
-                                                       max_rounds);
-            }
-            cudaGraph_t out = nullptr;
-            const cudaError_t e2 = cudaStreamEndCapture(s, &out);
-            if (e == cudaSuccess) e = e2;
-        }
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->tail.exec, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) {
-            // no graph (e.g. a driver without conditional nodes): the host
-            // drives the tail rounds as before, for the rest of this context
-            (void)cudaGetLastError();
-            ctx->tail_off = true;
-            return 1;
-        }
-        memcpy(ctx->tail.key, key, sizeof key);
-        ctx->tail.valid = true;
-    }
-    int h_tail[2] = {start_round, 0};
-    cudaEvent_t t0, t1;
-    CK(cudaEventCreate(&t0));
-    CK(cudaEventCreate(&t1));
-    CK(cudaMemcpyAsync(ctx->d_tail, h_tail, sizeof h_tail, cudaMemcpyHostToDevice, s));
-    CK(cudaEventRecord(t0, s));
-    CK(cudaGraphLaunch(ctx->tail.exec, s));
-    CK(cudaEventRecord(t1, s));
-    CK(cudaMemcpyAsync(h_tail, ctx->d_tail, sizeof h_tail, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    float m = 0.0f;
-    cudaEventElapsedTime(&m, t0, t1);
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
-    *round_ms += m;
-    // (the tail's rounds are one entry of the per-round time trace)
-    if ((int)ctx->round_ms_trace.size() < fm3dt_ctx::kTraceRounds) ctx->round_ms_trace.push_back(m);
-    ctx->launches += 2LL * (h_tail[0] - start_round + 1);
-    *rounds_out = h_tail[0];
-    *done_out = h_tail[1] != 0;
-    return FM3DT_OK;
-}
 
 // How a solve starts: from boundary frames (initialisation, sweep, rounds),
 // from the current fields (resume: rounds with every tile active), or from
@@ -535,35 +428,81 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         if (rc) return rc;
         const auto &P = *PP;
         const int seg_len = (g.nnr + nseg - 1) / nseg;
-        for (size_t h = 0; h < P.off.size(); ++h) {
-            const long long items = (long long)P.cnt[h] * nitems;
-            const int grid = (int)std::min<long long>(items, sgrid);
-            auto fill = [&](auto &a) {
-                a.hp_blocks = P.d_tiles; a.hoff = P.off[h]; a.hcount = P.cnt[h];
-                a.dir = ctx->d_dir; a.nev = nitems; a.nbx = nbx; a.nbz = nbz;
-                a.events = events;
-                a.flip = flip;
-                a.fresh = fresh ? 1 : 0;
-                a.seg_len = seg_len;
-                a.flag = flag;
-                a.list = list; a.count = count;
-                a.tr = ts.tr; a.tx = ts.tx; a.tz = ts.tz;
-                a.ntr = ntr; a.ntx = ntx; a.ntz = ntz; a.tiles_per_event = tpe;
-            };
-            if (ctx->prec == FM3DT_FP64) {
-                StreamArgs<double> a{};
-                a.f = f64;
-                fill(a);
-                launch_stream_f64(sidx, grid, a, st);
-            } else {
-                StreamArgs<float> a{};
-                a.f = f32;
-                fill(a);
-                launch_stream_f32(sidx, grid, a, st);
+        const int nlaunch = (int)P.off.size();
+        // the pass's launches, one per hyperplane
+        auto enqueue = [&]() {
+            for (size_t h = 0; h < P.off.size(); ++h) {
+                const long long items = (long long)P.cnt[h] * nitems;
+                const int grid = (int)std::min<long long>(items, sgrid);
+                auto fill = [&](auto &a) {
+                    a.hp_blocks = P.d_tiles; a.hoff = P.off[h]; a.hcount = P.cnt[h];
+                    a.dir = ctx->d_dir; a.nev = nitems; a.nbx = nbx; a.nbz = nbz;
+                    a.events = events;
+                    a.flip = flip;
+                    a.fresh = fresh ? 1 : 0;
+                    a.seg_len = seg_len;
+                    a.flag = flag;
+                    a.list = list; a.count = count;
+                    a.tr = ts.tr; a.tx = ts.tx; a.tz = ts.tz;
+                    a.ntr = ntr; a.ntx = ntx; a.ntz = ntz; a.tiles_per_event = tpe;
+                };
+                if (ctx->prec == FM3DT_FP64) {
+                    StreamArgs<double> a{};
+                    a.f = f64;
+                    fill(a);
+                    launch_stream_f64(sidx, grid, a, st);
+                } else {
+                    StreamArgs<float> a{};
+                    a.f = f32;
+                    fill(a);
+                    launch_stream_f32(sidx, grid, a, st);
+                }
             }
-            ++sweep_launches;
-            ctx->launches += 1;
+        };
+        // Passes that recur from solve to solve (the main sweeps and the
+        // near-tie events' extra sweeps; not the re-sweeps, whose event count
+        // varies) run as a graph captured on first use: one launch instead of
+        // one per hyperplane.
+        bool launched = false;
+        if (FM_SWEEP_GRAPHS && flag == nullptr && !ctx->sweep_graph_off) {
+            const long long key[fm3dt_ctx::kSweepKey] = {ctx->prec, sidx, nitems, (long long)(intptr_t)events, flip,
+                                                         nseg, fresh ? 1 : 0, (long long)(intptr_t)st, ctx->shape};
+            cudaGraphExec_t exec = nullptr;
+            for (const auto &sg : ctx->sweep_graphs)
+                if (memcmp(sg.key, key, sizeof key) == 0) exec = sg.exec;
+            if (!exec) {
+                cudaGraph_t gr = nullptr;
+                cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+                if (e == cudaSuccess) {
+                    enqueue();
+                    e = cudaStreamEndCapture(st, &gr);
+                }
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, gr, 0);
+                if (gr) cudaGraphDestroy(gr);
+                if (e != cudaSuccess) {
+                    // launched one by one from now on in this context
+                    (void)cudaGetLastError();
+                    ctx->sweep_graph_off = true;
+                    exec = nullptr;
+                } else {
+                    if (ctx->sweep_graphs.size() >= fm3dt_ctx::kSweepGraphs) {
+                        cudaGraphExecDestroy(ctx->sweep_graphs.front().exec);
+                        ctx->sweep_graphs.erase(ctx->sweep_graphs.begin());
+                    }
+                    fm3dt_ctx::SweepGraph sg;
+                    memcpy(sg.key, key, sizeof key);
+                    sg.exec = exec;
+                    ctx->sweep_graphs.push_back(sg);
+                }
+            }
+            if (exec) {
+                CK(cudaGraphLaunch(exec, st));
+                launched = true;
+            }
         }
+        if (!launched) enqueue();
+        sweep_launches += nlaunch;
+        ctx->launches += nlaunch;
         return FM3DT_OK;
     };
     CK(cudaEventRecord(sw0, s));
@@ -721,8 +660,6 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     a64.err = a32.err = ctx->d_err;
     a64.cert = a32.cert = ctx->d_cert;
     a64.cert_nw = a32.cert_nw = ctx->cert_nw;
-    a64.trace_cap = a32.trace_cap = fm3dt_ctx::kTraceRounds;
-    a64.round_dev = a32.round_dev = nullptr;
     {
         const CUtensorMap *map = field_tensor_map(ctx, shape);
         a64.tma = a32.tma = map ? 1 : 0;
@@ -873,20 +810,9 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         if (*ctx->h_count == 0) done = true;
     }
     while (!done && rounds < max_rounds) {
-        // the tail: once no re-sweep can follow, the remaining rounds run as
-        // one graph launch whose loop the device ends (from an even round,
-        // so that its body starts on list 0)
-        if (FM_TAIL_GRAPH && !ctx->tail_off && resweeps_left <= 0 && (rounds & 1) == 0) {
-            const int rc = run_tail_graph(ctx, s, rounds, max_rounds, grid, point, shape, a32, a64, &rounds,
-                                          &done, &round_ms);
-            if (rc < 0) return rc;
-            if (rc == 0) break;
-        }
         int k;
         const int first_round = rounds;
-        // (one round at a time while re-sweeps may follow, and to reach an
-        // even round for the tail graph)
-        const int chunk_now = (resweeps_left > 0 || (FM_TAIL_GRAPH && !ctx->tail_off && (rounds & 1))) ? 1 : chunk;
+        const int chunk_now = resweeps_left > 0 ? 1 : chunk;
         while ((int)ctx->round_events.size() < 2 * chunk) {
             cudaEvent_t e;
             CK(cudaEventCreate(&e));
@@ -1069,7 +995,6 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMalloc(&ctx->d_list_b, ctx->flag_capacity * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_count_b, sizeof(int)));
     CKC(cudaMalloc(&ctx->d_err, sizeof(int)));
-    CKC(cudaMalloc(&ctx->d_tail, 2 * sizeof(int)));
     {
         const char *env = std::getenv("FM3DT_TMA");
         if (env && env[0] == '0') ctx->use_tma = 0;
@@ -1642,7 +1567,7 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
 {
     if (!ctx) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    if (ctx->tail.exec) cudaGraphExecDestroy(ctx->tail.exec);
+    for (auto &sg : ctx->sweep_graphs) cudaGraphExecDestroy(sg.exec);
     for (auto e : ctx->round_events) cudaEventDestroy(e);
     cudaFree(ctx->d_velv);
     cudaFree(ctx->d_veln);
@@ -1659,7 +1584,6 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_list_b);
     cudaFree(ctx->d_count_b);
     cudaFree(ctx->d_err);
-    cudaFree(ctx->d_tail);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     if (ctx->h_dir) cudaFreeHost(ctx->h_dir);
     cudaFree(ctx->d_T);

@@ -66,8 +66,6 @@ struct RoundArgs {
     unsigned long long *stats;  // [0] tiles processed, [1] node updates, [2] staged nodes
     unsigned long long *trace;  // per round: [2*round] tiles, [2*round+1] node updates (or null)
     int round;
-    const int *round_dev;       // when set, the round's index is read here (rounds driven by a graph)
-    int trace_cap;              // rounds the trace holds
     // nodes a certified tile recomputes first: bit r%32 of word
     // ((e*nnx + x)*nnz + z)*cert_nw + r/32 (or null)
     const unsigned *cert;
@@ -319,17 +317,13 @@ struct fm3dt_ctx {
     size_t flag_capacity = 0;     // tiles allocated for flags/lists
     int64_t launches = 0;
     std::string err;
-    // the tail rounds as one graph: a device-driven loop of rounds (a
-    // conditional while node) that stops when a round queues nothing; rebuilt
-    // when its key (precision, tile shape, pass cap, launch grid, round cap,
-    // point boxes, TMA) changes
-    struct TailGraph {
-        bool valid = false;
-        long long key[7] = {};
-        cudaGraphExec_t exec = nullptr;
-    } tail;
-    int *d_tail = nullptr;        // [0] rounds done, [1] converged (the last round queued nothing)
-    bool tail_off = false;        // the graph could not be built: the host drives every round
+    // sweep passes captured as graphs, keyed by precision, sweep shape, event
+    // count, event list, flip, height segments, form, stream and tile shape
+    static constexpr int kSweepKey = 9;
+    static constexpr size_t kSweepGraphs = 24;
+    struct SweepGraph { long long key[kSweepKey]; cudaGraphExec_t exec; };
+    std::vector<SweepGraph> sweep_graphs;
+    bool sweep_graph_off = false;
     std::vector<cudaEvent_t> round_events;   // start/stop pairs of round kernels
     std::vector<float> round_ms_trace;       // device time of each round of the last solve
     // point sources: fixed node boxes, and the refined source grids' contexts

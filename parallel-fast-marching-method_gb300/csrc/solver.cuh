@@ -465,10 +465,9 @@ __global__ void __launch_bounds__(TX * TZ, (MinBlocks<R, TX * TZ>::round))
         atomicAdd(&a.stats[0], my_tiles);
         atomicAdd(&a.stats[1], s_upd);
         atomicAdd(&a.stats[2], my_staged);
-        const int rd = a.round_dev ? *((volatile const int *)a.round_dev) : a.round;
-        if (a.trace && rd < a.trace_cap) {
-            atomicAdd(&a.trace[2 * rd], my_tiles);
-            atomicAdd(&a.trace[2 * rd + 1], s_upd);
+        if (a.trace) {
+            atomicAdd(&a.trace[2 * a.round], my_tiles);
+            atomicAdd(&a.trace[2 * a.round + 1], s_upd);
         }
     }
 }
