@@ -470,6 +470,8 @@ def run_ours(a):
     tt, tu = solver.round_trace()
     trace_tiles, trace_updates = [int(x) for x in tt], [int(x) for x in tu]
     trace_ms = [round(float(x), 4) for x in solver.round_trace_ms()]
+    part_ms = [round(float(x), 3) for x in solver.part_ms()]
+    tie_run, tie_skip = solver.tie_sweep_items()
     clk = clocks.stop() if clocks else None
     dev_ms = sum(s["ms"] for s in sts)
     step_s = wall if forward else max(wall, dev_ms / 1000.0)
@@ -602,7 +604,9 @@ def run_ours(a):
                    "sweep_nodes_per_solve": sweep_nodes / a.steps,
                    "work_shares": {k: v / max(1e-9, sum(work.values())) for k, v in work.items()},
                    "round_trace_tiles": trace_tiles, "round_trace_updates": trace_updates,
-                   "round_trace_ms": trace_ms},
+                   "round_trace_ms": trace_ms,
+                   "first_round_parts_ms": dict(zip(("tie_sweeps", "tie_round", "certify", "other_round"), part_ms)),
+                   "tie_sweep_items": {"run": [int(x) for x in tie_run], "skipped": [int(x) for x in tie_skip]}},
     }
     line.update(extras)
     if clk:

@@ -89,7 +89,10 @@ typedef struct {
 typedef struct fm3dt_ctx fm3dt_ctx;
 
 /* Replaces F:6050-6191 (topology, input conversion, allocation).  Allocates
- * the device fields for desc->max_events events. */
+ * the device fields for desc->max_events events.  The scratch of the
+ * context's later calls (the largest: fm3dt_rays_frechet's dense rows,
+ * nev*nrc*(nvr+2)*(nvx+2)*(nvz+2)*4 bytes) comes from a memory pool of the
+ * context that keeps its memory until fm3dt_ctx_destroy. */
 int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out);
 
 /* Replaces F:6172 gridder (F:6989-7038): cubic B-spline interpolation of the
@@ -253,6 +256,19 @@ int fm3dt_round_trace(fm3dt_ctx *ctx, int cap, int64_t *tiles, int64_t *updates)
 /* Device time (ms, CUDA events around each launch) of each round of the last
  * solve, up to cap rounds.  Returns the number of rounds recorded. */
 int fm3dt_round_trace_ms(fm3dt_ctx *ctx, int cap, float *ms);
+
+/* Device times (ms) of the last solve's first round when it ran in two parts
+ * side by side: ms[0] the near-tie events' extra sweeps, ms[1] their first
+ * round, ms[2] the other events' certification, ms[3] their first round;
+ * zeros when the solve ran in one part. */
+int fm3dt_part_ms(fm3dt_ctx *ctx, float *ms);
+
+/* The last solve's near-tie extra sweeps after the first skip the work items
+ * (a height segment of a block of columns of one event) where nothing near
+ * them changed: run[k] / skipped[k] the items extra sweep k ran and skipped,
+ * for up to cap sweeps (sweep 0 runs every item and counts none).  Returns
+ * the number of extra sweeps recorded (0 when none tracked activity). */
+int fm3dt_tie_sweep_items(fm3dt_ctx *ctx, int cap, int64_t *run, int64_t *skipped);
 
 /* Number of available tile shapes and the shape (TR, TX, TZ) of one. */
 int fm3dt_tile_shapes(int *count);

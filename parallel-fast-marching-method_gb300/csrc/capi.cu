@@ -46,8 +46,11 @@ int fail(fm3dt_ctx *ctx, int code, const std::string &msg)
 // (stream-ordered) on every return path.
 struct DeviceScratch {
     cudaStream_t s;
+    cudaMemPool_t pool;
     std::vector<void *> bufs;
-    explicit DeviceScratch(cudaStream_t st) : s(st) {}
+    // from the context's pool (which keeps its memory between calls) on the
+    // context's stream
+    explicit DeviceScratch(const fm3dt_ctx *ctx) : s(ctx->stream), pool(ctx->pool) {}
     DeviceScratch(const DeviceScratch &) = delete;
     DeviceScratch &operator=(const DeviceScratch &) = delete;
     template <typename T>
@@ -55,7 +58,8 @@ struct DeviceScratch {
     {
         *p = nullptr;
         if (n == 0) return cudaSuccess;
-        cudaError_t e = cudaMallocAsync((void **)p, n * sizeof(T), s);
+        cudaError_t e = pool ? cudaMallocFromPoolAsync((void **)p, n * sizeof(T), pool, s)
+                             : cudaMallocAsync((void **)p, n * sizeof(T), s);
         if (e == cudaSuccess) bufs.push_back((void *)*p);
         return e;
     }
@@ -318,6 +322,17 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 //                          their extra sweeps, beside the other events' main sweep
 //   FM_FRESH_SWEEP         main sweeps from the unset field with upstream-only node
 //                          updates (the same values as the full update there)
+//   FM_TIE_QUEUE           the near-tie events' last extra sweep queues the tiles
+//                          it changes for their first round, which then takes
+//                          those tiles instead of every tile
+//   FM_TIE_SKIP            the near-tie events' extra sweeps after the first skip
+//                          the items where nothing near them changed (StreamArgs)
+#ifndef FM_TIE_QUEUE
+#define FM_TIE_QUEUE 1
+#endif
+#ifndef FM_TIE_SKIP
+#define FM_TIE_SKIP 1
+#endif
 #ifndef FM_FRESH_SWEEP
 #define FM_FRESH_SWEEP 1
 #endif
@@ -417,8 +432,13 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     // directions flipped by `flip`; with `flag`, changed nodes queue their
     // tiles (and face neighbours) on list/count for the rounds.  `fresh`: the
     // events' main sweep, from their unset fields (upstream-only updates).
+    // `recurs`: a pass that recurs from solve to solve (kept as a graph).
+    // `act`: the item activity of a chain of sweeps (this sweep's, the
+    // previous one's or null), see StreamArgs.
     auto stream_pass = [&](int nitems, const int *events, int flip, int nseg, int *flag, int *list,
-                           int *count, cudaStream_t st, bool fresh) -> int {
+                           int *count, cudaStream_t st, bool fresh, bool recurs,
+                           unsigned char *act_cur = nullptr, const unsigned char *act_prev = nullptr,
+                           unsigned long long *act_items = nullptr) -> int {
         sweep_nodes += (int64_t)nitems * (int64_t)ctx->N;
         const int sgrid = stream_grid(fresh);
         if (nseg <= 0) nseg = stream_segments(ctx, nitems, nbx, nbz, sgrid, kStreamShapes[sidx].sx + kStreamShapes[sidx].sz - 2);
@@ -445,6 +465,11 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                     a.list = list; a.count = count;
                     a.tr = ts.tr; a.tx = ts.tx; a.tz = ts.tz;
                     a.ntr = ntr; a.ntx = ntx; a.ntz = ntz; a.tiles_per_event = tpe;
+                    // (items of one layer or column would miss a 2-deep neighbour)
+                    const bool track = act_cur && seg_len >= 2 && kStreamShapes[sidx].sx >= 2;
+                    a.act_cur = track ? act_cur : nullptr;
+                    a.act_prev = track ? act_prev : nullptr;
+                    a.act_items = track ? act_items : nullptr;
                 };
                 if (ctx->prec == FM3DT_FP64) {
                     StreamArgs<double> a{};
@@ -464,9 +489,12 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         // varies) run as a graph captured on first use: one launch instead of
         // one per hyperplane.
         bool launched = false;
-        if (FM_SWEEP_GRAPHS && flag == nullptr && !ctx->sweep_graph_off) {
+        if (FM_SWEEP_GRAPHS && recurs && !ctx->sweep_graph_off) {
             const long long key[fm3dt_ctx::kSweepKey] = {ctx->prec, sidx, nitems, (long long)(intptr_t)events, flip,
-                                                         nseg, fresh ? 1 : 0, (long long)(intptr_t)st, ctx->shape};
+                                                         nseg, fresh ? 1 : 0, (long long)(intptr_t)st, ctx->shape,
+                                                         (long long)(intptr_t)flag, (long long)(intptr_t)list,
+                                                         (long long)(intptr_t)count, (long long)(intptr_t)act_cur,
+                                                         (long long)(intptr_t)act_prev, (long long)(intptr_t)act_items};
             cudaGraphExec_t exec = nullptr;
             for (const auto &sg : ctx->sweep_graphs)
                 if (memcmp(sg.key, key, sizeof key) == 0) exec = sg.exec;
@@ -508,6 +536,13 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     CK(cudaEventRecord(sw0, s));
     std::vector<int> ties, others;     // near-tie events and the rest
     bool overlap = false;              // ties' extra sweeps beside the others' first round
+    bool tie_queue = false;            // ties' last extra sweep queues their first round's tiles
+    bool tie_act = false;              // ties' extra sweeps skip items where nothing changed
+    // the activity buffers of extra sweep k: this sweep's and the previous one's
+    auto act_cur = [&](int k) { return tie_act ? ctx->d_act[k & 1] : nullptr; };
+    auto act_prev = [&](int k) -> const unsigned char * { return tie_act && k > 0 ? ctx->d_act[(k - 1) & 1] : nullptr; };
+    auto act_items = [&](int k) { return tie_act && k < fm3dt_ctx::kMaxTieSweeps ? ctx->d_act_items + 2 * k : nullptr; };
+    ctx->act_sweeps = 0;
     if (do_sweep && streaming) {
         // streaming sweep: one launch per column-block hyperplane
         // the events whose lateral direction is a near tie get two more
@@ -521,6 +556,38 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         // more to the priority stream than they gain)
         overlap = FM_OVERLAP_TIES && !ctx->verify && !ties.empty() && (int)others.size() >= FM_OVERLAP_MIN_EVENTS &&
                   ctx->tie_sweeps > 0;
+        // The near-tie events' last extra sweep runs in flag mode: a node it
+        // leaves unchanged, with every neighbour that was updated after it
+        // unchanged too, is a fixed point of the stencil, and every other node
+        // lies in a tile the sweep queues (its own, or a face neighbour's
+        // whose halo holds a changed node).  Their first round then takes the
+        // queued tiles, not every tile.  (The other events' first round is
+        // appended by their certification, so without it they need every
+        // tile, which the list cannot hold beside a queue.)
+        tie_queue = FM_TIE_QUEUE && !ctx->verify && !ties.empty() && ctx->tie_sweeps > 0 &&
+                    (overlap || FM_CERTIFY || others.empty());
+        if (tie_queue && !overlap) {
+            CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
+            CK(cudaMemsetAsync(ctx->d_count[0], 0, sizeof(int), s));
+        }
+        // item activity of the near-tie events' extra sweeps: one byte per
+        // (event, segment, column block), for at most 127 segments
+        if (FM_TIE_SKIP && !ties.empty() && ctx->tie_sweeps > 1) {
+            const size_t need = ties.size() * (size_t)std::min(127, g.nnr) * (size_t)nbx * (size_t)nbz;
+            if (need > ctx->act_bytes) {
+                CK(cudaStreamSynchronize(ctx->stream2));
+                for (auto &p : ctx->d_act) {
+                    cudaFree(p);
+                    p = nullptr;
+                }
+                ctx->act_bytes = 0;
+                for (auto &p : ctx->d_act) CK(cudaMalloc(&p, need));
+                ctx->act_bytes = need;
+            }
+            tie_act = true;
+            ctx->act_sweeps = std::min(ctx->tie_sweeps, fm3dt_ctx::kMaxTieSweeps);
+            CK(cudaMemsetAsync(ctx->d_act_items, 0, 2 * fm3dt_ctx::kMaxTieSweeps * sizeof(unsigned long long), s));
+        }
         if (!ties.empty())
             CK(cudaMemcpyAsync(ctx->d_events, ties.data(), ties.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         // pass 0 sweeps every event from the boundary, pass 1 the near-tie
@@ -532,10 +599,11 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         }
         // (ctx->tie_sweeps sweeps of the near-tie events, alternating reversed
         // and forward, stand for pass 1)
-        struct PassPlan { int pass, flip; };
-        std::vector<PassPlan> plan{{0, 0}};
-        for (int k = 0; k < ctx->tie_sweeps; ++k) plan.push_back({1, (k & 1) ? 0 : 4});
-        plan.push_back({2, 0});
+        struct PassPlan { int pass, flip; bool queue; int k; };
+        std::vector<PassPlan> plan{{0, 0, false, 0}};
+        for (int k = 0; k < ctx->tie_sweeps; ++k)
+            plan.push_back({1, (k & 1) ? 0 : 4, tie_queue && k == ctx->tie_sweeps - 1, k});
+        plan.push_back({2, 0, ctx->verify != 0, 0});
         for (const PassPlan &pl : plan) {
             const int pass = pl.pass;
             if ((pass == 0 && overlap && FM_OVERLAP_MAIN) || (pass == 1 && (ties.empty() || overlap)) ||
@@ -544,8 +612,9 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             const int nitems = pass == 1 ? (int)ties.size() : nev;
             const int rc = stream_pass(nitems, pass == 1 ? ctx->d_events : nullptr, pl.flip,
                                        pass == 1 ? ctx->tie_segments : ctx->sweep_segments,
-                                       pass == 2 ? ctx->d_flag : nullptr, ctx->d_list[0], ctx->d_count[0], s,
-                                       pass == 0 && FM_FRESH_SWEEP);
+                                       pl.queue ? ctx->d_flag : nullptr, ctx->d_list[0], ctx->d_count[0], s,
+                                       pass == 0 && FM_FRESH_SWEEP, pass != 2, pass == 1 ? act_cur(pl.k) : nullptr,
+                                       pass == 1 ? act_prev(pl.k) : nullptr, pass == 1 ? act_items(pl.k) : nullptr);
             if (rc) return rc;
         }
         CKL();
@@ -623,13 +692,19 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     };
     const bool certify_alone = FM_CERTIFY && do_sweep && streaming && !verified && !overlap && !others.empty();
     if (!verified) {
-        CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
+        // (with the near-tie events' tiles queued by their last sweep, the
+        // flags and list 0 were cleared before it)
+        if (!(tie_queue && !overlap)) CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
         if (overlap) {
             // the first round is launched below, in two parts
+        } else if (tie_queue && !certify_alone) {
+            // every event a near tie: list 0 holds the tiles their last sweep queued
         } else if (certify_alone) {
             // the near-tie events' tiles first (this sets the count), then the
             // other events' marked tiles appended
-            if (!ties.empty())
+            if (tie_queue) {
+                // (queued by the near-tie events' last sweep)
+            } else if (!ties.empty())
                 launch_initial_tiles((int)ties.size(), ctx->d_events, tpe, first, cnt, ctx->d_list[0],
                                      ctx->d_count[0], ctx->d_flag, s);
             else
@@ -673,6 +748,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     bool done = false;
     double round_ms = 0.0, resweep_ms = 0.0;
     ctx->round_ms_trace.clear();
+    for (float &m : ctx->part_ms) m = 0.0f;
     // after the first round of a swept solve, the events that still change
     // on many tiles are swept again (ctx->resweeps times at most): corrections
     // that the first round made deep in the grid then reach the top in one
@@ -699,14 +775,16 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         ctx->launches += 1;
     };
     // events that still change on many tiles after a round are swept again
-    // (see resweeps_left); `nl` is the list the next round takes
-    auto maybe_resweep = [&](int nl) -> int {
-        if (resweeps_left <= 0) return FM3DT_OK;
-        --resweeps_left;
-        const int queued = *ctx->h_count;
+    // (see resweeps_left; `left` counts down): `list`/`count` is the list the
+    // next round takes, `queued` its length, `ev_buf` a device array for the
+    // swept events' indices that no other stream reads meanwhile
+    auto maybe_resweep = [&](int *list, int *count, int queued, int *ev_buf, int &left) -> int {
+        if (left <= 0) return FM3DT_OK;
+        --left;
         if (!((double)queued > ctx->resweep_frac * (double)nev * (double)tpe)) return FM3DT_OK;
         std::vector<int> lst(queued);
-        CK(cudaMemcpy(lst.data(), ctx->d_list[nl], (size_t)queued * sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpyAsync(lst.data(), list, (size_t)queued * sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
         std::vector<int> per(nev, 0);
         for (int w : lst) per[w / tpe] += 1;
         std::vector<int> busy;
@@ -716,15 +794,14 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         cudaEvent_t r0, r1;
         CK(cudaEventCreate(&r0));
         CK(cudaEventCreate(&r1));
-        CK(cudaMemcpyAsync(ctx->d_events, busy.data(), busy.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ev_buf, busy.data(), busy.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         CK(cudaEventRecord(r0, s));
-        const int rc = stream_pass((int)busy.size(), ctx->d_events, 0, 0, ctx->d_flag, ctx->d_list[nl],
-                                   ctx->d_count[nl], s, false);
+        const int rc = stream_pass((int)busy.size(), ev_buf, 0, 0, ctx->d_flag, list, count, s, false, false);
         if (rc) return rc;
         interval_nodes += (int64_t)busy.size() * (int64_t)ctx->N;
         CK(cudaEventRecord(r1, s));
         CKL();
-        CK(cudaMemcpyAsync(ctx->h_count, ctx->d_count[nl], sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(ctx->h_count, count, sizeof(int), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         float m = 0.0f;
         cudaEventElapsedTime(&m, r0, r1);
@@ -733,19 +810,69 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         cudaEventDestroy(r1);
         return FM3DT_OK;
     };
+    // Rounds on the context stream until the list they take comes back empty
+    // (part_done) or the round cap: list[cur] is the list the next round
+    // takes, whose length is in *ctx->h_count when `known`.
+    struct RoundLists { int *list[2]; int *count[2]; int cur; };
+    auto converge = [&](RoundLists &L, bool known, int *ev_buf, int &left, bool &part_done) -> int {
+        if (known && *ctx->h_count == 0) part_done = true;
+        while (!part_done && rounds < max_rounds) {
+            int k;
+            const int first_round = rounds;
+            const int chunk_now = left > 0 ? 1 : chunk;
+            while ((int)ctx->round_events.size() < 2 * chunk) {
+                cudaEvent_t e;
+                CK(cudaEventCreate(&e));
+                ctx->round_events.push_back(e);
+            }
+            for (k = 0; k < chunk_now && rounds < max_rounds; ++k, ++rounds) {
+                const int cur = L.cur, nxt = cur ^ 1;
+                CK(cudaMemsetAsync(L.count[nxt], 0, sizeof(int), s));
+                CK(cudaEventRecord(ctx->round_events[2 * k], s));
+                // the first round's tile count is known on the host: one CTA per
+                // tile, so blocks free up as they finish
+                if (rounds == 0 && FM_ROUND0_PER_TILE && !verified && mode != kPoint && !certify_alone && !tie_queue)
+                    grid_override = (int)std::min<long long>((long long)nev * cnt, 1LL << 30);
+                launch_round(rounds, L.list[cur], L.count[cur], L.list[nxt], L.count[nxt], s);
+                grid_override = 0;
+                CK(cudaEventRecord(ctx->round_events[2 * k + 1], s));
+                L.cur = nxt;
+            }
+            CKL();
+            CK(cudaMemcpyAsync(ctx->h_count, L.count[L.cur], sizeof(int), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            for (int q = 0; q < rounds - first_round; ++q) {
+                float m = 0.0f;
+                cudaEventElapsedTime(&m, ctx->round_events[2 * q], ctx->round_events[2 * q + 1]);
+                round_ms += m;
+                if ((int)ctx->round_ms_trace.size() < fm3dt_ctx::kTraceRounds) ctx->round_ms_trace.push_back(m);
+            }
+            const int rc = maybe_resweep(L.list[L.cur], L.count[L.cur], *ctx->h_count, ev_buf, left);
+            if (rc) return rc;
+            if (*ctx->h_count == 0) part_done = true;
+        }
+        return FM3DT_OK;
+    };
     if (overlap) {
-        // the solve in two parts that run side by side, both queueing onto
-        // list 1 for the next round: on stream2, whose higher priority gets
-        // its blocks scheduled first, the near-tie events' main sweep, their
-        // extra sweeps and their first round (every tile); on the context
-        // stream, the other events' main sweep, their certification and their
+        // The solve in two parts that run side by side and converge apart
+        // (events do not interact).  On stream2, whose higher priority gets
+        // its blocks scheduled first: the near-tie events' main sweep, their
+        // extra sweeps and their first round (on the tiles the last sweep
+        // queued, or every tile), queueing onto list c.  On the context
+        // stream: the other events' main sweep, their certification, their
         // first round on the tiles it marks (or, without the certification,
         // every tile, one CTA per tile so that blocks free up as they finish)
+        // and their further rounds until they converge, while stream2 still
+        // runs the near-tie events' chain; then the near-tie events' rounds.
         cudaEvent_t fork, join, r0, r1;
         CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
         CK(cudaEventCreate(&r0));
         CK(cudaEventCreate(&r1));
+        // the parts' phases: near-tie extra sweeps and first round (stream2),
+        // the others' certification and first round (context stream)
+        cudaEvent_t pe[6];
+        for (auto &e : pe) CK(cudaEventCreate(&e));
         CK(cudaMemcpyAsync(ctx->d_events, ties.data(), ties.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->d_events_b, others.data(), others.size() * sizeof(int), cudaMemcpyHostToDevice, s));
         if (!FM_OVERLAP_MAIN) CK(cudaEventRecord(r0, s));
@@ -756,41 +883,53 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             // each part's main sweep: the near-tie events' on stream2 ahead of
             // their extra sweeps, the others' on the context stream
             int rc = stream_pass((int)ties.size(), ctx->d_events, 0, ctx->tie_segments, nullptr, ctx->d_list[0],
-                                 ctx->d_count[0], s2, FM_FRESH_SWEEP);
+                                 ctx->d_count[0], s2, FM_FRESH_SWEEP, true);
             if (rc) return rc;
             rc = stream_pass((int)others.size(), ctx->d_events_b, 0, ctx->sweep_segments, nullptr, ctx->d_list[0],
-                             ctx->d_count[0], s, FM_FRESH_SWEEP);
+                             ctx->d_count[0], s, FM_FRESH_SWEEP, true);
             if (rc) return rc;
             interval_nodes += (int64_t)nev * (int64_t)ctx->N;
             CK(cudaEventRecord(sw1, s));
             CK(cudaEventRecord(r0, s));
         }
+        if (tie_queue) CK(cudaMemsetAsync(ctx->d_count_b, 0, sizeof(int), s2));
+        CK(cudaEventRecord(pe[0], s2));
         for (int k = 0; k < ctx->tie_sweeps; ++k) {
             // (height segments by the time model for the near-tie events alone:
-            // their sweeps are the longer chain of the two parts)
+            // their sweeps are the longer chain of the two parts); the last one
+            // queues their first round's tiles on list b
+            const bool q = tie_queue && k == ctx->tie_sweeps - 1;
             const int rc = stream_pass((int)ties.size(), ctx->d_events, (k & 1) ? 0 : 4,
                                        FM_OVERLAP_MAIN ? ctx->tie_segments : (ctx->tie_segments > 0 ? ctx->tie_segments : 2),
-                                       nullptr, ctx->d_list[0], ctx->d_count[0], s2, false);
+                                       q ? ctx->d_flag : nullptr, ctx->d_list_b, ctx->d_count_b, s2, false, true,
+                                       act_cur(k), act_prev(k), act_items(k));
             if (rc) return rc;
         }
-        launch_initial_tiles((int)ties.size(), ctx->d_events, tpe, first, cnt, ctx->d_list_b, ctx->d_count_b,
-                             ctx->d_flag, s2);
-        launch_round(0, ctx->d_list_b, ctx->d_count_b, ctx->d_list[1], ctx->d_count[1], s2);
+        if (!tie_queue)
+            launch_initial_tiles((int)ties.size(), ctx->d_events, tpe, first, cnt, ctx->d_list_b, ctx->d_count_b,
+                                 ctx->d_flag, s2);
+        CK(cudaEventRecord(pe[1], s2));
+        CK(cudaMemsetAsync(ctx->d_count_c, 0, sizeof(int), s2));
+        launch_round(0, ctx->d_list_b, ctx->d_count_b, ctx->d_list_c, ctx->d_count_c, s2);
+        CK(cudaEventRecord(pe[2], s2));
         CK(cudaEventRecord(join, s2));
+        CK(cudaEventRecord(pe[3], s));
         if (FM_CERTIFY) {
             // the other events were swept once: only the tiles holding a node
             // the certification cannot clear, from those nodes
             CK(cudaMemsetAsync(ctx->d_count[0], 0, sizeof(int), s));
             certify(ctx->d_events_b, (int)others.size(), s);
+            CK(cudaEventRecord(pe[4], s));
             launch_round(0, ctx->d_list[0], ctx->d_count[0], ctx->d_list[1], ctx->d_count[1], s);
         } else {
             launch_initial_tiles((int)others.size(), ctx->d_events_b, tpe, first, cnt, ctx->d_list[0],
                                  ctx->d_count[0], ctx->d_flag, s);
             grid_override = (int)std::min<long long>((long long)others.size() * cnt, 1LL << 30);
+            CK(cudaEventRecord(pe[4], s));
             launch_round(0, ctx->d_list[0], ctx->d_count[0], ctx->d_list[1], ctx->d_count[1], s);
             grid_override = 0;
         }
-        CK(cudaStreamWaitEvent(s, join, 0));
+        CK(cudaEventRecord(pe[5], s));
         CK(cudaEventRecord(r1, s));
         ctx->launches += 2;
         CKL();
@@ -800,52 +939,49 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         cudaEventElapsedTime(&m, r0, r1);
         round_ms += m;
         ctx->round_ms_trace.push_back(m);
+        rounds = 1;
+        // the other events' rounds (re-sweeps take their indices in events b,
+        // which stream2 does not read)
+        RoundLists Lo{{ctx->d_list[1], ctx->d_list[0]}, {ctx->d_count[1], ctx->d_count[0]}, 0};
+        int left_o = resweeps_left;
+        bool done_o = false;
+        int rc = maybe_resweep(Lo.list[0], Lo.count[0], *ctx->h_count, ctx->d_events_b, left_o);
+        if (rc) return rc;
+        rc = converge(Lo, true, ctx->d_events_b, left_o, done_o);
+        if (rc) return rc;
+        // then the near-tie events' (their chain on stream2 has ended)
+        CK(cudaStreamWaitEvent(s, join, 0));
+        CK(cudaMemcpyAsync(ctx->h_count, ctx->d_count_c, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        cudaEventElapsedTime(&ctx->part_ms[0], pe[0], pe[1]);
+        cudaEventElapsedTime(&ctx->part_ms[1], pe[1], pe[2]);
+        cudaEventElapsedTime(&ctx->part_ms[2], pe[3], pe[4]);
+        cudaEventElapsedTime(&ctx->part_ms[3], pe[4], pe[5]);
+        for (auto &e : pe) cudaEventDestroy(e);
         cudaEventDestroy(fork);
         cudaEventDestroy(join);
         cudaEventDestroy(r0);
         cudaEventDestroy(r1);
-        rounds = 1;
-        const int rc = maybe_resweep(1);
+        RoundLists Lt{{ctx->d_list_c, ctx->d_list[0]}, {ctx->d_count_c, ctx->d_count[0]}, 0};
+        int left_t = resweeps_left;
+        bool done_t = false;
+        if (done_o) {
+            rc = maybe_resweep(Lt.list[0], Lt.count[0], *ctx->h_count, ctx->d_events, left_t);
+            if (rc) return rc;
+            rc = converge(Lt, true, ctx->d_events, left_t, done_t);
+            if (rc) return rc;
+        }
+        done = done_o && done_t;
+    } else {
+        RoundLists L{{ctx->d_list[0], ctx->d_list[1]}, {ctx->d_count[0], ctx->d_count[1]}, 0};
+        const int rc = converge(L, false, ctx->d_events, resweeps_left, done);
         if (rc) return rc;
-        if (*ctx->h_count == 0) done = true;
-    }
-    while (!done && rounds < max_rounds) {
-        int k;
-        const int first_round = rounds;
-        const int chunk_now = resweeps_left > 0 ? 1 : chunk;
-        while ((int)ctx->round_events.size() < 2 * chunk) {
-            cudaEvent_t e;
-            CK(cudaEventCreate(&e));
-            ctx->round_events.push_back(e);
-        }
-        for (k = 0; k < chunk_now && rounds < max_rounds; ++k, ++rounds) {
-            const int cur = rounds & 1, nxt = cur ^ 1;
-            CK(cudaMemsetAsync(ctx->d_count[nxt], 0, sizeof(int), s));
-            CK(cudaEventRecord(ctx->round_events[2 * k], s));
-            // the first round's tile count is known on the host: one CTA per
-            // tile, so blocks free up as they finish
-            if (rounds == 0 && FM_ROUND0_PER_TILE && !verified && mode != kPoint && !certify_alone)
-                grid_override = (int)std::min<long long>((long long)nev * cnt, 1LL << 30);
-            launch_round(rounds, ctx->d_list[cur], ctx->d_count[cur], ctx->d_list[nxt], ctx->d_count[nxt], s);
-            grid_override = 0;
-            CK(cudaEventRecord(ctx->round_events[2 * k + 1], s));
-        }
-        CKL();
-        const int last_next = ((rounds - 1) & 1) ^ 1;
-        CK(cudaMemcpyAsync(ctx->h_count, ctx->d_count[last_next], sizeof(int), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        for (int q = 0; q < rounds - first_round; ++q) {
-            float m = 0.0f;
-            cudaEventElapsedTime(&m, ctx->round_events[2 * q], ctx->round_events[2 * q + 1]);
-            round_ms += m;
-            if ((int)ctx->round_ms_trace.size() < fm3dt_ctx::kTraceRounds) ctx->round_ms_trace.push_back(m);
-        }
-        const int rc = maybe_resweep(last_next);
-        if (rc) return rc;
-        if (*ctx->h_count == 0) done = true;
     }
     CK(cudaEventRecord(ev1, s));
     CK(cudaMemcpyAsync(ctx->h_stats, ctx->d_stats, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    if (ctx->act_sweeps > 0)
+        CK(cudaMemcpyAsync(ctx->h_act_items, ctx->d_act_items, 2 * ctx->act_sweeps * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, s));
     int kerr = 0;
     CK(cudaMemcpyAsync(&kerr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     ctx->h_base.resize(nev);
@@ -962,6 +1098,20 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
                                 std::string(#call) + ": " + cudaGetErrorString(e_));                  \
     } while (0)
     CKC(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    {
+        // the scratch pool of the context's calls (the dense Frechet rows of
+        // a ray call are the largest): its memory is kept between calls
+        // rather than returned to the system at every synchronisation
+        int dev = 0;
+        CKC(cudaGetDevice(&dev));
+        cudaMemPoolProps pp{};
+        pp.allocType = cudaMemAllocationTypePinned;
+        pp.location.type = cudaMemLocationTypeDevice;
+        pp.location.id = dev;
+        CKC(cudaMemPoolCreate(&ctx->pool, &pp));
+        uint64_t keep = UINT64_MAX;
+        CKC(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    }
     const size_t nvel = (size_t)(d.nvr + 2) * (d.nvx + 2) * (d.nvz + 2);
     const size_t npad = (size_t)(d.nnr + 3) * (d.nnx + 3) * (d.nnz + 3);
     CKC(cudaMalloc(&ctx->d_velv, nvel * sizeof(double)));
@@ -994,6 +1144,9 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMalloc(&ctx->d_events_b, ctx->maxev * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_list_b, ctx->flag_capacity * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_count_b, sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_list_c, ctx->flag_capacity * sizeof(int)));
+    CKC(cudaMalloc(&ctx->d_act_items, 2 * fm3dt_ctx::kMaxTieSweeps * sizeof(unsigned long long)));
+    CKC(cudaMalloc(&ctx->d_count_c, sizeof(int)));
     CKC(cudaMalloc(&ctx->d_err, sizeof(int)));
     {
         const char *env = std::getenv("FM3DT_TMA");
@@ -1114,7 +1267,7 @@ int fm3dt_solve_point(fm3dt_ctx *ctx, int nev, const double *src, int refine, in
     ctx->launches += 1;
     if (!refine) {
         PointSource *d_src = nullptr;
-        DeviceScratch sc(s);
+        DeviceScratch sc(ctx);
         CK(sc.alloc(&d_src, (size_t)nev));
         CK(cudaMemcpyAsync(d_src, ps.data(), nev * sizeof(PointSource), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(ctx->d_box, box.data(), box.size() * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -1174,7 +1327,7 @@ int fm3dt_solve_point(fm3dt_ctx *ctx, int nev, const double *src, int refine, in
             CK(cudaMemcpyAsync(fc->d_box, fb, sizeof fb, cudaMemcpyHostToDevice, fc->stream));
             CK(cudaMemcpyAsync(fc->d_box_init, fb, sizeof fb, cudaMemcpyHostToDevice, fc->stream));
             PointSource *d_src = nullptr;
-            DeviceScratch sc(fc->stream);
+            DeviceScratch sc(fc);
             CK(sc.alloc(&d_src, 1));
             CK(cudaMemcpyAsync(d_src, &ps[e], sizeof(PointSource), cudaMemcpyHostToDevice, fc->stream));
             launch_point_analytic(fg, fc->prec, fc->d_veln, 1, d_src, fc->d_box, fc->d_T, fc->stream);
@@ -1214,7 +1367,7 @@ int fm3dt_receiver_times(fm3dt_ctx *ctx, int nrc, const double *rcr, const doubl
     RecCell *d_cells = nullptr;
     float *d_out = nullptr;
     const int nev = ctx->nev_solved;
-    DeviceScratch sc(ctx->stream);
+    DeviceScratch sc(ctx);
     CK(sc.alloc(&d_cells, (size_t)nrc));
     CK(sc.alloc(&d_out, (size_t)nev * nrc));
     CK(cudaMemcpyAsync(d_cells, cells.data(), nrc * sizeof(RecCell), cudaMemcpyHostToDevice, ctx->stream));
@@ -1233,7 +1386,7 @@ int fm3dt_receiver_times_device(fm3dt_ctx *ctx, int nrc, const double *d_rcr, co
     if (ctx->nev_solved < 1) return fail(ctx, FM3DT_ESTATE, "no solved events");
     if (nrc == 0) return FM3DT_OK;
     cudaStream_t s = ctx->stream;
-    DeviceScratch sc(s);
+    DeviceScratch sc(ctx);
     int *d_bad = nullptr;
     CK(sc.alloc(&d_bad, 1));
     CK(cudaMemsetAsync(d_bad, 0x7f, sizeof(int), s));           // 0x7f7f7f7f: none
@@ -1347,7 +1500,7 @@ int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double 
     }
     const int nrows = ctx->nev_solved * nrc;
     cudaStream_t s = ctx->stream;
-    DeviceScratch sc(s);
+    DeviceScratch sc(ctx);
     double *d_rec = nullptr, *d_end = nullptr;
     int64_t *d_rowptr = nullptr;
     CK(sc.alloc(&d_rec, 3 * (size_t)nrc));
@@ -1398,7 +1551,7 @@ int fm3dt_rays_frechet_device(fm3dt_ctx *ctx, int nrc, const double *d_rcr, cons
     if (total) *total = 0;
     if (nrc == 0) return FM3DT_OK;
     const int nrows = ctx->nev_solved * nrc;
-    DeviceScratch sc(ctx->stream);
+    DeviceScratch sc(ctx);
     int64_t n = 0;
     float *d_fdm = nullptr;
     rc = rays_trace(ctx, sc, nrc, d_rcr, d_rcx, d_rcz, want_rows, d_endpoints, d_row_ptr, &n, &d_fdm);
@@ -1424,7 +1577,7 @@ int fm3dt_get_times(fm3dt_ctx *ctx, int event, double *ttn)
     if (!ctx || !ttn) return FM3DT_EINVAL;
     if (event < 0 || event >= ctx->nev_solved) return fail(ctx, FM3DT_EINVAL, "event not solved");
     double *d_out = nullptr;
-    DeviceScratch sc(ctx->stream);
+    DeviceScratch sc(ctx);
     CK(sc.alloc(&d_out, ctx->N));
     const double base = ctx->prec == FM3DT_FP64 ? 0.0 : ctx->h_base[event];
     launch_to_absolute(ctx->g, ctx->prec, ctx->d_T, (size_t)event * ctx->N, base, d_out, ctx->stream);
@@ -1461,7 +1614,7 @@ int fm3dt_set_times(fm3dt_ctx *ctx, int event, int nev_total, const double *ttn)
     if ((int)ctx->h_base.size() < nev_total) ctx->h_base.resize(nev_total, 0.0);
     ctx->h_base[event] = base;
     double *d_in = nullptr;
-    DeviceScratch sc(ctx->stream);
+    DeviceScratch sc(ctx);
     CK(sc.alloc(&d_in, ctx->N));
     CK(cudaMemcpyAsync(d_in, ttn, ctx->N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     launch_from_absolute(ctx->g, ctx->prec, d_in, base, ctx->d_T, (size_t)event * ctx->N, ctx->stream);
@@ -1535,6 +1688,24 @@ int fm3dt_round_trace(fm3dt_ctx *ctx, int cap, int64_t *tiles, int64_t *updates)
     return ctx->last_rounds;
 }
 
+int fm3dt_tie_sweep_items(fm3dt_ctx *ctx, int cap, int64_t *run, int64_t *skipped)
+{
+    if (!ctx || cap < 0) return FM3DT_EINVAL;
+    const int n = std::min(cap, ctx->act_sweeps);
+    for (int i = 0; i < n; ++i) {
+        if (run) run[i] = (int64_t)ctx->h_act_items[2 * i];
+        if (skipped) skipped[i] = (int64_t)ctx->h_act_items[2 * i + 1];
+    }
+    return ctx->act_sweeps;
+}
+
+int fm3dt_part_ms(fm3dt_ctx *ctx, float *ms)
+{
+    if (!ctx || !ms) return FM3DT_EINVAL;
+    for (int i = 0; i < 4; ++i) ms[i] = ctx->part_ms[i];
+    return FM3DT_OK;
+}
+
 int fm3dt_round_trace_ms(fm3dt_ctx *ctx, int cap, float *ms)
 {
     if (!ctx || cap < 0) return FM3DT_EINVAL;
@@ -1583,6 +1754,11 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_events_b);
     cudaFree(ctx->d_list_b);
     cudaFree(ctx->d_count_b);
+    cudaFree(ctx->d_list_c);
+    cudaFree(ctx->d_act_items);
+    cudaFree(ctx->d_count_c);
+    cudaFree(ctx->d_act[0]);
+    cudaFree(ctx->d_act[1]);
     cudaFree(ctx->d_err);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     if (ctx->h_dir) cudaFreeHost(ctx->h_dir);
@@ -1605,6 +1781,7 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     if (ctx->h_count) cudaFreeHost(ctx->h_count);
     if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     delete ctx;
 }
 

@@ -115,6 +115,17 @@ struct StreamArgs {
     int *flag, *list, *count;
     int tr, tx, tz;             // the rounds' tile shape and tile counts
     int ntr, ntx, ntz, tiles_per_event;
+    // activity (a chain of sweeps of the same events and height segments):
+    // per item (event ordinal, segment, column block in grid order) whether
+    // a node changed in this sweep (act_cur) and in the previous one
+    // (act_prev).  An item runs when it or a face-neighbour item changed in
+    // the previous sweep, or an upstream face-neighbour item changed earlier
+    // in this one; act_cur null: no tracking, act_prev null: every item runs.
+    unsigned char *act_cur;
+    const unsigned char *act_prev;
+    // with tracking and a previous sweep (or null): [0] items that ran,
+    // [1] items skipped
+    unsigned long long *act_items;
 };
 
 void launch_stream_f32(int idx, int grid, const StreamArgs<float> &a, cudaStream_t st);
@@ -252,6 +263,7 @@ struct fm3dt_ctx {
     size_t N = 0;       // nodes per event
     size_t NB = 0;      // bottom-frame nodes per event
     cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;   // scratch of the context's calls, kept between them
     // device buffers
     double *d_velv = nullptr;
     double *d_veln = nullptr;
@@ -307,6 +319,17 @@ struct fm3dt_ctx {
     int *d_events_b = nullptr;    // [maxev] the other events
     int *d_list_b = nullptr;      // [flag_capacity]
     int *d_count_b = nullptr;
+    int *d_list_c = nullptr;      // [flag_capacity] what the near-tie events' first round queues
+    int *d_count_c = nullptr;
+    // item activity of the near-tie events' extra sweeps (this sweep's and
+    // the previous one's, alternating), grown on demand
+    unsigned char *d_act[2] = {nullptr, nullptr};
+    size_t act_bytes = 0;
+    // items run / skipped by each of the last solve's near-tie extra sweeps
+    static constexpr int kMaxTieSweeps = 16;
+    unsigned long long *d_act_items = nullptr;   // [2 * kMaxTieSweeps]
+    unsigned long long h_act_items[2 * kMaxTieSweeps] = {};
+    int act_sweeps = 0;
     // TMA tensor maps of the field, by round tile shape (encoded on first use)
     int *d_err = nullptr;         // raised by a kernel whose bounded wait gave up
     bool tmap_ok[fm3dt::kNumShapes] = {};
@@ -318,14 +341,16 @@ struct fm3dt_ctx {
     int64_t launches = 0;
     std::string err;
     // sweep passes captured as graphs, keyed by precision, sweep shape, event
-    // count, event list, flip, height segments, form, stream and tile shape
-    static constexpr int kSweepKey = 9;
+    // count, event list, flip, height segments, form, stream, tile shape,
+    // (flag mode) the flags and queue it writes and the activity it tracks
+    static constexpr int kSweepKey = 15;
     static constexpr size_t kSweepGraphs = 24;
     struct SweepGraph { long long key[kSweepKey]; cudaGraphExec_t exec; };
     std::vector<SweepGraph> sweep_graphs;
     bool sweep_graph_off = false;
     std::vector<cudaEvent_t> round_events;   // start/stop pairs of round kernels
     std::vector<float> round_ms_trace;       // device time of each round of the last solve
+    float part_ms[4] = {};                   // the first round's two parts (fm3dt_part_ms)
     // point sources: fixed node boxes, and the refined source grids' contexts
     int *d_box = nullptr;         // [maxev][6] fixed nodes
     int *d_box_init = nullptr;    // [maxev][6] nodes whose tiles start active

@@ -31,13 +31,21 @@ struct StreamRing {
     static constexpr int value = need <= 16 ? 16 : (need <= 32 ? 32 : 64);
 };
 
+// Queue tile w with flag bits `bits` unless it holds them already (flags only
+// gain bits while a sweep runs, so a stale read costs one needless atomic);
+// the node's new value is made visible before the flag that sends its tile
+// to a round.
 template <typename R>
 __device__ __forceinline__ void stream_queue(const StreamArgs<R> &a, int w, int bits)
 {
-    if (!(atomicOr(&a.flag[w], bits | kQueued) & kQueued)) a.list[atomicAdd(a.count, 1)] = w;
+    const int want = bits | kQueued;
+    if ((__ldcg(a.flag + w) & want) == want) return;
+    __threadfence();
+    if (!(atomicOr(&a.flag[w], want) & kQueued)) a.list[atomicAdd(a.count, 1)] = w;
 }
 
-// A node changed in the verification sweep: its tile recomputes every node,
+// A node changed in a flag-mode sweep (a verification sweep, a re-sweep, the
+// near-tie events' last extra sweep): its tile recomputes every node,
 // and each face neighbour whose 2-deep halo holds the node recomputes the
 // nodes next to that face (the flag bits of the rounds).
 template <typename R>
@@ -54,6 +62,41 @@ __device__ void stream_mark(const StreamArgs<R> &a, int e, int gr, int gx, int g
     if (xi >= a.tx - 2 && tj < a.ntx - 1) stream_queue(a, w + a.ntz, kFaceXm);
     if (zi < 2 && tk > 0) stream_queue(a, w - 1, kFaceZp);
     if (zi >= a.tz - 2 && tk < a.ntz - 1) stream_queue(a, w + 1, kFaceZm);
+}
+
+// Whether an item of a tracked sweep with a previous sweep runs (the same
+// answer in every lane): lanes 0-6 read the previous sweep's activity of the
+// item and its six face neighbours, lanes 7-9 this sweep's of its upstream
+// neighbours (below, and before it along theta and phi, already swept).  A
+// skipped item's activity is set to 0 here, and the item counted as run
+// (items[0]) or skipped (items[1]) when items is not null.  Out of line, so
+// that its registers stay out of the sweep's step loop.
+static __device__ __noinline__ bool stream_item_active(const unsigned char *prev, unsigned char *cur, int lane,
+                                                       int k, int nsegs, int seg, int bx, int bz, int nbx, int nbz,
+                                                       bool sx, bool sz, unsigned long long *items)
+{
+    const size_t self = ((size_t)(k * nsegs + seg) * nbx + bx) * nbz + bz;
+    int ds = 0, dx = 0, dz = 0;
+    const unsigned char *src = prev;
+    if (lane >= 1 && lane <= 6) {
+        const int ax = (lane - 1) >> 1, sg = (lane & 1) ? -1 : 1;
+        if (ax == 0) ds = sg; else if (ax == 1) dx = sg; else dz = sg;
+    } else if (lane >= 7 && lane <= 9) {
+        src = cur;
+        if (lane == 7) ds = -1; else if (lane == 8) dx = sx ? -1 : 1; else dz = sz ? -1 : 1;
+    }
+    bool hit = false;
+    if (lane <= 9) {
+        const int s_ = seg + ds, x_ = bx + dx, z_ = bz + dz;
+        if (s_ >= 0 && s_ < nsegs && x_ >= 0 && x_ < nbx && z_ >= 0 && z_ < nbz)
+            hit = __ldcg(src + ((size_t)(k * nsegs + s_) * nbx + x_) * nbz + z_) != 0;
+    }
+    const bool run = __any_sync(0xffffffffu, hit);
+    if (lane == 0) {
+        if (items) atomicAdd(items + (run ? 0 : 1), 1ull);
+        if (!run) cur[self] = 0;
+    }
+    return run;
 }
 
 // FRESH: the main sweep of a solve, from an unset field (every node except
@@ -74,6 +117,10 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
     constexpr int LX = SX + 4, LZ = SZ + 4, LAYER = LX * LZ;
     constexpr int RING = StreamRing<SX, SZ>::value;
     __shared__ R ring[RING * LAYER];
+    // the item's activity slot and whether one of its nodes changed (kept
+    // here rather than in registers through the step loop)
+    __shared__ size_t s_aslot;
+    __shared__ int s_changed;
     using TL = Tile<R, 1, SX, SZ>;
     const FieldArgs<R> &f = a.f;
     const int lane = threadIdx.x;
@@ -100,6 +147,20 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
         const int gx = x0 + lx, gz = z0 + lz;
         const bool colv = gx < f.nnx && gz < f.nnz;
         R *Te = f.T + (size_t)e * N;
+        // activity: this item's slot, and whether it runs
+        if (!FRESH && a.act_cur) {
+            const int nsegs = (f.nnr + a.seg_len - 1) / a.seg_len;
+            const int bx = x0 / SX, bz = z0 / SZ;
+            const size_t aslot = ((size_t)(k * nsegs + seg) * a.nbx + bx) * a.nbz + bz;
+            __syncwarp();
+            if (lane == 0) {
+                s_aslot = aslot;
+                s_changed = 0;
+            }
+            if (a.act_prev && !stream_item_active(a.act_prev, a.act_cur, lane, k, nsegs, seg, bx, bz, a.nbx, a.nbz,
+                                                  sx, sz, a.act_items))
+                continue;
+        }
         // layer rp (counted upward from the bottom) into registers (this
         // lane's share of the layer), unset outside the grid; then into its
         // ring slot
@@ -181,18 +242,16 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
                     if (fbits(v) != fbits(old)) {
                         ring[((rp + RING) & (RING - 1)) * LAYER + c] = v;
                         Te[((size_t)gr * f.nnx + gx) * f.nnz + gz] = v;
-                        if (a.flag) {
-                            // the value before its tile's flag, for rounds
-                            // that read it
-                            __threadfence();
-                            stream_mark(a, e, gr, gx, gz);
-                        }
+                        if (!FRESH && a.act_cur) s_changed = 1;
+                        if (a.flag) stream_mark(a, e, gr, gx, gz);
                     }
                 }
             }
             __syncwarp();
         }
+        if (!FRESH && a.act_cur && lane == 0) a.act_cur[s_aslot] = (unsigned char)s_changed;
     }
+
 }
 
 template <typename R, int SX, int SZ>

@@ -57,7 +57,7 @@ EXPORTS = [
     "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_resume",
     "fm3dt_solve_planewave", "fm3dt_solve_point",
     "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_receiver_times_device", "fm3dt_rays_frechet_device", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
-    "fm3dt_set_tuning", "fm3dt_set_schedule", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_round_trace_ms", "fm3dt_tile_shapes", "fm3dt_tile_shape",
+    "fm3dt_set_tuning", "fm3dt_set_schedule", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_round_trace_ms", "fm3dt_part_ms", "fm3dt_tie_sweep_items", "fm3dt_tile_shapes", "fm3dt_tile_shape",
     "fm3dt_launch_count",
     "fm3dt_last_error", "fm3dt_ctx_destroy",
 ]
@@ -98,6 +98,8 @@ def load(path: str | None = None):
     L.fm3dt_set_sweep_segments.argtypes = [vp, C.c_int, C.c_int]
     L.fm3dt_round_trace.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.fm3dt_round_trace_ms.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
+    L.fm3dt_part_ms.argtypes = [vp, C.POINTER(C.c_float)]
+    L.fm3dt_tie_sweep_items.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.fm3dt_tile_shapes.argtypes = [C.POINTER(C.c_int)]
     L.fm3dt_tile_shape.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.fm3dt_launch_count.argtypes = [vp]
@@ -244,6 +246,26 @@ class Solver:
         if n < 0:
             self._check(n)
         return m[:min(n, cap)].astype(np.float64)
+
+    def part_ms(self):
+        """Device times (ms) of the last solve's first round in two parts:
+        near-tie extra sweeps, their first round, the others' certification,
+        their first round (zeros for a solve in one part)."""
+        m = np.zeros(4, dtype=np.float32)
+        self._check(self._L.fm3dt_part_ms(self._ctx, m.ctypes.data_as(C.POINTER(C.c_float))))
+        return m.astype(np.float64)
+
+    def tie_sweep_items(self, cap: int = 16):
+        """Items run and skipped by each near-tie extra sweep of the last
+        solve: (run, skipped) arrays."""
+        run = np.zeros(cap, dtype=np.int64)
+        skip = np.zeros(cap, dtype=np.int64)
+        n = self._L.fm3dt_tie_sweep_items(self._ctx, cap, run.ctypes.data_as(C.POINTER(C.c_int64)),
+                                          skip.ctypes.data_as(C.POINTER(C.c_int64)))
+        if n < 0:
+            self._check(n)
+        n = min(n, cap)
+        return run[:n], skip[:n]
 
     def set_velocity(self, velv):
         velv = np.ascontiguousarray(velv, dtype=np.float64)
