@@ -437,7 +437,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     // previous one's or null), see StreamArgs.
     auto stream_pass = [&](int nitems, const int *events, int flip, int nseg, int *flag, int *list,
                            int *count, cudaStream_t st, bool fresh, bool recurs,
-                           unsigned char *act_cur = nullptr, const unsigned char *act_prev = nullptr,
+                           unsigned *act_cur = nullptr, const unsigned *act_prev = nullptr,
                            unsigned long long *act_items = nullptr) -> int {
         sweep_nodes += (int64_t)nitems * (int64_t)ctx->N;
         const int sgrid = stream_grid(fresh);
@@ -448,8 +448,10 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         if (rc) return rc;
         const auto &P = *PP;
         const int seg_len = (g.nnr + nseg - 1) / nseg;
-        const int nlaunch = (int)P.off.size();
-        // the pass's launches, one per hyperplane
+        // (items of one layer or column would miss a 2-deep neighbour)
+        const bool track = !fresh && act_cur && seg_len >= 2 && kStreamShapes[sidx].sx >= 2;
+        // the pass's launches, one per hyperplane (two with a tracked previous sweep)
+        const int nlaunch = (int)P.off.size() * (track && act_prev ? 2 : 1);
         auto enqueue = [&]() {
             for (size_t h = 0; h < P.off.size(); ++h) {
                 const long long items = (long long)P.cnt[h] * nitems;
@@ -465,11 +467,15 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                     a.list = list; a.count = count;
                     a.tr = ts.tr; a.tx = ts.tx; a.tz = ts.tz;
                     a.ntr = ntr; a.ntx = ntx; a.ntz = ntz; a.tiles_per_event = tpe;
-                    // (items of one layer or column would miss a 2-deep neighbour)
-                    const bool track = act_cur && seg_len >= 2 && kStreamShapes[sidx].sx >= 2;
                     a.act_cur = track ? act_cur : nullptr;
                     a.act_prev = track ? act_prev : nullptr;
+                    a.act_run = track ? ctx->d_act[2] : nullptr;
+                    // chunks of at least 4 layers, at most 32 of them per item
+                    a.act_shift = 2;
+                    while (((seg_len - 1) >> a.act_shift) >= 32) ++a.act_shift;
                     a.act_items = track ? act_items : nullptr;
+                    a.act_n = ctx->act_bytes / sizeof(unsigned);
+                    a.err = ctx->d_err;
                 };
                 if (ctx->prec == FM3DT_FP64) {
                     StreamArgs<double> a{};
@@ -540,7 +546,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     bool tie_act = false;              // ties' extra sweeps skip items where nothing changed
     // the activity buffers of extra sweep k: this sweep's and the previous one's
     auto act_cur = [&](int k) { return tie_act ? ctx->d_act[k & 1] : nullptr; };
-    auto act_prev = [&](int k) -> const unsigned char * { return tie_act && k > 0 ? ctx->d_act[(k - 1) & 1] : nullptr; };
+    auto act_prev = [&](int k) -> const unsigned * { return tie_act && k > 0 ? ctx->d_act[(k - 1) & 1] : nullptr; };
     auto act_items = [&](int k) { return tie_act && k < fm3dt_ctx::kMaxTieSweeps ? ctx->d_act_items + 2 * k : nullptr; };
     ctx->act_sweeps = 0;
     if (do_sweep && streaming) {
@@ -570,10 +576,11 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             CK(cudaMemsetAsync(ctx->d_flag, 0, (size_t)nev * tpe * sizeof(int), s));
             CK(cudaMemsetAsync(ctx->d_count[0], 0, sizeof(int), s));
         }
-        // item activity of the near-tie events' extra sweeps: one byte per
+        // item activity of the near-tie events' extra sweeps: one mask per
         // (event, segment, column block), for at most 127 segments
         if (FM_TIE_SKIP && !ties.empty() && ctx->tie_sweeps > 1) {
-            const size_t need = ties.size() * (size_t)std::min(127, g.nnr) * (size_t)nbx * (size_t)nbz;
+            const size_t need = ties.size() * (size_t)std::min(127, g.nnr) * (size_t)nbx * (size_t)nbz *
+                                sizeof(unsigned);
             if (need > ctx->act_bytes) {
                 CK(cudaStreamSynchronize(ctx->stream2));
                 for (auto &p : ctx->d_act) {
@@ -1012,6 +1019,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         st->interval_nodes = interval_nodes;
     }
     if (kerr == 2) return fail(ctx, FM3DT_ECUDA, "a tile copy (TMA) destination was not 128-byte aligned");
+    if (kerr & 4) return fail(ctx, FM3DT_ECUDA, "a tracked sweep met an activity slot out of range");
     if (kerr) return fail(ctx, FM3DT_ECUDA, "a tile copy (TMA) did not complete in time");
     if (!done) return fail(ctx, FM3DT_ENOCONV, "solver round limit reached before convergence");
     return FM3DT_OK;
@@ -1757,8 +1765,7 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_list_c);
     cudaFree(ctx->d_act_items);
     cudaFree(ctx->d_count_c);
-    cudaFree(ctx->d_act[0]);
-    cudaFree(ctx->d_act[1]);
+    for (auto p : ctx->d_act) cudaFree(p);
     cudaFree(ctx->d_err);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     if (ctx->h_dir) cudaFreeHost(ctx->h_dir);

@@ -116,13 +116,19 @@ struct StreamArgs {
     int tr, tx, tz;             // the rounds' tile shape and tile counts
     int ntr, ntx, ntz, tiles_per_event;
     // activity (a chain of sweeps of the same events and height segments):
-    // per item (event ordinal, segment, column block in grid order) whether
-    // a node changed in this sweep (act_cur) and in the previous one
-    // (act_prev).  An item runs when it or a face-neighbour item changed in
-    // the previous sweep, or an upstream face-neighbour item changed earlier
-    // in this one; act_cur null: no tracking, act_prev null: every item runs.
-    unsigned char *act_cur;
-    const unsigned char *act_prev;
+    // per item (event ordinal, segment, column block in grid order) a mask of
+    // its chunks of 1 << act_shift layers in which a node changed in this
+    // sweep (act_cur) and in the previous one (act_prev).  A step of an item
+    // runs when one of its nodes lies in a chunk that can change: one near a
+    // chunk that changed in the previous sweep (in the item or a face
+    // neighbour), or earlier in this one (an upstream neighbour, or the item
+    // itself); act_cur null: no tracking, act_prev null: everything runs.
+    unsigned *act_cur;
+    const unsigned *act_prev;
+    unsigned *act_run;          // the chunks of each item that run (stream_activity_kernel)
+    int act_shift;
+    size_t act_n;               // masks in each activity buffer
+    int *err;                   // bit 2 raised: an activity slot out of range (not accessed)
     // with tracking and a previous sweep (or null): [0] items that ran,
     // [1] items skipped
     unsigned long long *act_items;
@@ -323,7 +329,7 @@ struct fm3dt_ctx {
     int *d_count_c = nullptr;
     // item activity of the near-tie events' extra sweeps (this sweep's and
     // the previous one's, alternating), grown on demand
-    unsigned char *d_act[2] = {nullptr, nullptr};
+    unsigned *d_act[3] = {nullptr, nullptr, nullptr};   // [2]: the chunks that run
     size_t act_bytes = 0;
     // items run / skipped by each of the last solve's near-tie extra sweeps
     static constexpr int kMaxTieSweeps = 16;

@@ -64,39 +64,83 @@ __device__ void stream_mark(const StreamArgs<R> &a, int e, int gr, int gx, int g
     if (zi >= a.tz - 2 && tk < a.ntz - 1) stream_queue(a, w + 1, kFaceZm);
 }
 
-// Whether an item of a tracked sweep with a previous sweep runs (the same
-// answer in every lane): lanes 0-6 read the previous sweep's activity of the
-// item and its six face neighbours, lanes 7-9 this sweep's of its upstream
-// neighbours (below, and before it along theta and phi, already swept).  A
-// skipped item's activity is set to 0 here, and the item counted as run
-// (items[0]) or skipped (items[1]) when items is not null.  Out of line, so
-// that its registers stay out of the sweep's step loop.
-static __device__ __noinline__ bool stream_item_active(const unsigned char *prev, unsigned char *cur, int lane,
-                                                       int k, int nsegs, int seg, int bx, int bz, int nbx, int nbz,
-                                                       bool sx, bool sz, unsigned long long *items)
+// Activity of a tracked sweep, by chunks of 1 << act_shift layers of an
+// item (bit c of a mask: layers [c << act_shift, (c + 1) << act_shift) of the
+// item's segment).  Ahead of each launch of a tracked sweep with a previous
+// sweep, this kernel writes, for every item of the launch (one thread each),
+// the chunks whose nodes can change in this sweep (act_run), given the
+// previous sweep's changed chunks (act_prev) and this sweep's (act_cur,
+// written by the launches before): a node can change only if a node within
+// two layers or columns of it changed since it was last computed -- in this
+// item or a face neighbour in the previous sweep, or in an upstream face
+// neighbour (below, and before it along theta and phi) in this one.  A
+// lateral neighbour's chunk c holds the same layers as this item's chunk c,
+// and each changed chunk wakes its own and the adjacent chunks; the items
+// above and below meet this one in their (and its) two edge layers.  A
+// skipped item's changed chunks are 0.  Items run and skipped are added to
+// act_items; a slot beyond the act_n masks is not accessed (bit 2 of *err).
+template <typename R>
+__global__ void __launch_bounds__(128) stream_activity_kernel(StreamArgs<R> a)
 {
-    const size_t self = ((size_t)(k * nsegs + seg) * nbx + bx) * nbz + bz;
-    int ds = 0, dx = 0, dz = 0;
-    const unsigned char *src = prev;
-    if (lane >= 1 && lane <= 6) {
-        const int ax = (lane - 1) >> 1, sg = (lane & 1) ? -1 : 1;
-        if (ax == 0) ds = sg; else if (ax == 1) dx = sg; else dz = sg;
-    } else if (lane >= 7 && lane <= 9) {
-        src = cur;
-        if (lane == 7) ds = -1; else if (lane == 8) dx = sx ? -1 : 1; else dz = sz ? -1 : 1;
+    const long long count = (long long)a.hcount * a.nev;
+    const int nsegs = (a.f.nnr + a.seg_len - 1) / a.seg_len;
+    const int sh = a.act_shift;
+    unsigned nrun = 0, nskip = 0;
+    for (long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x; item < count;
+         item += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(item / a.hcount);
+        const int j = (int)(item - (long long)k * a.hcount);
+        const int e = a.events ? a.events[k] : k;
+        const int packed = a.hp_blocks[a.hoff + j];
+        const int seg = packed >> 24, bxp = (packed >> 12) & 0xfff, bzp = packed & 0xfff;
+        int dir = a.dir[e];
+        if (a.flip & 4) dir ^= ((dir >> 2) & 1) | (((dir >> 3) & 1) << 1);
+        dir ^= a.flip & 3;
+        const bool sx = dir & 1, sz = (dir >> 1) & 1;
+        const int bx = sx ? bxp : a.nbx - 1 - bxp, bz = sz ? bzp : a.nbz - 1 - bzp;
+        const int lo = seg * a.seg_len, nlay = min(a.f.nnr, lo + a.seg_len) - lo;
+        auto slot = [&](int s_, int x_, int z_) { return ((size_t)(k * nsegs + s_) * a.nbx + x_) * a.nbz + z_; };
+        auto mask = [&](const unsigned *src, int s_, int x_, int z_) -> unsigned {
+            if (s_ < 0 || s_ >= nsegs || x_ < 0 || x_ >= a.nbx || z_ < 0 || z_ >= a.nbz) return 0u;
+            const size_t q = slot(s_, x_, z_);
+            if (q >= a.act_n) {
+                atomicOr(a.err, 4);
+                return 0u;
+            }
+            return __ldcg(src + q);
+        };
+        auto spread = [](unsigned m) { return m | (m << 1) | (m >> 1); };
+        const unsigned *prev = a.act_prev, *cur = a.act_cur;
+        unsigned run = spread(mask(prev, seg, bx, bz) | mask(prev, seg, bx - 1, bz) | mask(prev, seg, bx + 1, bz) |
+                              mask(prev, seg, bx, bz - 1) | mask(prev, seg, bx, bz + 1) |
+                              mask(cur, seg, bx + (sx ? -1 : 1), bz) | mask(cur, seg, bx, bz + (sz ? -1 : 1)));
+        // the item below: its top two layers, next to this item's bottom chunk
+        const unsigned below_top2 = (1u << ((a.seg_len - 1) >> sh)) | (1u << ((a.seg_len - 2) >> sh));
+        if ((mask(prev, seg - 1, bx, bz) | mask(cur, seg - 1, bx, bz)) & below_top2) run |= 1u;
+        // the item above: its bottom chunk, next to this item's top two layers
+        if (mask(prev, seg + 1, bx, bz) & 1u)
+            run |= (1u << ((nlay - 1) >> sh)) | (nlay >= 2 ? 1u << ((nlay - 2) >> sh) : 0u);
+        const int nch = ((nlay - 1) >> sh) + 1;
+        if (nch < 32) run &= (1u << nch) - 1u;
+        const size_t self = slot(seg, bx, bz);
+        if (self < a.act_n) {
+            a.act_run[self] = run;
+            if (!run) a.act_cur[self] = 0;
+        } else {
+            atomicOr(a.err, 4);
+        }
+        if (run) ++nrun; else ++nskip;
     }
-    bool hit = false;
-    if (lane <= 9) {
-        const int s_ = seg + ds, x_ = bx + dx, z_ = bz + dz;
-        if (s_ >= 0 && s_ < nsegs && x_ >= 0 && x_ < nbx && z_ >= 0 && z_ < nbz)
-            hit = __ldcg(src + ((size_t)(k * nsegs + s_) * nbx + x_) * nbz + z_) != 0;
+    if (a.act_items) {
+        for (int o = 16; o > 0; o >>= 1) {
+            nrun += __shfl_xor_sync(0xffffffffu, nrun, o);
+            nskip += __shfl_xor_sync(0xffffffffu, nskip, o);
+        }
+        if ((threadIdx.x & 31) == 0 && (nrun | nskip)) {
+            atomicAdd(&a.act_items[0], (unsigned long long)nrun);
+            atomicAdd(&a.act_items[1], (unsigned long long)nskip);
+        }
     }
-    const bool run = __any_sync(0xffffffffu, hit);
-    if (lane == 0) {
-        if (items) atomicAdd(items + (run ? 0 : 1), 1ull);
-        if (!run) cur[self] = 0;
-    }
-    return run;
 }
 
 // FRESH: the main sweep of a solve, from an unset field (every node except
@@ -117,10 +161,11 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
     constexpr int LX = SX + 4, LZ = SZ + 4, LAYER = LX * LZ;
     constexpr int RING = StreamRing<SX, SZ>::value;
     __shared__ R ring[RING * LAYER];
-    // the item's activity slot and whether one of its nodes changed (kept
-    // here rather than in registers through the step loop)
+    // tracked sweeps (kept here rather than in registers through the step
+    // loop): the item's activity slot, its chunks that changed, and its
+    // chunks whose nodes can change (see stream_activity_kernel)
     __shared__ size_t s_aslot;
-    __shared__ int s_changed;
+    __shared__ unsigned s_changed, s_active;
     using TL = Tile<R, 1, SX, SZ>;
     const FieldArgs<R> &f = a.f;
     const int lane = threadIdx.x;
@@ -147,19 +192,20 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
         const int gx = x0 + lx, gz = z0 + lz;
         const bool colv = gx < f.nnx && gz < f.nnz;
         R *Te = f.T + (size_t)e * N;
-        // activity: this item's slot, and whether it runs
+        // activity: this item's slot, and the chunks that run
         if (!FRESH && a.act_cur) {
             const int nsegs = (f.nnr + a.seg_len - 1) / a.seg_len;
             const int bx = x0 / SX, bz = z0 / SZ;
             const size_t aslot = ((size_t)(k * nsegs + seg) * a.nbx + bx) * a.nbz + bz;
+            // (stream_activity_kernel wrote the chunks that run)
+            const unsigned run = a.act_prev ? (aslot < a.act_n ? __ldcg(a.act_run + aslot) : 0u) : ~0u;
+            if (!run) continue;
             __syncwarp();
             if (lane == 0) {
                 s_aslot = aslot;
                 s_changed = 0;
+                s_active = run;
             }
-            if (a.act_prev && !stream_item_active(a.act_prev, a.act_cur, lane, k, nsegs, seg, bx, bz, a.nbx, a.nbz,
-                                                  sx, sz, a.act_items))
-                continue;
         }
         // layer rp (counted upward from the bottom) into registers (this
         // lane's share of the layer), unset outside the grid; then into its
@@ -208,6 +254,13 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
             const typename TL::Params pcur = pnext;
             // the next node's slowness and spacings, one step ahead
             if (colv && rp + 1 >= lo && rp + 1 < hi) pnext = TL::params_global(f, f.nnr - 2 - rp, gx, gz);
+            // (tracked sweeps: the step runs when a lane's node lies in a
+            // chunk that can change)
+            if (!FRESH && a.act_cur &&
+                !__any_sync(0xffffffffu, colv && rp >= lo && rp < hi && ((s_active >> ((rp - lo) >> a.act_shift)) & 1u))) {
+                __syncwarp();
+                continue;
+            }
             if (colv && rp >= lo && rp < hi) {
                 const int gr = f.nnr - 1 - rp;
                 if (!TL::frozen(f, e, gr, gx, gz)) {
@@ -242,14 +295,19 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
                     if (fbits(v) != fbits(old)) {
                         ring[((rp + RING) & (RING - 1)) * LAYER + c] = v;
                         Te[((size_t)gr * f.nnx + gx) * f.nnz + gz] = v;
-                        if (!FRESH && a.act_cur) s_changed = 1;
+                        if (!FRESH && a.act_cur) {
+                            // this chunk changed; it and its neighbours can change further
+                            const unsigned b = 1u << ((rp - lo) >> a.act_shift);
+                            atomicOr(&s_changed, b);
+                            atomicOr(&s_active, b | (b << 1) | (b >> 1));
+                        }
                         if (a.flag) stream_mark(a, e, gr, gx, gz);
                     }
                 }
             }
             __syncwarp();
         }
-        if (!FRESH && a.act_cur && lane == 0) a.act_cur[s_aslot] = (unsigned char)s_changed;
+        if (!FRESH && a.act_cur && lane == 0 && s_aslot < a.act_n) a.act_cur[s_aslot] = s_changed;
     }
 
 }
@@ -258,6 +316,11 @@ template <typename R, int SX, int SZ>
 struct StreamKernels {
     static void sweep(int grid, const StreamArgs<R> &a, cudaStream_t st)
     {
+        if (!a.fresh && a.act_cur && a.act_prev) {
+            const long long items = (long long)a.hcount * a.nev;
+            const int blocks = (int)std::min<long long>((items + 127) / 128, 4096);
+            stream_activity_kernel<R><<<blocks, 128, 0, st>>>(a);
+        }
         if (a.fresh)
             stream_sweep_kernel<R, SX, SZ, true><<<grid, 32, 0, st>>>(a);
         else
