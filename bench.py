@@ -414,10 +414,15 @@ def run_ours(a):
         solver.set_sweep_shape(sweep_shape)
         if a.schedule:
             solver.set_schedule(int(a.schedule[0]), a.schedule[1], int(a.schedule[2]), a.schedule[3])
-        tuned = (a.shape, a.passes or 64, sweep_shape, None, tuple(a.schedule) if a.schedule else None)
+        tuned = (a.shape, a.passes or 64, sweep_shape, None, tuple(a.schedule) if a.schedule else None,
+                 a.segments[1])
     else:
-        # (tuned on up to 128 of the events: the choice never changes results)
-        tuned = autotune.autotune(solver, fptr, min(nev, 128), device=True)
+        # (tuned on the whole batch, up to 512 events: the choice never changes
+        # results; the near-tie sweeps' segments only when not given)
+        # (each trial the median of three solves: a single one can be slowed by
+        # the host, which drives the rounds)
+        tuned = autotune.autotune(solver, fptr, min(nev, 512), device=True, repeats=3,
+                                  tune_segments=tuple(a.segments) == (0, 0))
     shape = fm3dt.tile_shapes()[tuned[0]]
     sweep_shape_dims = fm3dt.sweep_shapes()[tuned[2]]
 
@@ -586,7 +591,8 @@ def run_ours(a):
         "config": workload_config(a.config, a.step, h, nev, nrc, a.prec),
         "tuning": {"tile_shape": list(shape), "max_passes": tuned[1], "sweep_tile_shape": list(sweep_shape_dims),
                    "schedule": dict(zip(("tie_sweeps", "tie_ratio", "resweeps", "resweep_frac"), tuned[4]))
-                   if tuned[4] else "default"},
+                   if tuned[4] else "default",
+                   "tie_segments": tuned[5] if tuned[5] is not None else a.segments[1]},
         "p50_ms": p50, "p99_ms": p99,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

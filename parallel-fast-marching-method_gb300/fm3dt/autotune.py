@@ -3,10 +3,11 @@
 Tunes, on a sample batch, (1) the shape of the directional sweep (tile or
 streaming),
 (2) the tile shape and in-tile pass cap of the fast-iterative rounds (the
-shape also fixes the CTA size: one thread per column), and (3) the solve
+shape also fixes the CTA size: one thread per column), (3) the solve
 schedule -- how many extra sweeps, alternately reversed and forward, the
-near-tie events get and how wide the near-tie band is -- keeping the fastest
-device time.  The schedule depends most on the model: on a smooth one
+near-tie events get and how wide the near-tie band is -- and (4) the height
+segments of those sweeps (automatic, or a few more, whose smaller items skip
+more where nothing changed), keeping the fastest device time.  The schedule depends most on the model: on a smooth one
 (Gaussian node noise) two extra sweeps of the events within ~6 degrees of an
 axis are best; on a checkerboard, whose fast cells carry head waves across
 the sweep direction, five or six of them over a band twice as wide halve the
@@ -21,7 +22,9 @@ from . import sweep_shapes, tile_shapes
 
 PASS_CAPS = (16, 64)
 # (extra sweeps of the near-tie events, near-tie band)
-SCHEDULES = ((2, 0.1), (3, 0.15), (4, 0.15), (5, 0.15), (5, 0.2), (6, 0.2))
+SCHEDULES = ((2, 0.1), (3, 0.15), (4, 0.15), (5, 0.15), (5, 0.2), (6, 0.2), (8, 0.2))
+# height segments of the near-tie events' sweeps (0: the solver's time model)
+TIE_SEGMENTS = (0, 4, 8)
 
 
 def _time(solver, frames_ptr, nev, device, repeats):
@@ -29,10 +32,12 @@ def _time(solver, frames_ptr, nev, device, repeats):
     return float(np.median([solver.solve_ptr(nev, frames_ptr, device)["ms"] for _ in range(repeats)]))
 
 
-def autotune(solver, frames_ptr: int, nev: int, device: bool = True, repeats: int = 1):
-    """Returns (round_shape, max_passes, sweep_shape, ms, schedule) and applies
-    it; schedule = (tie_sweeps, tie_ratio, resweeps, resweep_frac), negative
-    values being the defaults kept."""
+def autotune(solver, frames_ptr: int, nev: int, device: bool = True, repeats: int = 1,
+             tune_segments: bool = True):
+    """Returns (round_shape, max_passes, sweep_shape, ms, schedule,
+    tie_segments) and applies it; schedule = (tie_sweeps, tie_ratio,
+    resweeps, resweep_frac), negative values being the defaults kept;
+    tie_segments None when not tuned (the solver's setting is kept)."""
     nshapes = len(tile_shapes())
     round_shape, cap = 0, PASS_CAPS[0]
     solver.set_tuning(round_shape, cap, 0, 1)
@@ -58,4 +63,13 @@ def autotune(solver, frames_ptr: int, nev: int, device: bool = True, repeats: in
         if best_sched is None or ms < best_sched[2]:
             best_sched = (ts, tr, ms)
     solver.set_schedule(best_sched[0], best_sched[1], -1, -1.0)
-    return best[0], best[1], best_sweep[0], min(best[2], best_sched[2]), (best_sched[0], best_sched[1], -1, -1.0)
+    best_seg = (None, best_sched[2])
+    if tune_segments:
+        for ts in TIE_SEGMENTS:
+            solver.set_sweep_segments(0, ts)
+            ms = _time(solver, frames_ptr, nev, device, repeats)
+            if best_seg[0] is None or ms < best_seg[1]:
+                best_seg = (ts, ms)
+        solver.set_sweep_segments(0, best_seg[0])
+    return (best[0], best[1], best_sweep[0], min(best[2], best_sched[2], best_seg[1]),
+            (best_sched[0], best_sched[1], -1, -1.0), best_seg[0])
