@@ -7,8 +7,10 @@
 // rows it creates disappear; the global outer faces stop a ray exactly where
 // the reference's boundary subdomains stop it (clip to the first face
 // crossed, F:7474-7541).  The ray path is double precision like the
-// reference's; the row's weights are single precision and accumulate in the
-// same order as the reference's REAL(4) fdm (F:7722-7732), including its quirks:
+// reference's (with the single-precision field, each step's direction is
+// formed in single precision, see rays_kernel); the row's weights are single
+// precision and accumulate in the same order as the reference's REAL(4) fdm
+// (F:7722-7732), including its quirks:
 // the segment clipped at the grid face is integrated with the full nominal
 // step length (dinc from vrat*dpl), and the start-point B-spline weights of a
 // sub-segment that follows a velocity-cell crossing keep the indices of the
@@ -77,6 +79,21 @@ __global__ void __launch_bounds__(kRayBlock) rays_kernel(RayArgs a)
     const float fnr = (float)g.dnr, fnx = (float)g.dnx, fnz = (float)g.dnz;
     const float inr = 1.0f / fnr, inx = 1.0f / fnx, inz = 1.0f / fnz;
     const double ivr_ = 1.0 / g.dvr, ivx_ = 1.0 / g.dvx, ivz_ = 1.0 / g.dvz;
+    // With the single-precision (offset) field the direction of each step --
+    // gradient, its norm, sin(colatitude) -- is formed in single precision
+    // (G = float), and cells are located by multiplying with the spacings'
+    // reciprocals; positions, crossings and clipping stay in double.  With
+    // the double-precision field everything is the reference's double
+    // arithmetic (G = double, divisions).
+    using G = R;
+    constexpr bool kFast = sizeof(R) == sizeof(float);
+    const double inr_ = 1.0 / g.dnr, inx_ = 1.0 / g.dnx, inz_ = 1.0 / g.dnz;
+    auto cellr = [&](double v) { return kFast ? (int)floor((g.rgor - v) * inr_) + 1 : (int)floor((g.rgor - v) / g.dnr) + 1; };
+    auto cellx = [&](double v) { return kFast ? (int)floor((v - g.rgox) * inx_) + 1 : (int)floor((v - g.rgox) / g.dnx) + 1; };
+    auto cellz = [&](double v) { return kFast ? (int)floor((v - g.rgoz) * inz_) + 1 : (int)floor((v - g.rgoz) / g.dnz) + 1; };
+    auto vcellr = [&](double v) { return kFast ? (int)floor((g.gor - v) * ivr_) + 1 : (int)floor((g.gor - v) / g.dvr) + 1; };
+    auto vcellx = [&](double v) { return kFast ? (int)floor((v - g.gox) * ivx_) + 1 : (int)floor((v - g.gox) / g.dvx) + 1; };
+    auto vcellz = [&](double v) { return kFast ? (int)floor((v - g.goz) * ivz_) + 1 : (int)floor((v - g.goz) / g.dvz) + 1; };
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
         const int e = q / a.nrc, i = q - e * a.nrc;
         const R *Te = (const R *)a.T + (size_t)e * N;
@@ -112,8 +129,8 @@ __global__ void __launch_bounds__(kRayBlock) rays_kernel(RayArgs a)
                 c[3 * kRayBlock] = 0.0f;
             }
         };
-        auto TD = [&](int iz, int ix, int ir) -> double {
-            return (double)Te[((size_t)(ir - 1) * g.nnx + (ix - 1)) * g.nnz + (iz - 1)];
+        auto TD = [&](int iz, int ix, int ir) -> G {
+            return (G)Te[((size_t)(ir - 1) * g.nnx + (ix - 1)) * g.nnz + (iz - 1)];
         };
         int st = 0;
         double rgr = a.rcr[i], rgx = a.rcx[i], rgz = a.rcz[i];
@@ -133,34 +150,34 @@ __global__ void __launch_bounds__(kRayBlock) rays_kernel(RayArgs a)
         if (inside) {
             for (int jstep = 1; jstep <= maxrp; ++jstep) {
                 ++steps;
-                double dtr = 0.0;
+                G dtr = 0;
                 int temp = 0;
                 if (TD(ipz, ipx, ipr + 1) < TD(ipz, ipx, ipr)) { dtr = dtr + TD(ipz, ipx, ipr + 1) - TD(ipz, ipx, ipr); temp++; }
                 if (TD(ipz + 1, ipx, ipr + 1) < TD(ipz + 1, ipx, ipr)) { dtr = dtr + TD(ipz + 1, ipx, ipr + 1) - TD(ipz + 1, ipx, ipr); temp++; }
                 if (TD(ipz + 1, ipx + 1, ipr + 1) < TD(ipz + 1, ipx + 1, ipr)) { dtr = dtr + TD(ipz + 1, ipx + 1, ipr + 1) - TD(ipz + 1, ipx + 1, ipr); temp++; }
                 if (TD(ipz, ipx + 1, ipr + 1) < TD(ipz, ipx + 1, ipr)) { dtr = dtr + TD(ipz, ipx + 1, ipr + 1) - TD(ipz, ipx + 1, ipr); temp++; }
-                if (temp != 0) dtr = dtr / ((double)temp * g.dnr);
-                const double rcell = g.earth + g.rgor - (double)(ipr - 1) * g.dnr;
-                double dtx = TD(ipz, ipx + 1, ipr) - TD(ipz, ipx, ipr);
+                if (temp != 0) dtr = dtr / ((G)temp * (G)g.dnr);
+                const G rcell = (G)(g.earth + g.rgor - (double)(ipr - 1) * g.dnr);
+                G dtx = TD(ipz, ipx + 1, ipr) - TD(ipz, ipx, ipr);
                 dtx = dtx + TD(ipz + 1, ipx + 1, ipr) - TD(ipz + 1, ipx, ipr);
                 dtx = dtx + TD(ipz + 1, ipx + 1, ipr + 1) - TD(ipz + 1, ipx, ipr + 1);
                 dtx = dtx + TD(ipz, ipx + 1, ipr + 1) - TD(ipz, ipx, ipr + 1);
-                dtx = dtx / (4.0 * rcell * g.dnx);
-                const double sx = sin(rgx);
-                double dtz = TD(ipz + 1, ipx, ipr) - TD(ipz, ipx, ipr);
+                dtx = dtx / ((G)4 * rcell * (G)g.dnx);
+                const G sx = sin((G)rgx);
+                G dtz = TD(ipz + 1, ipx, ipr) - TD(ipz, ipx, ipr);
                 dtz = dtz + TD(ipz + 1, ipx + 1, ipr + 1) - TD(ipz, ipx + 1, ipr + 1);
                 dtz = dtz + TD(ipz + 1, ipx + 1, ipr) - TD(ipz, ipx + 1, ipr);
                 dtz = dtz + TD(ipz + 1, ipx, ipr + 1) - TD(ipz, ipx, ipr + 1);
-                dtz = dtz / (4.0 * rcell * sx * g.dnz);
-                const double crad = g.earth + rgr;
-                const double rd1 = sqrt(dtr * dtr + dtx * dtx + dtz * dtz);
-                double nr = rgr + dpl * dtr / rd1;
-                double nx = rgx - dpl * dtx / (crad * rd1);
-                double nz = rgz - dpl * dtz / (crad * sx * rd1);
+                dtz = dtz / ((G)4 * rcell * sx * (G)g.dnz);
+                const G crad = (G)(g.earth + rgr);
+                const G rd1 = sqrt(dtr * dtr + dtx * dtx + dtz * dtz);
+                double nr = rgr + (double)((G)dpl * dtr / rd1);
+                double nx = rgx - (double)((G)dpl * dtx / (crad * rd1));
+                double nz = rgz - (double)((G)dpl * dtz / (crad * sx * rd1));
                 const int ipro = ipr, ipxo = ipx, ipzo = ipz;
-                ipr = (int)floor((g.rgor - nr) / g.dnr) + 1;
-                ipx = (int)floor((nx - g.rgox) / g.dnx) + 1;
-                ipz = (int)floor((nz - g.rgoz) / g.dnz) + 1;
+                ipr = cellr(nr);
+                ipx = cellx(nx);
+                ipz = cellz(nz);
                 const bool swr = (ipr < 1 || ipr >= g.nnr);
                 const bool swx = (ipx < 1 || ipx >= g.nnx);
                 const bool swz = (ipz < 1 || ipz >= g.nnz);
@@ -200,12 +217,12 @@ __global__ void __launch_bounds__(kRayBlock) rays_kernel(RayArgs a)
                     stop = true;
                 }
                 if (fdm) {
-                    const int ivr = (int)floor((g.gor - nr) / g.dvr) + 1;
-                    const int ivx = (int)floor((nx - g.gox) / g.dvx) + 1;
-                    const int ivz = (int)floor((nz - g.goz) / g.dvz) + 1;
-                    const int ivro = (int)floor((g.gor - rgr) / g.dvr) + 1;
-                    const int ivxo = (int)floor((rgx - g.gox) / g.dvx) + 1;
-                    const int ivzo = (int)floor((rgz - g.goz) / g.dvz) + 1;
+                    const int ivr = vcellr(nr);
+                    const int ivx = vcellx(nx);
+                    const int ivz = vcellz(nz);
+                    const int ivro = vcellr(rgr);
+                    const int ivxo = vcellx(rgx);
+                    const int ivzo = vcellz(rgz);
                     double vrat[4];
                     int chp[4];
                     int nhp = 0;
@@ -265,9 +282,9 @@ __global__ void __launch_bounds__(kRayBlock) rays_kernel(RayArgs a)
                         const double rigz = rgz + vrat[k] * (nz - rgz);
                         const double rigx = rgx + vrat[k] * (nx - rgx);
                         const double rigr = rgr + vrat[k] * (nr - rgr);
-                        const int iprt = (int)floor((g.rgor - rigr) / g.dnr) + 1;
-                        const int ipxt = (int)floor((rigx - g.rgox) / g.dnx) + 1;
-                        const int ipzt = (int)floor((rigz - g.rgoz) / g.dnz) + 1;
+                        const int iprt = cellr(rigr);
+                        const int ipxt = cellx(rigx);
+                        const int ipzt = cellz(rigz);
                         drr = (g.rgor - rigr) - (double)(iprt - 1) * g.dnr;
                         drx = (rigx - g.rgox) - (double)(ipxt - 1) * g.dnx;
                         drz = (rigz - g.rgoz) - (double)(ipzt - 1) * g.dnz;
