@@ -333,6 +333,11 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #ifndef FM_TIE_SKIP
 #define FM_TIE_SKIP 1
 #endif
+//   FM_TIES_FIRST          in a two-part solve the other events' main sweep waits
+//                          for the near-tie events' one
+#ifndef FM_TIES_FIRST
+#define FM_TIES_FIRST 1
+#endif
 #ifndef FM_FRESH_SWEEP
 #define FM_FRESH_SWEEP 1
 #endif
@@ -888,10 +893,17 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         CK(cudaStreamWaitEvent(s2, fork, 0));
         if (FM_OVERLAP_MAIN) {
             // each part's main sweep: the near-tie events' on stream2 ahead of
-            // their extra sweeps, the others' on the context stream
+            // their extra sweeps, the others' on the context stream -- after
+            // the near-tie events' (FM_TIES_FIRST), which then has the GPU to
+            // itself and starts the longer chain sooner, the others' main
+            // sweep filling the gaps of its extra sweeps
             int rc = stream_pass((int)ties.size(), ctx->d_events, 0, ctx->tie_segments, nullptr, ctx->d_list[0],
                                  ctx->d_count[0], s2, FM_FRESH_SWEEP, true);
             if (rc) return rc;
+            if (FM_TIES_FIRST) {
+                CK(cudaEventRecord(pe[0], s2));
+                CK(cudaStreamWaitEvent(s, pe[0], 0));
+            }
             rc = stream_pass((int)others.size(), ctx->d_events_b, 0, ctx->sweep_segments, nullptr, ctx->d_list[0],
                              ctx->d_count[0], s, FM_FRESH_SWEEP, true);
             if (rc) return rc;

@@ -143,6 +143,27 @@ __global__ void __launch_bounds__(128) stream_activity_kernel(StreamArgs<R> a)
     }
 }
 
+// A tracked sweep goes straight to the next step that can change a node
+// (seating its ring anew) when at least this many quiet steps lie before it.
+constexpr int kStreamJump = 4;
+
+// One field element into shared memory by an asynchronous copy (L1-cached:
+// the layers an item reads are written in other launches, or by the item
+// itself); cp_async_wait_all waits for this thread's copies.
+template <typename R>
+__device__ __forceinline__ void cp_async_elem(R *smem, const R *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    if (sizeof(R) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 // FRESH: the main sweep of a solve, from an unset field (every node except
 // the fixed bottom layer unset).  Each node above the bottom layer then sees
 // its downstream neighbours (up, and the lateral ones the sweep runs toward)
@@ -258,6 +279,40 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
             // chunk that can change)
             if (!FRESH && a.act_cur &&
                 !__any_sync(0xffffffffu, colv && rp >= lo && rp < hi && ((s_active >> ((rp - lo) >> a.act_shift)) & 1u))) {
+                // A quiet step.  The first step from here with a node in a
+                // chunk that can change (at step t the lanes hold layers
+                // lo + t - (SX + SZ - 2) .. lo + t); none: the item is done.
+                // The steps between change nothing and so wake no chunk: far
+                // enough ahead, go there directly, the ring seated anew by
+                // asynchronous copies (one wait for all of them).
+                const int r0 = max(0, step - (SX + SZ - 2));
+                const int c0 = r0 >> a.act_shift;
+                const unsigned m = c0 < 32 ? s_active & (~0u << c0) : 0u;
+                if (!m) break;
+                const int t = max((__ffs(m) - 1) << a.act_shift, r0);
+                if (t - step >= kStreamJump && t < steps) {
+                    __syncwarp();
+                    for (int r = max(lo - 2, lo + t - (SX + SZ)); r <= lo + t + 2; ++r) {
+                        const bool rin = r >= 0 && r < f.nnr;
+                        const R *src = Te + (size_t)(f.nnr - 1 - (rin ? r : 0)) * lstride;
+                        R *dst = ring + ((r + RING) & (RING - 1)) * LAYER;
+#pragma unroll
+                        for (int k = 0; k < PER; ++k) {
+                            const int q = lane + 32 * k;
+                            if (q < LAYER) {
+                                if (rin && loff[k] >= 0)
+                                    cp_async_elem(dst + q, src + loff[k]);
+                                else
+                                    dst[q] = INF;
+                            }
+                        }
+                    }
+                    cp_async_wait_all();
+                    fetch_layer(lo + t + 3);
+                    const int rq = lo + t - xs - zs;
+                    if (colv && rq >= lo && rq < hi) pnext = TL::params_global(f, f.nnr - 1 - rq, gx, gz);
+                    step = t - 1;
+                }
                 __syncwarp();
                 continue;
             }
