@@ -336,7 +336,7 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 //   FM_TIES_FIRST          in a two-part solve the other events' main sweep waits
 //                          for the near-tie events' one
 #ifndef FM_TIES_FIRST
-#define FM_TIES_FIRST 1
+#define FM_TIES_FIRST 0
 #endif
 #ifndef FM_FRESH_SWEEP
 #define FM_FRESH_SWEEP 1
