@@ -171,20 +171,21 @@ def measured_peak_hbm():
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per node of
 # each single-precision solver kernel, from ncu captures of smaller cases of
 # the same kernels: a first round with every tile staged (96^3, 64 events)
-# and a full mid-sweep launch of a main sweep in four height segments (128^3,
-# 64 events); the bench scales it to its own launches by the nodes they
-# process.
-KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.15, "stream_sweep_kernel": 30.6}
+# and a full mid-sweep launch of a main sweep (the upstream-only form) in four
+# height segments (128^3, 64 events: 118.1 MB over 3.87 M nodes); the bench
+# scales it to its own launches by the nodes they process.
+KERNEL_DRAM_BYTES_PER_NODE = {"round_kernel": 4.15, "stream_sweep_kernel": 30.5}
 
 # Warp instructions per node of the same kernels, from ncu's
-# smsp__inst_executed.sum summed over every launch of three solves: per node
-# swept on the 128^3 grid with sweeps in two height segments (16 events; the
-# 128^3 x 256 workload's main sweeps use two),
-# and per node staged by the rounds on the 96^3 case (64 events: first
-# rounds after certification and tail rounds together).  The kernels are
-# bound by instruction issue, so the bench also reports the issue rate they
-# reach against the SMs' peak of four warp instructions per cycle.
-KERNEL_WARP_INST_PER_NODE = {"round_kernel": 41.6, "stream_sweep_kernel": 20.15}
+# smsp__inst_executed.sum: for the sweep, the same mid-sweep launch of a main
+# sweep (58.9 M over 3.87 M nodes; the sweep interval the roofline line times
+# holds the main sweeps and the re-sweeps, and the main sweeps are most of
+# it), and per node staged by the rounds on the 96^3 case (64 events: first
+# rounds after certification and tail rounds together, summed over every
+# launch of three solves).  The kernels are bound by instruction issue, so
+# the bench also reports the issue rate they reach against the SMs' peak of
+# four warp instructions per cycle.
+KERNEL_WARP_INST_PER_NODE = {"round_kernel": 41.6, "stream_sweep_kernel": 15.2}
 
 
 def workload_config(cfg, step, h, nev, nrc, prec):
@@ -477,6 +478,7 @@ def run_ours(a):
     trace_ms = [round(float(x), 4) for x in solver.round_trace_ms()]
     part_ms = [round(float(x), 3) for x in solver.part_ms()]
     tie_run, tie_skip = solver.tie_sweep_items()
+    tie_ms = [round(float(x), 3) for x in solver.tie_sweep_ms()]
     clk = clocks.stop() if clocks else None
     dev_ms = sum(s["ms"] for s in sts)
     step_s = wall if forward else max(wall, dev_ms / 1000.0)
@@ -612,7 +614,8 @@ def run_ours(a):
                    "round_trace_tiles": trace_tiles, "round_trace_updates": trace_updates,
                    "round_trace_ms": trace_ms,
                    "first_round_parts_ms": dict(zip(("tie_sweeps", "tie_round", "certify", "other_round"), part_ms)),
-                   "tie_sweep_items": {"run": [int(x) for x in tie_run], "skipped": [int(x) for x in tie_skip]}},
+                   "tie_sweep_items": {"run": [int(x) for x in tie_run], "skipped": [int(x) for x in tie_skip],
+                                       "ms": tie_ms}},
     }
     line.update(extras)
     if clk:

@@ -270,6 +270,10 @@ int fm3dt_part_ms(fm3dt_ctx *ctx, float *ms);
  * the number of extra sweeps recorded (0 when none tracked activity). */
 int fm3dt_tie_sweep_items(fm3dt_ctx *ctx, int cap, int64_t *run, int64_t *skipped);
 
+/* Device time (ms) of each near-tie extra sweep of the last solve when it ran
+ * in two parts (up to cap of them); returns their number (0 otherwise). */
+int fm3dt_tie_sweep_ms(fm3dt_ctx *ctx, int cap, float *ms);
+
 /* Number of available tile shapes and the shape (TR, TX, TZ) of one. */
 int fm3dt_tile_shapes(int *count);
 int fm3dt_tile_shape(int index, int *tr, int *tx, int *tz);

@@ -554,6 +554,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     auto act_prev = [&](int k) -> const unsigned * { return tie_act && k > 0 ? ctx->d_act[(k - 1) & 1] : nullptr; };
     auto act_items = [&](int k) { return tie_act && k < fm3dt_ctx::kMaxTieSweeps ? ctx->d_act_items + 2 * k : nullptr; };
     ctx->act_sweeps = 0;
+    ctx->tie_sweep_n = 0;
     if (do_sweep && streaming) {
         // streaming sweep: one launch per column-block hyperplane
         // the events whose lateral direction is a near tie get two more
@@ -913,7 +914,12 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         }
         if (tie_queue) CK(cudaMemsetAsync(ctx->d_count_b, 0, sizeof(int), s2));
         CK(cudaEventRecord(pe[0], s2));
+        // the extra sweeps' own times (events between them on stream2)
+        const int nts = std::min(ctx->tie_sweeps, fm3dt_ctx::kMaxTieSweeps);
+        std::vector<cudaEvent_t> tse(nts + 1);
+        for (auto &e : tse) CK(cudaEventCreate(&e));
         for (int k = 0; k < ctx->tie_sweeps; ++k) {
+            if (k <= nts) CK(cudaEventRecord(tse[k], s2));
             // (height segments by the time model for the near-tie events alone:
             // their sweeps are the longer chain of the two parts); the last one
             // queues their first round's tiles on list b
@@ -924,6 +930,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                                        act_cur(k), act_prev(k), act_items(k));
             if (rc) return rc;
         }
+        if (ctx->tie_sweeps <= nts) CK(cudaEventRecord(tse[nts], s2));
         if (!tie_queue)
             launch_initial_tiles((int)ties.size(), ctx->d_events, tpe, first, cnt, ctx->d_list_b, ctx->d_count_b,
                                  ctx->d_flag, s2);
@@ -976,6 +983,9 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         cudaEventElapsedTime(&ctx->part_ms[1], pe[1], pe[2]);
         cudaEventElapsedTime(&ctx->part_ms[2], pe[3], pe[4]);
         cudaEventElapsedTime(&ctx->part_ms[3], pe[4], pe[5]);
+        for (int k = 0; k < nts; ++k) cudaEventElapsedTime(&ctx->tie_sweep_ms[k], tse[k], tse[k + 1]);
+        ctx->tie_sweep_n = nts;
+        for (auto &e : tse) cudaEventDestroy(e);
         for (auto &e : pe) cudaEventDestroy(e);
         cudaEventDestroy(fork);
         cudaEventDestroy(join);
@@ -1717,6 +1727,13 @@ int fm3dt_tie_sweep_items(fm3dt_ctx *ctx, int cap, int64_t *run, int64_t *skippe
         if (skipped) skipped[i] = (int64_t)ctx->h_act_items[2 * i + 1];
     }
     return ctx->act_sweeps;
+}
+
+int fm3dt_tie_sweep_ms(fm3dt_ctx *ctx, int cap, float *ms)
+{
+    if (!ctx || cap < 0) return FM3DT_EINVAL;
+    for (int i = 0; i < std::min(cap, ctx->tie_sweep_n) && ms; ++i) ms[i] = ctx->tie_sweep_ms[i];
+    return ctx->tie_sweep_n;
 }
 
 int fm3dt_part_ms(fm3dt_ctx *ctx, float *ms)

@@ -336,6 +336,8 @@ struct fm3dt_ctx {
     unsigned long long *d_act_items = nullptr;   // [2 * kMaxTieSweeps]
     unsigned long long h_act_items[2 * kMaxTieSweeps] = {};
     int act_sweeps = 0;
+    float tie_sweep_ms[kMaxTieSweeps] = {};      // device time of each (two-part solves)
+    int tie_sweep_n = 0;
     // TMA tensor maps of the field, by round tile shape (encoded on first use)
     int *d_err = nullptr;         // raised by a kernel whose bounded wait gave up
     bool tmap_ok[fm3dt::kNumShapes] = {};

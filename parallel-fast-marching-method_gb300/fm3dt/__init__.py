@@ -57,7 +57,7 @@ EXPORTS = [
     "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_resume",
     "fm3dt_solve_planewave", "fm3dt_solve_point",
     "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_receiver_times_device", "fm3dt_rays_frechet_device", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
-    "fm3dt_set_tuning", "fm3dt_set_schedule", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_round_trace_ms", "fm3dt_part_ms", "fm3dt_tie_sweep_items", "fm3dt_tile_shapes", "fm3dt_tile_shape",
+    "fm3dt_set_tuning", "fm3dt_set_schedule", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_round_trace_ms", "fm3dt_part_ms", "fm3dt_tie_sweep_items", "fm3dt_tie_sweep_ms", "fm3dt_tile_shapes", "fm3dt_tile_shape",
     "fm3dt_launch_count",
     "fm3dt_last_error", "fm3dt_ctx_destroy",
 ]
@@ -100,6 +100,7 @@ def load(path: str | None = None):
     L.fm3dt_round_trace_ms.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     L.fm3dt_part_ms.argtypes = [vp, C.POINTER(C.c_float)]
     L.fm3dt_tie_sweep_items.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.fm3dt_tie_sweep_ms.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     L.fm3dt_tile_shapes.argtypes = [C.POINTER(C.c_int)]
     L.fm3dt_tile_shape.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.fm3dt_launch_count.argtypes = [vp]
@@ -266,6 +267,15 @@ class Solver:
             self._check(n)
         n = min(n, cap)
         return run[:n], skip[:n]
+
+    def tie_sweep_ms(self, cap: int = 16):
+        """Device time (ms) of each near-tie extra sweep of the last solve
+        (two-part solves)."""
+        m = np.zeros(cap, dtype=np.float32)
+        n = self._L.fm3dt_tie_sweep_ms(self._ctx, cap, m.ctypes.data_as(C.POINTER(C.c_float)))
+        if n < 0:
+            self._check(n)
+        return m[:min(n, cap)].astype(np.float64)
 
     def set_velocity(self, velv):
         velv = np.ascontiguousarray(velv, dtype=np.float64)
