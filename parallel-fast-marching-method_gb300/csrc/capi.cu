@@ -338,6 +338,12 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #ifndef FM_TIES_FIRST
 #define FM_TIES_FIRST 0
 #endif
+//   FM_SWEEP_FLOW          a streaming sweep pass as one launch whose items start
+//                          when their upstream neighbours are done (instead of
+//                          one launch per hyperplane)
+#ifndef FM_SWEEP_FLOW
+#define FM_SWEEP_FLOW 1
+#endif
 #ifndef FM_FRESH_SWEEP
 #define FM_FRESH_SWEEP 1
 #endif
@@ -428,9 +434,9 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     const int nbz = (g.nnz + kStreamShapes[sidx].sz - 1) / kStreamShapes[sidx].sz;
     // resident one-warp CTAs of the streaming sweep (the main sweep's form and
     // the general form differ in registers)
-    auto stream_grid = [&](bool fresh) {
-        return streaming ? std::max(1, ctx->prec == FM3DT_FP64 ? occupancy_stream_f64(sidx, fresh)
-                                                               : occupancy_stream_f32(sidx, fresh)) * sm_count()
+    auto stream_grid = [&](bool fresh, bool flow = false) {
+        return streaming ? std::max(1, ctx->prec == FM3DT_FP64 ? occupancy_stream_f64(sidx, fresh, flow)
+                                                               : occupancy_stream_f32(sidx, fresh, flow)) * sm_count()
                          : 1;
     };
     // One streaming sweep of nitems events (events == null: all), lateral
@@ -455,14 +461,47 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         const int seg_len = (g.nnr + nseg - 1) / nseg;
         // (items of one layer or column would miss a 2-deep neighbour)
         const bool track = !fresh && act_cur && seg_len >= 2 && kStreamShapes[sidx].sx >= 2;
-        // the pass's launches, one per hyperplane (two with a tracked previous sweep)
-        const int nlaunch = (int)P.off.size() * (track && act_prev ? 2 : 1);
-        auto enqueue = [&]() {
-            for (size_t h = 0; h < P.off.size(); ++h) {
+        // One launch for the whole pass (FM_SWEEP_FLOW): items start as their
+        // upstream neighbours finish, with a done flag per item and a queue
+        // counter of the pass's stream, both zeroed ahead of the launch.  For
+        // the tracked sweeps after a chain's first, whose few active items
+        // would leave most of each hyperplane's launch idle; passes that run
+        // every item keep one launch per hyperplane, which shares the GPU with
+        // the other stream's work (a one-launch pass holds every SM slot).
+        const bool flow = FM_SWEEP_FLOW && streaming && track && act_prev != nullptr;
+        const int nblocks = P.off.empty() ? 0 : P.off.back() + P.cnt.back();
+        const size_t done_n = (size_t)nitems * (size_t)((g.nnr + seg_len - 1) / seg_len) * (size_t)nbx * (size_t)nbz;
+        const int si = st == ctx->stream2 ? 1 : 0;
+        if (flow && done_n * sizeof(unsigned) > ctx->done_bytes[si]) {
+            CK(cudaStreamSynchronize(st));
+            cudaFree(ctx->d_done[si]);
+            ctx->d_done[si] = nullptr;
+            ctx->done_bytes[si] = 0;
+            CK(cudaMalloc(&ctx->d_done[si], done_n * sizeof(unsigned)));
+            ctx->done_bytes[si] = done_n * sizeof(unsigned);
+        }
+        const int fgrid = flow ? (int)std::min<long long>((long long)nblocks * nitems, stream_grid(fresh, true)) : 0;
+        // the pass's launches: one (flow), else one per hyperplane (two with a
+        // tracked previous sweep)
+        const int nlaunch = flow ? 1 : (int)P.off.size() * (track && act_prev ? 2 : 1);
+        // (returns the first error of the flags' and counter's zeroing; the
+        // launches' errors surface at the next check)
+        auto enqueue = [&]() -> cudaError_t {
+            cudaError_t ez = cudaSuccess;
+            if (flow) {
+                ez = cudaMemsetAsync(ctx->d_done[si], 0, done_n * sizeof(unsigned), st);
+                if (ez == cudaSuccess) ez = cudaMemsetAsync(ctx->d_next + si, 0, sizeof(unsigned), st);
+                if (ez != cudaSuccess) return ez;
+            }
+            for (size_t h = 0; h < (flow ? (size_t)1 : P.off.size()); ++h) {
                 const long long items = (long long)P.cnt[h] * nitems;
-                const int grid = (int)std::min<long long>(items, sgrid);
+                const int grid = flow ? fgrid : (int)std::min<long long>(items, sgrid);
                 auto fill = [&](auto &a) {
-                    a.hp_blocks = P.d_tiles; a.hoff = P.off[h]; a.hcount = P.cnt[h];
+                    a.hp_blocks = P.d_tiles; a.hoff = flow ? 0 : P.off[h]; a.hcount = flow ? nblocks : P.cnt[h];
+                    a.flow = flow ? 1 : 0;
+                    a.done = flow ? ctx->d_done[si] : nullptr;
+                    a.done_n = flow ? done_n : 0;
+                    a.next = flow ? ctx->d_next + si : nullptr;
                     a.dir = ctx->d_dir; a.nev = nitems; a.nbx = nbx; a.nbz = nbz;
                     a.events = events;
                     a.flip = flip;
@@ -474,7 +513,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                     a.ntr = ntr; a.ntx = ntx; a.ntz = ntz; a.tiles_per_event = tpe;
                     a.act_cur = track ? act_cur : nullptr;
                     a.act_prev = track ? act_prev : nullptr;
-                    a.act_run = track ? ctx->d_act[2] : nullptr;
+                    a.act_run = track && !flow ? ctx->d_act[2] : nullptr;
                     // chunks of at least 4 layers, at most 32 of them per item
                     a.act_shift = 2;
                     while (((seg_len - 1) >> a.act_shift) >= 32) ++a.act_shift;
@@ -494,6 +533,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                     launch_stream_f32(sidx, grid, a, st);
                 }
             }
+            return cudaSuccess;
         };
         // Passes that recur from solve to solve (the main sweeps and the
         // near-tie events' extra sweeps; not the re-sweeps, whose event count
@@ -505,7 +545,8 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                                                          nseg, fresh ? 1 : 0, (long long)(intptr_t)st, ctx->shape,
                                                          (long long)(intptr_t)flag, (long long)(intptr_t)list,
                                                          (long long)(intptr_t)count, (long long)(intptr_t)act_cur,
-                                                         (long long)(intptr_t)act_prev, (long long)(intptr_t)act_items};
+                                                         (long long)(intptr_t)act_prev, (long long)(intptr_t)act_items,
+                                                         (long long)(intptr_t)(flow ? ctx->d_done[si] : nullptr)};
             cudaGraphExec_t exec = nullptr;
             for (const auto &sg : ctx->sweep_graphs)
                 if (memcmp(sg.key, key, sizeof key) == 0) exec = sg.exec;
@@ -513,8 +554,9 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                 cudaGraph_t gr = nullptr;
                 cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
                 if (e == cudaSuccess) {
-                    enqueue();
+                    const cudaError_t eq = enqueue();
                     e = cudaStreamEndCapture(st, &gr);
+                    if (e == cudaSuccess) e = eq;
                 }
                 if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, gr, 0);
                 if (gr) cudaGraphDestroy(gr);
@@ -539,7 +581,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
                 launched = true;
             }
         }
-        if (!launched) enqueue();
+        if (!launched) CK(enqueue());
         sweep_launches += nlaunch;
         ctx->launches += nlaunch;
         return FM3DT_OK;
@@ -1042,6 +1084,8 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
     }
     if (kerr == 2) return fail(ctx, FM3DT_ECUDA, "a tile copy (TMA) destination was not 128-byte aligned");
     if (kerr & 4) return fail(ctx, FM3DT_ECUDA, "a tracked sweep met an activity slot out of range");
+    if (kerr & 16)
+        return fail(ctx, FM3DT_ECUDA, "a one-launch sweep pass gave up waiting for an item's upstream neighbours");
     if (kerr) return fail(ctx, FM3DT_ECUDA, "a tile copy (TMA) did not complete in time");
     if (!done) return fail(ctx, FM3DT_ENOCONV, "solver round limit reached before convergence");
     return FM3DT_OK;
@@ -1176,6 +1220,7 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMalloc(&ctx->d_count_b, sizeof(int)));
     CKC(cudaMalloc(&ctx->d_list_c, ctx->flag_capacity * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_act_items, 2 * fm3dt_ctx::kMaxTieSweeps * sizeof(unsigned long long)));
+    CKC(cudaMalloc(&ctx->d_next, 2 * sizeof(unsigned)));
     CKC(cudaMalloc(&ctx->d_count_c, sizeof(int)));
     CKC(cudaMalloc(&ctx->d_err, sizeof(int)));
     {
@@ -1793,6 +1838,8 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_count_b);
     cudaFree(ctx->d_list_c);
     cudaFree(ctx->d_act_items);
+    cudaFree(ctx->d_next);
+    for (auto p : ctx->d_done) cudaFree(p);
     cudaFree(ctx->d_count_c);
     for (auto p : ctx->d_act) cudaFree(p);
     cudaFree(ctx->d_err);

@@ -132,12 +132,21 @@ struct StreamArgs {
     // with tracking and a previous sweep (or null): [0] items that ran,
     // [1] items skipped
     unsigned long long *act_items;
+    // one launch for the whole pass (flow): items taken in order from the
+    // counter *next (zero at the start), hp_blocks holding every hyperplane's
+    // blocks in order (hcount: all of them, hoff 0); an item starts when the
+    // done flags (zero at the start, done_n of them, same slots as the
+    // activity masks) of its three upstream neighbours are set
+    int flow;
+    unsigned *done;
+    size_t done_n;
+    unsigned *next;
 };
 
 void launch_stream_f32(int idx, int grid, const StreamArgs<float> &a, cudaStream_t st);
 void launch_stream_f64(int idx, int grid, const StreamArgs<double> &a, cudaStream_t st);
-int occupancy_stream_f32(int idx, bool fresh);
-int occupancy_stream_f64(int idx, bool fresh);
+int occupancy_stream_f32(int idx, bool fresh, bool flow = false);
+int occupancy_stream_f64(int idx, bool fresh, bool flow = false);
 
 // After a single sweep from an unset field: mark the nodes a recomputation
 // could change (certification bitmap) and queue their tiles (kCert).
@@ -334,6 +343,11 @@ struct fm3dt_ctx {
     // items run / skipped by each of the last solve's near-tie extra sweeps
     static constexpr int kMaxTieSweeps = 16;
     unsigned long long *d_act_items = nullptr;   // [2 * kMaxTieSweeps]
+    // one-launch sweep passes: done flags and queue counters, per stream
+    // (context stream, stream2), the flags grown on demand
+    unsigned *d_done[2] = {nullptr, nullptr};
+    size_t done_bytes[2] = {0, 0};
+    unsigned *d_next = nullptr;                  // [2]
     unsigned long long h_act_items[2 * kMaxTieSweeps] = {};
     int act_sweeps = 0;
     float tie_sweep_ms[kMaxTieSweeps] = {};      // device time of each (two-part solves)
@@ -350,8 +364,9 @@ struct fm3dt_ctx {
     std::string err;
     // sweep passes captured as graphs, keyed by precision, sweep shape, event
     // count, event list, flip, height segments, form, stream, tile shape,
-    // (flag mode) the flags and queue it writes and the activity it tracks
-    static constexpr int kSweepKey = 15;
+    // (flag mode) the flags and queue it writes, the activity it tracks and
+    // (one-launch passes) its done flags
+    static constexpr int kSweepKey = 16;
     static constexpr size_t kSweepGraphs = 24;
     struct SweepGraph { long long key[kSweepKey]; cudaGraphExec_t exec; };
     std::vector<SweepGraph> sweep_graphs;

@@ -55,10 +55,10 @@ void launch_stream_f64(int idx, int grid, const StreamArgs<double> &a, cudaStrea
 #undef C_
 }
 
-int occupancy_stream_f64(int idx, bool fresh)
+int occupancy_stream_f64(int idx, bool fresh, bool flow)
 {
     int r = 0;
-#define C_(X, Z) r = StreamKernels<double, X, Z>::occ(fresh)
+#define C_(X, Z) r = StreamKernels<double, X, Z>::occ(fresh, flow)
     FM_STREAM_SWITCH(idx, C_)
 #undef C_
     return r;

@@ -79,6 +79,53 @@ __device__ void stream_mark(const StreamArgs<R> &a, int e, int gr, int gx, int g
 // above and below meet this one in their (and its) two edge layers.  A
 // skipped item's changed chunks are 0.  Items run and skipped are added to
 // act_items; a slot beyond the act_n masks is not accessed (bit 2 of *err).
+// One of the ten activity masks an item's chunks depend on (which = 0: the
+// item, previous sweep; 1 / 2: the items below / above, previous sweep; 3-6:
+// the lateral neighbours, previous sweep; 7: the item below, this sweep; 8 /
+// 9: the upstream neighbours along theta / phi, this sweep); 0 outside the
+// grid of items.  (bx, bz): the item's block in grid order; (sx, sz): the
+// sweep's directions.
+template <typename R>
+__device__ __forceinline__ unsigned stream_mask_read(const StreamArgs<R> &a, int which, int k, int nsegs, int seg,
+                                                     int bx, int bz, bool sx, bool sz)
+{
+    int s_ = seg, x_ = bx, z_ = bz;
+    switch (which) {
+        case 1: case 7: s_ = seg - 1; break;
+        case 2: s_ = seg + 1; break;
+        case 3: x_ = bx - 1; break;
+        case 4: x_ = bx + 1; break;
+        case 5: z_ = bz - 1; break;
+        case 6: z_ = bz + 1; break;
+        case 8: x_ = bx + (sx ? -1 : 1); break;
+        case 9: z_ = bz + (sz ? -1 : 1); break;
+        default: break;
+    }
+    if (s_ < 0 || s_ >= nsegs || x_ < 0 || x_ >= a.nbx || z_ < 0 || z_ >= a.nbz) return 0u;
+    const size_t q = ((size_t)(k * nsegs + s_) * a.nbx + x_) * a.nbz + z_;
+    if (q >= a.act_n) {
+        atomicOr(a.err, 4);
+        return 0u;
+    }
+    return __ldcg((which >= 7 ? a.act_cur : a.act_prev) + q);
+}
+
+// The chunks of an item that run, from its ten masks m[] (see
+// stream_mask_read); seg_len: layers per segment, nlay: this item's layers.
+__device__ __forceinline__ unsigned stream_mask_combine(const unsigned *m, int seg_len, int nlay, int sh)
+{
+    auto spread = [](unsigned v) { return v | (v << 1) | (v >> 1); };
+    unsigned run = spread(m[0] | m[3] | m[4] | m[5] | m[6] | m[8] | m[9]);
+    // the item below: its top two layers, next to this item's bottom chunk
+    const unsigned below_top2 = (1u << ((seg_len - 1) >> sh)) | (1u << ((seg_len - 2) >> sh));
+    if ((m[1] | m[7]) & below_top2) run |= 1u;
+    // the item above: its bottom chunk, next to this item's top two layers
+    if (m[2] & 1u) run |= (1u << ((nlay - 1) >> sh)) | (nlay >= 2 ? 1u << ((nlay - 2) >> sh) : 0u);
+    const int nch = ((nlay - 1) >> sh) + 1;
+    if (nch < 32) run &= (1u << nch) - 1u;
+    return run;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(128) stream_activity_kernel(StreamArgs<R> a)
 {
@@ -99,30 +146,11 @@ __global__ void __launch_bounds__(128) stream_activity_kernel(StreamArgs<R> a)
         const bool sx = dir & 1, sz = (dir >> 1) & 1;
         const int bx = sx ? bxp : a.nbx - 1 - bxp, bz = sz ? bzp : a.nbz - 1 - bzp;
         const int lo = seg * a.seg_len, nlay = min(a.f.nnr, lo + a.seg_len) - lo;
-        auto slot = [&](int s_, int x_, int z_) { return ((size_t)(k * nsegs + s_) * a.nbx + x_) * a.nbz + z_; };
-        auto mask = [&](const unsigned *src, int s_, int x_, int z_) -> unsigned {
-            if (s_ < 0 || s_ >= nsegs || x_ < 0 || x_ >= a.nbx || z_ < 0 || z_ >= a.nbz) return 0u;
-            const size_t q = slot(s_, x_, z_);
-            if (q >= a.act_n) {
-                atomicOr(a.err, 4);
-                return 0u;
-            }
-            return __ldcg(src + q);
-        };
-        auto spread = [](unsigned m) { return m | (m << 1) | (m >> 1); };
-        const unsigned *prev = a.act_prev, *cur = a.act_cur;
-        unsigned run = spread(mask(prev, seg, bx, bz) | mask(prev, seg, bx - 1, bz) | mask(prev, seg, bx + 1, bz) |
-                              mask(prev, seg, bx, bz - 1) | mask(prev, seg, bx, bz + 1) |
-                              mask(cur, seg, bx + (sx ? -1 : 1), bz) | mask(cur, seg, bx, bz + (sz ? -1 : 1)));
-        // the item below: its top two layers, next to this item's bottom chunk
-        const unsigned below_top2 = (1u << ((a.seg_len - 1) >> sh)) | (1u << ((a.seg_len - 2) >> sh));
-        if ((mask(prev, seg - 1, bx, bz) | mask(cur, seg - 1, bx, bz)) & below_top2) run |= 1u;
-        // the item above: its bottom chunk, next to this item's top two layers
-        if (mask(prev, seg + 1, bx, bz) & 1u)
-            run |= (1u << ((nlay - 1) >> sh)) | (nlay >= 2 ? 1u << ((nlay - 2) >> sh) : 0u);
-        const int nch = ((nlay - 1) >> sh) + 1;
-        if (nch < 32) run &= (1u << nch) - 1u;
-        const size_t self = slot(seg, bx, bz);
+        unsigned m[10];
+#pragma unroll
+        for (int w = 0; w < 10; ++w) m[w] = stream_mask_read(a, w, k, nsegs, seg, bx, bz, sx, sz);
+        const unsigned run = stream_mask_combine(m, a.seg_len, nlay, sh);
+        const size_t self = ((size_t)(k * nsegs + seg) * a.nbx + bx) * a.nbz + bz;
         if (self < a.act_n) {
             a.act_run[self] = run;
             if (!run) a.act_cur[self] = 0;
@@ -141,6 +169,29 @@ __global__ void __launch_bounds__(128) stream_activity_kernel(StreamArgs<R> a)
             atomicAdd(&a.act_items[1], (unsigned long long)nskip);
         }
     }
+}
+
+// Bounded wait of the one-launch (FLOW) form of a sweep for an upstream
+// item's done flag: past this many polls (each an L2 round trip and a
+// ~64 ns sleep: about a second in all) the error flag is raised and the item
+// goes on.
+constexpr unsigned kFlowSpins = 1u << 20;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_volatile_i32(const int *p)
+{
+    int v;
+    asm volatile("ld.volatile.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
 // A tracked sweep goes straight to the next step that can change a node
@@ -175,8 +226,8 @@ __device__ __forceinline__ void cp_async_wait_all()
 // column; the upstream form leaves it out, as a sweep from an unset field
 // would, and the rounds reach the same fixed point either way.)  The bottom
 // layer keeps fm_update: fixed boundary nodes beside an unset one are set.
-template <typename R, int SX, int SZ, bool FRESH>
-__global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
+template <typename R, int SX, int SZ, bool FRESH, bool FLOW>
+__device__ __forceinline__ void stream_sweep_body(const StreamArgs<R> &a)
 {
     static_assert(SX * SZ == 32, "one warp per column block");
     constexpr int LX = SX + 4, LZ = SZ + 4, LAYER = LX * LZ;
@@ -187,6 +238,11 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
     // chunks whose nodes can change (see stream_activity_kernel)
     __shared__ size_t s_aslot;
     __shared__ unsigned s_changed, s_active;
+    // FLOW: the item taken from the pass's queue; the activity masks read by
+    // lanes 0-9
+    __shared__ long long s_item;
+    __shared__ size_t s_slot;
+    __shared__ unsigned s_m[10];
     using TL = Tile<R, 1, SX, SZ>;
     const FieldArgs<R> &f = a.f;
     const int lane = threadIdx.x;
@@ -194,11 +250,28 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
     const R INF = Lim<R>::inf();
     const size_t N = (size_t)f.nnx * f.nnz * (size_t)f.nnr;
     const long long count = (long long)a.hcount * a.nev;
-    for (long long item = blockIdx.x; item < count; item += gridDim.x) {
-        const int k = (int)(item / a.hcount);
-        const int j = (int)(item - (long long)k * a.hcount);
+    for (long long it = blockIdx.x;; it += gridDim.x) {
+        // FLOW: one launch per pass; items in the order of their hyperplanes
+        // (block-major, then event), each taken from the queue and started
+        // when its three upstream neighbours are done
+        long long item = it;
+        if (FLOW) {
+            if (lane == 0) s_item = (long long)atomicAdd(a.next, 1u);
+            __syncwarp();
+            item = s_item;
+            __syncwarp();
+        }
+        if (item >= count) break;
+        int k, packed;
+        if (FLOW) {
+            const long long fb = item / a.nev;
+            k = (int)(item - fb * a.nev);
+            packed = a.hp_blocks[fb];
+        } else {
+            k = (int)(item / a.hcount);
+            packed = a.hp_blocks[a.hoff + (int)(item - (long long)k * a.hcount)];
+        }
         const int e = a.events ? a.events[k] : k;
-        const int packed = a.hp_blocks[a.hoff + j];
         const int seg = packed >> 24, bxp = (packed >> 12) & 0xfff, bzp = packed & 0xfff;
         int dir = a.dir[e];
         if (a.flip & 4) dir ^= ((dir >> 2) & 1) | (((dir >> 3) & 1) << 1);
@@ -213,14 +286,62 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
         const int gx = x0 + lx, gz = z0 + lz;
         const bool colv = gx < f.nnx && gz < f.nnz;
         R *Te = f.T + (size_t)e * N;
-        // activity: this item's slot, and the chunks that run
+        // the item's slot (event ordinal, segment, column block in grid
+        // order) in the activity masks and the done flags
+        const int nsegs = (f.nnr + a.seg_len - 1) / a.seg_len;
+        const size_t slot = ((size_t)(k * nsegs + seg) * a.nbx + x0 / SX) * a.nbz + z0 / SZ;
+        if (FLOW) {
+            // (kept in shared memory for the item's end)
+            __syncwarp();
+            if (lane == 0) s_slot = slot;
+            // lanes 0-2: the items below, and before this one along theta
+            // and phi, done (a bounded wait: past the limit the error flag
+            // is raised and the item goes on)
+            if (lane < 3) {
+                const int s_ = seg - (lane == 0), xq = bxp - (lane == 1), zq = bzp - (lane == 2);
+                if (s_ >= 0 && xq >= 0 && zq >= 0) {
+                    const int bxq = sx ? xq : a.nbx - 1 - xq, bzq = sz ? zq : a.nbz - 1 - zq;
+                    const size_t q = ((size_t)(k * nsegs + s_) * a.nbx + bxq) * a.nbz + bzq;
+                    if (q < a.done_n) {
+                        // (once any wait of the launch has given up, the
+                        // others do too)
+                        unsigned spins = 0;
+                        while (ld_acquire_u32(a.done + q) == 0u) {
+                            if (++spins > kFlowSpins || ((spins & 63u) == 0u && (ld_volatile_i32(a.err) & 16))) {
+                                atomicOr(a.err, 16);
+                                break;
+                            }
+                            __nanosleep(64);
+                        }
+                    } else {
+                        atomicOr(a.err, 16);
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        {
+        // activity: the chunks that run
         if (!FRESH && a.act_cur) {
-            const int nsegs = (f.nnr + a.seg_len - 1) / a.seg_len;
-            const int bx = x0 / SX, bz = z0 / SZ;
-            const size_t aslot = ((size_t)(k * nsegs + seg) * a.nbx + bx) * a.nbz + bz;
-            // (stream_activity_kernel wrote the chunks that run)
-            const unsigned run = a.act_prev ? (aslot < a.act_n ? __ldcg(a.act_run + aslot) : 0u) : ~0u;
-            if (!run) continue;
+            const size_t aslot = slot;
+            unsigned run = ~0u;
+            if (a.act_prev) {
+                if (FLOW) {
+                    // from the neighbours' masks, as stream_activity_kernel
+                    // computes it for a launch of a hyperplane
+                    if (lane < 10) s_m[lane] = stream_mask_read(a, lane, k, nsegs, seg, x0 / SX, z0 / SZ, sx, sz);
+                    __syncwarp();
+                    run = stream_mask_combine(s_m, a.seg_len, hi - lo, a.act_shift);
+                    if (lane == 0) {
+                        if (!run && aslot < a.act_n) a.act_cur[aslot] = 0;
+                        if (a.act_items) atomicAdd(a.act_items + (run ? 0 : 1), 1ull);
+                    }
+                } else {
+                    // (stream_activity_kernel wrote the chunks that run)
+                    run = aslot < a.act_n ? __ldcg(a.act_run + aslot) : 0u;
+                }
+            }
+            if (!run) goto item_done;
             __syncwarp();
             if (lane == 0) {
                 s_aslot = aslot;
@@ -293,6 +414,13 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
                 if (t - step >= kStreamJump && t < steps) {
                     __syncwarp();
                     for (int r = max(lo - 2, lo + t - (SX + SZ)); r <= lo + t + 2; ++r) {
+                        if (FLOW) {
+                            // (other CTAs of this launch wrote these layers:
+                            // loads from L2, not a possibly older L1 line)
+                            fetch_layer(r);
+                            store_layer(r);
+                            continue;
+                        }
                         const bool rin = r >= 0 && r < f.nnr;
                         const R *src = Te + (size_t)(f.nnr - 1 - (rin ? r : 0)) * lstride;
                         R *dst = ring + ((r + RING) & (RING - 1)) * LAYER;
@@ -307,7 +435,7 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
                             }
                         }
                     }
-                    cp_async_wait_all();
+                    if (!FLOW) cp_async_wait_all();
                     fetch_layer(lo + t + 3);
                     const int rq = lo + t - xs - zs;
                     if (colv && rq >= lo && rq < hi) pnext = TL::params_global(f, f.nnr - 1 - rq, gx, gz);
@@ -363,14 +491,53 @@ __global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
             __syncwarp();
         }
         if (!FRESH && a.act_cur && lane == 0 && s_aslot < a.act_n) a.act_cur[s_aslot] = s_changed;
+        }
+    item_done:
+        if (FLOW) {
+            // the item's writes (field, masks, queued tiles) before its flag
+            __threadfence();
+            __syncwarp();
+            if (lane == 0) {
+                const size_t q = s_slot;
+                if (q < a.done_n)
+                    st_release_u32(a.done + q, 1u);
+                else
+                    atomicOr(a.err, 16);
+            }
+        }
     }
+}
 
+// The per-hyperplane form (one launch per hyperplane of a pass) and the
+// one-launch form, each with its own register budget: the one-launch form
+// holds its items' queue state, and is bounded to the resident CTAs of the
+// per-hyperplane form's main sweep.
+template <typename R> struct FlowBlocks { static constexpr int value = 20; };
+template <> struct FlowBlocks<double> { static constexpr int value = 12; };
+
+template <typename R, int SX, int SZ, bool FRESH>
+__global__ void __launch_bounds__(32) stream_sweep_kernel(StreamArgs<R> a)
+{
+    stream_sweep_body<R, SX, SZ, FRESH, false>(a);
+}
+
+template <typename R, int SX, int SZ, bool FRESH>
+__global__ void __launch_bounds__(32, FlowBlocks<R>::value) stream_flow_kernel(StreamArgs<R> a)
+{
+    stream_sweep_body<R, SX, SZ, FRESH, true>(a);
 }
 
 template <typename R, int SX, int SZ>
 struct StreamKernels {
     static void sweep(int grid, const StreamArgs<R> &a, cudaStream_t st)
     {
+        if (a.flow) {
+            if (a.fresh)
+                stream_flow_kernel<R, SX, SZ, true><<<grid, 32, 0, st>>>(a);
+            else
+                stream_flow_kernel<R, SX, SZ, false><<<grid, 32, 0, st>>>(a);
+            return;
+        }
         if (!a.fresh && a.act_cur && a.act_prev) {
             const long long items = (long long)a.hcount * a.nev;
             const int blocks = (int)std::min<long long>((items + 127) / 128, 4096);
@@ -381,13 +548,19 @@ struct StreamKernels {
         else
             stream_sweep_kernel<R, SX, SZ, false><<<grid, 32, 0, st>>>(a);
     }
-    static int occ(bool fresh)
+    static int occ(bool fresh, bool flow)
     {
         int nb = 0;
-        if (fresh)
+        if (flow) {
+            if (fresh)
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stream_flow_kernel<R, SX, SZ, true>, 32, 0);
+            else
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stream_flow_kernel<R, SX, SZ, false>, 32, 0);
+        } else if (fresh) {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stream_sweep_kernel<R, SX, SZ, true>, 32, 0);
-        else
+        } else {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stream_sweep_kernel<R, SX, SZ, false>, 32, 0);
+        }
         return nb;
     }
 };

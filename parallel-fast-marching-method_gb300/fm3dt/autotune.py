@@ -22,7 +22,7 @@ from . import sweep_shapes, tile_shapes
 
 PASS_CAPS = (16, 64)
 # (extra sweeps of the near-tie events, near-tie band)
-SCHEDULES = ((2, 0.1), (3, 0.15), (4, 0.15), (5, 0.15), (5, 0.2), (6, 0.2), (8, 0.2))
+SCHEDULES = ((2, 0.1), (3, 0.15), (4, 0.15), (5, 0.15), (5, 0.2), (6, 0.2), (8, 0.2), (10, 0.2))
 # height segments of the near-tie events' sweeps (0: the solver's time model)
 TIE_SEGMENTS = (0, 4, 8)
 

@@ -22,7 +22,10 @@ DRIVER_DIR = os.path.join(ROOT, "driver")
 DRIVER = os.path.join(ROOT, "fm3dt_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# (a function that can end without its return value is an error: the host
+# compiler may otherwise treat that end as unreachable)
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Werror=return-type",
+          "--expt-relaxed-constexpr"]
 SOURCES = {
     "model.cu": ["-fmad=false"],
     "boundary.cu": ["-fmad=false"],
