@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -830,16 +831,18 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         ctx->launches += 1;
     };
     // events that still change on many tiles after a round are swept again
-    // (see resweeps_left; `left` counts down): `list`/`count` is the list the
-    // next round takes, `queued` its length, `ev_buf` a device array for the
-    // swept events' indices that no other stream reads meanwhile
-    auto maybe_resweep = [&](int *list, int *count, int queued, int *ev_buf, int &left) -> int {
+    // (see resweeps_left; `left` counts down), on stream st: `list`/`count`
+    // is the list the next round takes, `queued` its length, `ev_buf` a
+    // device array for the swept events' indices that no other stream reads
+    // meanwhile; the list's new length goes to the pinned *h_cnt
+    auto maybe_resweep = [&](cudaStream_t st, int *h_cnt, int *list, int *count, int queued, int *ev_buf,
+                             int &left) -> int {
         if (left <= 0) return FM3DT_OK;
         --left;
         if (!((double)queued > ctx->resweep_frac * (double)nev * (double)tpe)) return FM3DT_OK;
         std::vector<int> lst(queued);
-        CK(cudaMemcpyAsync(lst.data(), list, (size_t)queued * sizeof(int), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
+        CK(cudaMemcpyAsync(lst.data(), list, (size_t)queued * sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
         std::vector<int> per(nev, 0);
         for (int w : lst) per[w / tpe] += 1;
         std::vector<int> busy;
@@ -849,15 +852,15 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         cudaEvent_t r0, r1;
         CK(cudaEventCreate(&r0));
         CK(cudaEventCreate(&r1));
-        CK(cudaMemcpyAsync(ev_buf, busy.data(), busy.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-        CK(cudaEventRecord(r0, s));
-        const int rc = stream_pass((int)busy.size(), ev_buf, 0, 0, ctx->d_flag, list, count, s, false, false);
+        CK(cudaMemcpyAsync(ev_buf, busy.data(), busy.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaEventRecord(r0, st));
+        const int rc = stream_pass((int)busy.size(), ev_buf, 0, 0, ctx->d_flag, list, count, st, false, false);
         if (rc) return rc;
         interval_nodes += (int64_t)busy.size() * (int64_t)ctx->N;
-        CK(cudaEventRecord(r1, s));
+        CK(cudaEventRecord(r1, st));
         CKL();
-        CK(cudaMemcpyAsync(ctx->h_count, count, sizeof(int), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
+        CK(cudaMemcpyAsync(h_cnt, count, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
         float m = 0.0f;
         cudaEventElapsedTime(&m, r0, r1);
         resweep_ms += m;
@@ -865,49 +868,104 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         cudaEventDestroy(r1);
         return FM3DT_OK;
     };
-    // Rounds on the context stream until the list they take comes back empty
-    // (part_done) or the round cap: list[cur] is the list the next round
-    // takes, whose length is in *ctx->h_count when `known`.
+    // A part's rounds, a chunk at a time, so that two parts (on two streams)
+    // can alternate: L.list[L.cur] is the list its next round takes; ev_buf
+    // and left for its re-sweeps; h_cnt the pinned copy of its list's length;
+    // ev its round events (2 per round of a chunk); ready recorded after the
+    // chunk's length is read back.
     struct RoundLists { int *list[2]; int *count[2]; int cur; };
-    auto converge = [&](RoundLists &L, bool known, int *ev_buf, int &left, bool &part_done) -> int {
-        if (known && *ctx->h_count == 0) part_done = true;
-        while (!part_done && rounds < max_rounds) {
-            int k;
-            const int first_round = rounds;
-            const int chunk_now = left > 0 ? 1 : chunk;
-            while ((int)ctx->round_events.size() < 2 * chunk) {
-                cudaEvent_t e;
-                CK(cudaEventCreate(&e));
-                ctx->round_events.push_back(e);
+    struct Part {
+        cudaStream_t st;
+        RoundLists L;
+        int *ev_buf;
+        int left;
+        int *h_cnt;
+        std::vector<cudaEvent_t> *ev;
+        cudaEvent_t ready;
+        bool pending, done;
+        int first, n;
+    };
+    auto part_launch = [&](Part &p) -> int {
+        const int chunk_now = p.left > 0 ? 1 : chunk;
+        while ((int)p.ev->size() < 2 * chunk) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            p.ev->push_back(e);
+        }
+        p.first = rounds;
+        for (int k = 0; k < chunk_now && rounds < max_rounds; ++k, ++rounds) {
+            const int cur = p.L.cur, nxt = cur ^ 1;
+            CK(cudaMemsetAsync(p.L.count[nxt], 0, sizeof(int), p.st));
+            CK(cudaEventRecord((*p.ev)[2 * k], p.st));
+            // the first round's tile count is known on the host: one CTA per
+            // tile, so blocks free up as they finish
+            if (rounds == 0 && FM_ROUND0_PER_TILE && !verified && mode != kPoint && !certify_alone && !tie_queue)
+                grid_override = (int)std::min<long long>((long long)nev * cnt, 1LL << 30);
+            launch_round(rounds, p.L.list[cur], p.L.count[cur], p.L.list[nxt], p.L.count[nxt], p.st);
+            grid_override = 0;
+            CK(cudaEventRecord((*p.ev)[2 * k + 1], p.st));
+            p.L.cur = nxt;
+        }
+        p.n = rounds - p.first;
+        CKL();
+        CK(cudaMemcpyAsync(p.h_cnt, p.L.count[p.L.cur], sizeof(int), cudaMemcpyDeviceToHost, p.st));
+        CK(cudaEventRecord(p.ready, p.st));
+        p.pending = true;
+        return FM3DT_OK;
+    };
+    // (after the part's ready event) the chunk's times, re-sweeps, and the end
+    auto part_finish = [&](Part &p) -> int {
+        for (int q = 0; q < p.n; ++q) {
+            float m = 0.0f;
+            cudaEventElapsedTime(&m, (*p.ev)[2 * q], (*p.ev)[2 * q + 1]);
+            round_ms += m;
+            if ((int)ctx->round_ms_trace.size() < fm3dt_ctx::kTraceRounds) ctx->round_ms_trace.push_back(m);
+        }
+        p.pending = false;
+        const int rc = maybe_resweep(p.st, p.h_cnt, p.L.list[p.L.cur], p.L.count[p.L.cur], *p.h_cnt, p.ev_buf, p.left);
+        if (rc) return rc;
+        if (*p.h_cnt == 0) p.done = true;
+        return FM3DT_OK;
+    };
+    // Rounds of one or two parts until their lists come back empty or the
+    // round cap; two parts alternate, each chunk launched as soon as its
+    // part's previous one has been read back.
+    auto converge = [&](Part *parts, int np) -> int {
+        for (;;) {
+            bool open = false, progressed = false;
+            for (int i = 0; i < np; ++i) {
+                Part &p = parts[i];
+                if (p.done) continue;
+                if (p.pending) {
+                    const cudaError_t q = np > 1 ? cudaEventQuery(p.ready) : cudaEventSynchronize(p.ready);
+                    if (q == cudaErrorNotReady) {
+                        open = true;
+                        continue;
+                    }
+                    CK(q);
+                    const int rc = part_finish(p);
+                    if (rc) return rc;
+                    progressed = true;
+                }
+                if (!p.done && rounds < max_rounds) {
+                    const int rc = part_launch(p);
+                    if (rc) return rc;
+                    progressed = true;
+                }
+                if (p.pending) open = true;
             }
-            for (k = 0; k < chunk_now && rounds < max_rounds; ++k, ++rounds) {
-                const int cur = L.cur, nxt = cur ^ 1;
-                CK(cudaMemsetAsync(L.count[nxt], 0, sizeof(int), s));
-                CK(cudaEventRecord(ctx->round_events[2 * k], s));
-                // the first round's tile count is known on the host: one CTA per
-                // tile, so blocks free up as they finish
-                if (rounds == 0 && FM_ROUND0_PER_TILE && !verified && mode != kPoint && !certify_alone && !tie_queue)
-                    grid_override = (int)std::min<long long>((long long)nev * cnt, 1LL << 30);
-                launch_round(rounds, L.list[cur], L.count[cur], L.list[nxt], L.count[nxt], s);
-                grid_override = 0;
-                CK(cudaEventRecord(ctx->round_events[2 * k + 1], s));
-                L.cur = nxt;
-            }
-            CKL();
-            CK(cudaMemcpyAsync(ctx->h_count, L.count[L.cur], sizeof(int), cudaMemcpyDeviceToHost, s));
-            CK(cudaStreamSynchronize(s));
-            for (int q = 0; q < rounds - first_round; ++q) {
-                float m = 0.0f;
-                cudaEventElapsedTime(&m, ctx->round_events[2 * q], ctx->round_events[2 * q + 1]);
-                round_ms += m;
-                if ((int)ctx->round_ms_trace.size() < fm3dt_ctx::kTraceRounds) ctx->round_ms_trace.push_back(m);
-            }
-            const int rc = maybe_resweep(L.list[L.cur], L.count[L.cur], *ctx->h_count, ev_buf, left);
-            if (rc) return rc;
-            if (*ctx->h_count == 0) part_done = true;
+            if (!open) break;
+            if (!progressed) std::this_thread::yield();
         }
         return FM3DT_OK;
     };
+    cudaEvent_t ready_ev[2];
+    CK(cudaEventCreateWithFlags(&ready_ev[0], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ready_ev[1], cudaEventDisableTiming));
+    struct ReadyGuard {
+        cudaEvent_t *e;
+        ~ReadyGuard() { cudaEventDestroy(e[0]); cudaEventDestroy(e[1]); }
+    } ready_guard{ready_ev};
     if (overlap) {
         // The solve in two parts that run side by side and converge apart
         // (events do not interact).  On stream2, whose higher priority gets
@@ -1008,18 +1066,25 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         round_ms += m;
         ctx->round_ms_trace.push_back(m);
         rounds = 1;
-        // the other events' rounds (re-sweeps take their indices in events b,
-        // which stream2 does not read)
-        RoundLists Lo{{ctx->d_list[1], ctx->d_list[0]}, {ctx->d_count[1], ctx->d_count[0]}, 0};
-        int left_o = resweeps_left;
-        bool done_o = false;
-        int rc = maybe_resweep(Lo.list[0], Lo.count[0], *ctx->h_count, ctx->d_events_b, left_o);
+        // The two parts' further rounds, alternating: the other events' on
+        // the context stream (re-sweeps take their indices in events b, which
+        // stream2 does not read), the near-tie events' on stream2 after their
+        // chain (lists c and b; their first chunk is queued behind the chain
+        // at once).
+        Part parts[2] = {
+            {s, {{ctx->d_list[1], ctx->d_list[0]}, {ctx->d_count[1], ctx->d_count[0]}, 0}, ctx->d_events_b,
+             resweeps_left, ctx->h_count, &ctx->round_events, ready_ev[0], false, false, 0, 0},
+            {s2, {{ctx->d_list_c, ctx->d_list_b}, {ctx->d_count_c, ctx->d_count_b}, 0}, ctx->d_events,
+             resweeps_left, ctx->h_count + 1, &ctx->round_events_b, ready_ev[1], false, false, 0, 0}};
+        int rc = maybe_resweep(s, ctx->h_count, parts[0].L.list[0], parts[0].L.count[0], *ctx->h_count,
+                               ctx->d_events_b, parts[0].left);
         if (rc) return rc;
-        rc = converge(Lo, true, ctx->d_events_b, left_o, done_o);
+        if (*ctx->h_count == 0) parts[0].done = true;
+        rc = converge(parts, 2);
         if (rc) return rc;
-        // then the near-tie events' (their chain on stream2 has ended)
+        // (the context stream waits for stream2's last chunk)
+        CK(cudaEventRecord(join, s2));
         CK(cudaStreamWaitEvent(s, join, 0));
-        CK(cudaMemcpyAsync(ctx->h_count, ctx->d_count_c, sizeof(int), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         cudaEventElapsedTime(&ctx->part_ms[0], pe[0], pe[1]);
         cudaEventElapsedTime(&ctx->part_ms[1], pe[1], pe[2]);
@@ -1033,20 +1098,13 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         cudaEventDestroy(join);
         cudaEventDestroy(r0);
         cudaEventDestroy(r1);
-        RoundLists Lt{{ctx->d_list_c, ctx->d_list[0]}, {ctx->d_count_c, ctx->d_count[0]}, 0};
-        int left_t = resweeps_left;
-        bool done_t = false;
-        if (done_o) {
-            rc = maybe_resweep(Lt.list[0], Lt.count[0], *ctx->h_count, ctx->d_events, left_t);
-            if (rc) return rc;
-            rc = converge(Lt, true, ctx->d_events, left_t, done_t);
-            if (rc) return rc;
-        }
-        done = done_o && done_t;
+        done = parts[0].done && parts[1].done;
     } else {
-        RoundLists L{{ctx->d_list[0], ctx->d_list[1]}, {ctx->d_count[0], ctx->d_count[1]}, 0};
-        const int rc = converge(L, false, ctx->d_events, resweeps_left, done);
+        Part part{s, {{ctx->d_list[0], ctx->d_list[1]}, {ctx->d_count[0], ctx->d_count[1]}, 0}, ctx->d_events,
+                  resweeps_left, ctx->h_count, &ctx->round_events, ready_ev[0], false, false, 0, 0};
+        const int rc = converge(&part, 1);
         if (rc) return rc;
+        done = part.done;
     }
     CK(cudaEventRecord(ev1, s));
     CK(cudaMemcpyAsync(ctx->h_stats, ctx->d_stats, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
@@ -1212,7 +1270,7 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMalloc(&ctx->d_params, 4 * ctx->maxev * sizeof(double)));
     CKC(cudaMalloc(&ctx->d_box, 6 * ctx->maxev * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_box_init, 6 * ctx->maxev * sizeof(int)));
-    CKC(cudaMallocHost(&ctx->h_count, sizeof(int)));
+    CKC(cudaMallocHost(&ctx->h_count, 2 * sizeof(int)));
     CKC(cudaMallocHost(&ctx->h_dir, ctx->maxev * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_events, ctx->maxev * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_events_b, ctx->maxev * sizeof(int)));
@@ -1822,6 +1880,7 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (auto &sg : ctx->sweep_graphs) cudaGraphExecDestroy(sg.exec);
     for (auto e : ctx->round_events) cudaEventDestroy(e);
+    for (auto e : ctx->round_events_b) cudaEventDestroy(e);
     cudaFree(ctx->d_velv);
     cudaFree(ctx->d_veln);
     cudaFree(ctx->d_s);

@@ -299,7 +299,7 @@ struct fm3dt_ctx {
     int *d_count[2] = {nullptr, nullptr};
     unsigned long long *d_stats = nullptr;
     double *d_params = nullptr;
-    int *h_count = nullptr;       // pinned
+    int *h_count = nullptr;       // pinned [2]: the list lengths of a solve's (up to) two parts
     unsigned long long *h_stats = nullptr;  // pinned
     std::vector<double> h_base;
     double hr = 0.0;
@@ -372,6 +372,7 @@ struct fm3dt_ctx {
     std::vector<SweepGraph> sweep_graphs;
     bool sweep_graph_off = false;
     std::vector<cudaEvent_t> round_events;   // start/stop pairs of round kernels
+    std::vector<cudaEvent_t> round_events_b; // ... of a second part's rounds (stream2)
     std::vector<float> round_ms_trace;       // device time of each round of the last solve
     float part_ms[4] = {};                   // the first round's two parts (fm3dt_part_ms)
     // point sources: fixed node boxes, and the refined source grids' contexts
