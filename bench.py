@@ -555,13 +555,23 @@ def run_ours(a):
         h_cols = torch.empty(max(cap, 1), dtype=torch.int32).pin_memory() if forward else None
         h_vals = torch.empty(max(cap, 1), dtype=torch.float32).pin_memory() if forward else None
 
+        hphase = {"solve": [], "receivers": [], "rays": []}
+
         def step_host():
+            t0_ = time.perf_counter()
             solver.solve_ptr(nev, h_frames.data_ptr(), False)
+            t1_ = time.perf_counter()
             solver.receiver_times_into(rcr, rcx, rcz, h_out.data_ptr())
+            t2_ = time.perf_counter()
+            n = 0
             if forward:
-                return solver.rays_frechet_into(rcr, rcx, rcz, h_rowptr.data_ptr(), h_cols.data_ptr(),
-                                                h_vals.data_ptr(), cap)
-            return 0
+                n = solver.rays_frechet_into(rcr, rcx, rcz, h_rowptr.data_ptr(), h_cols.data_ptr(),
+                                             h_vals.data_ptr(), cap)
+            t3_ = time.perf_counter()
+            hphase["solve"].append(1000.0 * (t1_ - t0_))
+            hphase["receivers"].append(1000.0 * (t2_ - t1_))
+            hphase["rays"].append(1000.0 * (t3_ - t2_))
+            return n
 
         step_host()
         d.barrier()
@@ -570,6 +580,7 @@ def run_ours(a):
         for _ in range(a.steps):
             entries = step_host()
         e2e_s = d.max(time.perf_counter() - t0)
+        extras["e2e_ms_per_step"] = {k: statistics.median(v[1:]) for k, v in hphase.items() if len(v) > 1}
         extras["e2e"] = {"value": ws * nev * a.steps / e2e_s, "unit": "solves/s",
                          "h2d_bytes_per_step": int(frames.nbytes + (2 if forward else 1) * 3 * rcr.nbytes),
                          "d2h_bytes_per_step": int(h_out.numel() * 4 +

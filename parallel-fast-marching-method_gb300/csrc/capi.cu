@@ -345,6 +345,19 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #ifndef FM_SWEEP_FLOW
 #define FM_SWEEP_FLOW 1
 #endif
+//   FM_FLOW_FIRST          ... the first tracked sweep of a chain too
+#ifndef FM_FLOW_FIRST
+#define FM_FLOW_FIRST 1
+#endif
+//   FM_FLOW_SHARE_FIRST    percent of the resident slots a one-launch pass on stream2
+//   FM_FLOW_SHARE          takes: the chain's first tracked sweep (beside the other part's
+//                          certification), the later ones
+#ifndef FM_FLOW_SHARE_FIRST
+#define FM_FLOW_SHARE_FIRST 75
+#endif
+#ifndef FM_FLOW_SHARE
+#define FM_FLOW_SHARE 75
+#endif
 #ifndef FM_FRESH_SWEEP
 #define FM_FRESH_SWEEP 1
 #endif
@@ -469,7 +482,7 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         // would leave most of each hyperplane's launch idle; passes that run
         // every item keep one launch per hyperplane, which shares the GPU with
         // the other stream's work (a one-launch pass holds every SM slot).
-        const bool flow = FM_SWEEP_FLOW && streaming && track && act_prev != nullptr;
+        const bool flow = FM_SWEEP_FLOW && streaming && track && (act_prev != nullptr || FM_FLOW_FIRST);
         const int nblocks = P.off.empty() ? 0 : P.off.back() + P.cnt.back();
         const size_t done_n = (size_t)nitems * (size_t)((g.nnr + seg_len - 1) / seg_len) * (size_t)nbx * (size_t)nbz;
         const int si = st == ctx->stream2 ? 1 : 0;
@@ -481,7 +494,14 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             CK(cudaMalloc(&ctx->d_done[si], done_n * sizeof(unsigned)));
             ctx->done_bytes[si] = done_n * sizeof(unsigned);
         }
-        const int fgrid = flow ? (int)std::min<long long>((long long)nblocks * nitems, stream_grid(fresh, true)) : 0;
+        // (on stream2, beside the other part's work, a share of the resident
+        // slots: a one-launch pass holds its slots to the end)
+        const int fgrid = flow ? (int)std::min<long long>((long long)nblocks * nitems,
+                                                          std::max(1, stream_grid(fresh, true) *
+                                                                          (si ? (act_prev ? FM_FLOW_SHARE
+                                                                                          : FM_FLOW_SHARE_FIRST)
+                                                              : 100) / 100))
+                               : 0;
         // the pass's launches: one (flow), else one per hyperplane (two with a
         // tracked previous sweep)
         const int nlaunch = flow ? 1 : (int)P.off.size() * (track && act_prev ? 2 : 1);
