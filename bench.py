@@ -581,6 +581,9 @@ def run_ours(a):
             entries = step_host()
         e2e_s = d.max(time.perf_counter() - t0)
         extras["e2e_ms_per_step"] = {k: statistics.median(v[1:]) for k, v in hphase.items() if len(v) > 1}
+        if forward:
+            extras["e2e_ms_per_step"]["rays_parts"] = dict(zip(("trace", "compact", "copy_out", "wall"),
+                                                               [round(float(x), 3) for x in solver.rays_ms()]))
         extras["e2e"] = {"value": ws * nev * a.steps / e2e_s, "unit": "solves/s",
                          "h2d_bytes_per_step": int(frames.nbytes + (2 if forward else 1) * 3 * rcr.nbytes),
                          "d2h_bytes_per_step": int(h_out.numel() * 4 +

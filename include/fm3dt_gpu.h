@@ -89,10 +89,12 @@ typedef struct {
 typedef struct fm3dt_ctx fm3dt_ctx;
 
 /* Replaces F:6050-6191 (topology, input conversion, allocation).  Allocates
- * the device fields for desc->max_events events.  The scratch of the
- * context's later calls (the largest: fm3dt_rays_frechet's dense rows,
- * nev*nrc*(nvr+2)*(nvx+2)*(nvz+2)*4 bytes) comes from a memory pool of the
- * context that keeps its memory until fm3dt_ctx_destroy. */
+ * the device fields for desc->max_events events.  The context keeps the
+ * rays' dense rows (nev*nrc*(nvr+2)*(nvx+2)*(nvz+2)*4 bytes, from the first
+ * fm3dt_rays_frechet* call with rows, grown by a larger one) and the host
+ * entry point's compacted rows until fm3dt_ctx_destroy; the other scratch of
+ * its calls comes from a memory pool of the context that keeps its memory
+ * until then too. */
 int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out);
 
 /* Replaces F:6172 gridder (F:6989-7038): cubic B-spline interpolation of the
@@ -262,6 +264,11 @@ int fm3dt_round_trace_ms(fm3dt_ctx *ctx, int cap, float *ms);
  * round, ms[2] the other events' certification, ms[3] their first round;
  * zeros when the solve ran in one part. */
 int fm3dt_part_ms(fm3dt_ctx *ctx, float *ms);
+
+/* Times (ms) of the last fm3dt_rays_frechet call: ms[0] device time of the
+ * receivers' copy in, the rays and the row pointers; ms[1] of the rows'
+ * compaction; ms[2] of the copies out; ms[3] the call's wall time. */
+int fm3dt_rays_ms(fm3dt_ctx *ctx, float *ms);
 
 /* The last solve's near-tie extra sweeps after the first skip the work items
  * (a height segment of a block of columns of one event) where nothing near

@@ -5,6 +5,7 @@
 // loop, receiver times, rays and Frechet rows.  All device memory is owned by
 // the context; all work goes to the context's stream.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -349,6 +350,10 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #ifndef FM_FLOW_FIRST
 #define FM_FLOW_FIRST 1
 #endif
+//   FM_FLOW_TIE_MAIN       ... and the near-tie events' main sweep (stream2)
+#ifndef FM_FLOW_TIE_MAIN
+#define FM_FLOW_TIE_MAIN 0
+#endif
 //   FM_FLOW_SHARE_FIRST    percent of the resident slots a one-launch pass on stream2
 //   FM_FLOW_SHARE          takes: the chain's first tracked sweep (beside the other part's
 //                          certification), the later ones
@@ -482,10 +487,11 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         // would leave most of each hyperplane's launch idle; passes that run
         // every item keep one launch per hyperplane, which shares the GPU with
         // the other stream's work (a one-launch pass holds every SM slot).
-        const bool flow = FM_SWEEP_FLOW && streaming && track && (act_prev != nullptr || FM_FLOW_FIRST);
+        const int si = st == ctx->stream2 ? 1 : 0;
+        const bool flow = FM_SWEEP_FLOW && streaming &&
+                          ((track && (act_prev != nullptr || FM_FLOW_FIRST)) || (fresh && si == 1 && FM_FLOW_TIE_MAIN));
         const int nblocks = P.off.empty() ? 0 : P.off.back() + P.cnt.back();
         const size_t done_n = (size_t)nitems * (size_t)((g.nnr + seg_len - 1) / seg_len) * (size_t)nbx * (size_t)nbz;
-        const int si = st == ctx->stream2 ? 1 : 0;
         if (flow && done_n * sizeof(unsigned) > ctx->done_bytes[si]) {
             CK(cudaStreamSynchronize(st));
             cudaFree(ctx->d_done[si]);
@@ -1573,8 +1579,20 @@ static int rays_trace(fm3dt_ctx *ctx, DeviceScratch &sc, int nrc, const double *
     CK(sc.alloc(&d_flags, 2));
     CK(cudaMemsetAsync(d_flags, 0x7f, 2 * sizeof(int), s));     // 0x7f7f7f7f: no ray flagged
     if (want_rows) {
-        CK(sc.alloc(&d_fdm, (size_t)nrows * nmp));
-        CK(cudaMemsetAsync(d_fdm, 0, (size_t)nrows * nmp * sizeof(float), s));
+        // the dense rows: the context's own buffer, kept between calls (a
+        // pool allocation of this size was not always reused once smaller
+        // allocations had come and gone)
+        const size_t need = (size_t)nrows * nmp * sizeof(float);
+        if (need > ctx->dense_bytes) {
+            CK(cudaStreamSynchronize(s));
+            cudaFree(ctx->d_dense);
+            ctx->d_dense = nullptr;
+            ctx->dense_bytes = 0;
+            CK(cudaMalloc(&ctx->d_dense, need));
+            ctx->dense_bytes = need;
+        }
+        d_fdm = ctx->d_dense;
+        CK(cudaMemsetAsync(d_fdm, 0, need, s));
     }
     RayArgs ra;
     ra.g = g;
@@ -1653,6 +1671,14 @@ int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double 
     }
     const int nrows = ctx->nev_solved * nrc;
     cudaStream_t s = ctx->stream;
+    const auto h0 = std::chrono::steady_clock::now();
+    cudaEvent_t pev[4];
+    for (auto &e : pev) CK(cudaEventCreate(&e));
+    struct EvGuard {
+        cudaEvent_t *e;
+        ~EvGuard() { for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]); }
+    } ev_guard{pev};
+    CK(cudaEventRecord(pev[0], s));
     DeviceScratch sc(ctx);
     double *d_rec = nullptr, *d_end = nullptr;
     int64_t *d_rowptr = nullptr;
@@ -1666,6 +1692,8 @@ int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double 
     float *d_fdm = nullptr;
     rc = rays_trace(ctx, sc, nrc, d_rec, d_rec + nrc, d_rec + 2 * nrc, want_rows, d_end, d_rowptr, &total, &d_fdm);
     if (rc != FM3DT_OK) return rc;
+    CK(cudaEventRecord(pev[1], s));
+    CK(cudaEventRecord(pev[2], s));
     if (endpoints)
         CK(cudaMemcpyAsync(endpoints, d_end, 3 * (size_t)nrows * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (want_rows) {
@@ -1676,19 +1704,33 @@ int fm3dt_rays_frechet(fm3dt_ctx *ctx, int nrc, const double *rcr, const double 
                                                std::to_string(cap));
         }
         if (total > 0) {
-            int32_t *d_cols = nullptr;
-            float *d_vals = nullptr;
-            CK(sc.alloc(&d_cols, (size_t)total));
-            CK(sc.alloc(&d_vals, (size_t)total));
+            // (the compacted rows in the context's buffer, kept between calls)
+            const size_t need = (size_t)total * (sizeof(int32_t) + sizeof(float));
+            if (need > ctx->compact_bytes) {
+                CK(cudaStreamSynchronize(s));
+                cudaFree(ctx->d_compact);
+                ctx->d_compact = nullptr;
+                ctx->compact_bytes = 0;
+                CK(cudaMalloc(&ctx->d_compact, need));
+                ctx->compact_bytes = need;
+            }
+            int32_t *d_cols = (int32_t *)ctx->d_compact;
+            float *d_vals = (float *)((char *)ctx->d_compact + (size_t)total * sizeof(int32_t));
             rc = rays_compact(ctx, d_fdm, nrows, d_rowptr, d_cols, d_vals);
             if (rc != FM3DT_OK) return rc;
+            CK(cudaEventRecord(pev[2], s));
             CK(cudaMemcpyAsync(cols, d_cols, (size_t)total * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
             CK(cudaMemcpyAsync(vals, d_vals, (size_t)total * sizeof(float), cudaMemcpyDeviceToHost, s));
         }
     } else if (row_ptr) {
         for (int q = 0; q <= nrows; ++q) row_ptr[q] = 0;
     }
+    CK(cudaEventRecord(pev[3], s));
     CK(cudaStreamSynchronize(s));
+    cudaEventElapsedTime(&ctx->rays_ms[0], pev[0], pev[1]);
+    cudaEventElapsedTime(&ctx->rays_ms[1], pev[1], pev[2]);
+    cudaEventElapsedTime(&ctx->rays_ms[2], pev[2], pev[3]);
+    ctx->rays_ms[3] = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - h0).count();
     return FM3DT_OK;
 }
 
@@ -1859,6 +1901,13 @@ int fm3dt_tie_sweep_ms(fm3dt_ctx *ctx, int cap, float *ms)
     return ctx->tie_sweep_n;
 }
 
+int fm3dt_rays_ms(fm3dt_ctx *ctx, float *ms)
+{
+    if (!ctx || !ms) return FM3DT_EINVAL;
+    for (int i = 0; i < 4; ++i) ms[i] = ctx->rays_ms[i];
+    return FM3DT_OK;
+}
+
 int fm3dt_part_ms(fm3dt_ctx *ctx, float *ms)
 {
     if (!ctx || !ms) return FM3DT_EINVAL;
@@ -1919,6 +1968,8 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_act_items);
     cudaFree(ctx->d_next);
     for (auto p : ctx->d_done) cudaFree(p);
+    cudaFree(ctx->d_dense);
+    cudaFree(ctx->d_compact);
     cudaFree(ctx->d_count_c);
     for (auto p : ctx->d_act) cudaFree(p);
     cudaFree(ctx->d_err);

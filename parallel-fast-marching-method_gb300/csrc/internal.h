@@ -348,6 +348,11 @@ struct fm3dt_ctx {
     unsigned *d_done[2] = {nullptr, nullptr};
     size_t done_bytes[2] = {0, 0};
     unsigned *d_next = nullptr;                  // [2]
+    // the rays' dense rows and (host entry point) compacted rows, grown on demand
+    float *d_dense = nullptr;
+    size_t dense_bytes = 0;
+    void *d_compact = nullptr;
+    size_t compact_bytes = 0;
     unsigned long long h_act_items[2 * kMaxTieSweeps] = {};
     int act_sweeps = 0;
     float tie_sweep_ms[kMaxTieSweeps] = {};      // device time of each (two-part solves)
@@ -375,6 +380,7 @@ struct fm3dt_ctx {
     std::vector<cudaEvent_t> round_events_b; // ... of a second part's rounds (stream2)
     std::vector<float> round_ms_trace;       // device time of each round of the last solve
     float part_ms[4] = {};                   // the first round's two parts (fm3dt_part_ms)
+    float rays_ms[4] = {};                   // the last host-buffer ray call's phases (fm3dt_rays_ms)
     // point sources: fixed node boxes, and the refined source grids' contexts
     int *d_box = nullptr;         // [maxev][6] fixed nodes
     int *d_box_init = nullptr;    // [maxev][6] nodes whose tiles start active

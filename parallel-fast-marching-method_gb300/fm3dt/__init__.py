@@ -57,7 +57,7 @@ EXPORTS = [
     "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_resume",
     "fm3dt_solve_planewave", "fm3dt_solve_point",
     "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_receiver_times_device", "fm3dt_rays_frechet_device", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
-    "fm3dt_set_tuning", "fm3dt_set_schedule", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_round_trace_ms", "fm3dt_part_ms", "fm3dt_tie_sweep_items", "fm3dt_tie_sweep_ms", "fm3dt_tile_shapes", "fm3dt_tile_shape",
+    "fm3dt_set_tuning", "fm3dt_set_schedule", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_round_trace_ms", "fm3dt_part_ms", "fm3dt_rays_ms", "fm3dt_tie_sweep_items", "fm3dt_tie_sweep_ms", "fm3dt_tile_shapes", "fm3dt_tile_shape",
     "fm3dt_launch_count",
     "fm3dt_last_error", "fm3dt_ctx_destroy",
 ]
@@ -99,6 +99,7 @@ def load(path: str | None = None):
     L.fm3dt_round_trace.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.fm3dt_round_trace_ms.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     L.fm3dt_part_ms.argtypes = [vp, C.POINTER(C.c_float)]
+    L.fm3dt_rays_ms.argtypes = [vp, C.POINTER(C.c_float)]
     L.fm3dt_tie_sweep_items.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.fm3dt_tie_sweep_ms.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     L.fm3dt_tile_shapes.argtypes = [C.POINTER(C.c_int)]
@@ -276,6 +277,13 @@ class Solver:
         if n < 0:
             self._check(n)
         return m[:min(n, cap)].astype(np.float64)
+
+    def rays_ms(self):
+        """Times (ms) of the last host-buffer ray call: rays and row pointers,
+        compaction, copies out (device), and the call's wall time."""
+        m = np.zeros(4, dtype=np.float32)
+        self._check(self._L.fm3dt_rays_ms(self._ctx, m.ctypes.data_as(C.POINTER(C.c_float))))
+        return m.astype(np.float64)
 
     def set_velocity(self, velv):
         velv = np.ascontiguousarray(velv, dtype=np.float64)
