@@ -476,3 +476,41 @@ def test_schedule_does_not_change_the_field(gpu_lib, prec):
             with pytest.raises(fm3dt.Fm3dtError) as ei:
                 s.set_schedule(*bad)
             assert ei.value.code == fm3dt.EINVAL
+
+
+def test_solve_profile_is_reported(gpu_lib):
+    """The last solve's profile: a batch in two parts reports its first
+    round's parts, and one time and one item count (run + skipped = every item
+    of the sweep) per near-tie extra sweep after the first; a host-buffer ray
+    call reports its phases.  The chunk activity and the one-launch sweeps
+    leave the field as the schedule without extra sweeps gives it."""
+    import fm3dt
+    baz = np.concatenate([np.linspace(0.0, 352.5, 40), [0.4, 90.3, 179.6, 270.2]])
+    events = np.stack([np.linspace(32.0, 88.0, len(baz)), baz], axis=1)
+    w = _setup(3, 30, events=events)
+    params = _params(w)
+    n = len(params)
+    rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat, w.rec_lon)
+    rcr = np.asarray(w.rec_elev, dtype=np.float64)
+    with fm3dt.Solver(w.header, precision=fm3dt.FP32_OFFSET, max_events=n) as s:
+        s.set_velocity(w.velv)
+        s.set_schedule(0, 0.1, 0, 0.01)
+        assert s.solve_planewave(params)["converged"] == 1
+        ref = np.concatenate([s.get_times(e) for e in range(n)])
+        s.set_schedule(4, 0.1, -1, -1.0)
+        assert s.solve_planewave(params)["converged"] == 1
+        assert np.array_equal(np.concatenate([s.get_times(e) for e in range(n)]), ref)
+        parts = s.part_ms()
+        assert parts.shape == (4,) and parts[0] > 0.0 and parts[2] > 0.0
+        ms = s.tie_sweep_ms()
+        assert len(ms) == 4 and np.all(ms > 0.0)
+        assert sum(ms) <= parts[0] * 1.01 + 0.05
+        run, skipped = s.tie_sweep_items()
+        assert len(run) == 4 and run[0] == 0 and skipped[0] == 0
+        totals = run[1:] + skipped[1:]
+        assert np.all(totals == totals[0]) and totals[0] > 0
+        assert np.all(run[1:] <= totals)
+        rows = s.rays_frechet(rcr, rcx, rcz)
+        assert rows[0][-1] > 0
+        rm = s.rays_ms()
+        assert rm.shape == (4,) and np.all(rm >= 0.0) and rm[0] > 0.0 and rm[3] > 0.0
