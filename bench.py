@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--passes", type=int, default=0)
     ap.add_argument("--sweep-shape", type=int, default=-1, help="sweep tile shape index (-1: same as --shape)")
     ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline, FP64 checks and e2e leg")
+    ap.add_argument("--separate-calls", action="store_true",
+                    help="forward step as three calls (solve, receiver times, rays) instead of fm3dt_forward")
     ap.add_argument("--duration", type=float, default=30.0, help="config 4: seconds of Poisson arrivals")
     ap.add_argument("--sweep-mode", type=int, default=1,
                     help="with --shape: 1 sweep then rounds, 2 sweep + verifying sweep, 0 no sweep")
@@ -437,10 +439,19 @@ def run_ours(a):
         d_cols = torch.empty(cap, dtype=torch.int32, device="cuda")
         d_vals = torch.empty(cap, dtype=torch.float32, device="cuda")
 
-    phase = {"solve": [], "receivers": [], "rays": []}
+    phase = {"solve": [], "receivers": [], "rays": [], "forward": []}
+
+    fused = forward and not a.separate_calls
 
     def step_device():
         t0 = time.perf_counter()
+        if fused:
+            # one call: the solve with the rays of the part that converges
+            # first traced inside it, then the receivers and remaining rays
+            st, _ = solver.forward_device(nev, fptr, nrc, *rec_ptrs, d_times.data_ptr(), d_rowptr.data_ptr(),
+                                          d_cols.data_ptr(), d_vals.data_ptr(), cap)
+            phase["forward"].append(1000.0 * (time.perf_counter() - t0))
+            return st
         st = solver.solve_ptr(nev, fptr, True)
         t1 = time.perf_counter()
         if forward:
@@ -545,6 +556,8 @@ def run_ours(a):
     extras = {}
     if forward:
         extras["forward_ms_per_step"] = {k: statistics.median(v) for k, v in phase.items() if v}
+        if fused:
+            extras["forward_early_ray_events"] = solver.forward_early_events
         extras["frechet_entries_per_step"] = int(d_rowptr[-1].item())
     if not a.no_extras:
         # e2e through the host entry points with pinned host buffers: frames
@@ -555,10 +568,15 @@ def run_ours(a):
         h_cols = torch.empty(max(cap, 1), dtype=torch.int32).pin_memory() if forward else None
         h_vals = torch.empty(max(cap, 1), dtype=torch.float32).pin_memory() if forward else None
 
-        hphase = {"solve": [], "receivers": [], "rays": []}
+        hphase = {"solve": [], "receivers": [], "rays": [], "forward": []}
 
         def step_host():
             t0_ = time.perf_counter()
+            if fused:
+                n = solver.forward_into(nev, h_frames.data_ptr(), rcr, rcx, rcz, h_out.data_ptr(),
+                                        h_rowptr.data_ptr(), h_cols.data_ptr(), h_vals.data_ptr(), cap)
+                hphase["forward"].append(1000.0 * (time.perf_counter() - t0_))
+                return n
             solver.solve_ptr(nev, h_frames.data_ptr(), False)
             t1_ = time.perf_counter()
             solver.receiver_times_into(rcr, rcx, rcz, h_out.data_ptr())
@@ -581,7 +599,7 @@ def run_ours(a):
             entries = step_host()
         e2e_s = d.max(time.perf_counter() - t0)
         extras["e2e_ms_per_step"] = {k: statistics.median(v[1:]) for k, v in hphase.items() if len(v) > 1}
-        if forward:
+        if forward and not fused:
             extras["e2e_ms_per_step"]["rays_parts"] = dict(zip(("trace", "compact", "copy_out", "wall"),
                                                                [round(float(x), 3) for x in solver.rays_ms()]))
         extras["e2e"] = {"value": ws * nev * a.steps / e2e_s, "unit": "solves/s",

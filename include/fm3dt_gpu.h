@@ -205,6 +205,30 @@ int fm3dt_rays_frechet_device(fm3dt_ctx *ctx, int nrc, const double *d_rcr, cons
                               const double *d_rcz, int64_t *d_row_ptr, int32_t *d_cols, float *d_vals,
                               int64_t cap, int64_t *total, double *d_endpoints);
 
+/* One forward step of a batch, as the reference's per-source loop runs it
+ * (F:6273-6370: local_fmm, then srtimes F:7040-7248 and parallel_rpaths
+ * F:7250-7777 on the field): fm3dt_solve, fm3dt_receiver_times and
+ * fm3dt_rays_frechet in one call, with the same arguments, results and
+ * errors as those three called in turn.  In a batch solved in two parts
+ * (near-tie events and the others), the rays of the part that converges
+ * first are traced while the other part still solves.
+ * fm3dt_forward: host buffers (boundary frames, receivers in; times nev x nrc,
+ * rows and nullable endpoints out; cols = vals = NULL traces rays only).
+ * fm3dt_forward_device: every array a device pointer (d_boundary frames
+ * are copied into the context), *total on the host as in
+ * fm3dt_rays_frechet_device.  st is nullable.  Both return after the GPU work
+ * has finished. */
+int fm3dt_forward(fm3dt_ctx *ctx, int nev, const double *boundary, int nrc, const double *rcr,
+                  const double *rcx, const double *rcz, float *times, int64_t *row_ptr, int32_t *cols,
+                  float *vals, int64_t cap, double *endpoints, fm3dt_status *st);
+int fm3dt_forward_device(fm3dt_ctx *ctx, int nev, const double *d_boundary, int nrc, const double *d_rcr,
+                         const double *d_rcx, const double *d_rcz, float *d_times, int64_t *d_row_ptr,
+                         int32_t *d_cols, float *d_vals, int64_t cap, int64_t *total, double *d_endpoints,
+                         fm3dt_status *st);
+/* Events whose rays the last forward call traced inside its solve (0 when
+ * the batch was solved in one part). */
+int fm3dt_forward_early_events(const fm3dt_ctx *ctx);
+
 /* Copies the solved traveltime field of one event to the host: nnr*nnx*nnz
  * doubles, phi fastest (absolute seconds in both precisions; unreached nodes
  * are 0.0 like the reference's ttn). */

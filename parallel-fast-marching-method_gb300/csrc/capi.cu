@@ -391,6 +391,31 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 // point-source boxes the caller already wrote (rounds from the boxes' tiles).
 enum SolveMode { kFrames = 0, kResume = 1, kPoint = 2 };
 
+// The rays of nlist listed events (d_events; null: all nev events) from the
+// receivers, into the dense rows and end points of a forward call's plan.
+void launch_ray_list(fm3dt_ctx *ctx, int nev, const fm3dt_ctx::EarlyRays &er, const int *d_events, int nlist,
+                     cudaStream_t s)
+{
+    RayArgs ra{};
+    ra.g = ctx->g;
+    ra.prec = ctx->prec;
+    ra.T = ctx->d_T;
+    ra.veln = ctx->d_veln;
+    ra.nev = nev;
+    ra.nrc = er.nrc;
+    ra.events = d_events;
+    ra.nlist = nlist;
+    ra.rcr = er.rcr;
+    ra.rcx = er.rcx;
+    ra.rcz = er.rcz;
+    ra.fdm = er.fdm;
+    ra.endpoints = er.endpoints;
+    ra.nsteps = nullptr;
+    ra.flags = er.flags;
+    launch_rays(ra, s);
+    ctx->launches += 1;
+}
+
 int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
 {
     const bool resume = mode == kResume;
@@ -953,6 +978,19 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
         if (*p.h_cnt == 0) p.done = true;
         return FM3DT_OK;
     };
+    // A forward call's early rays: once the other events (part 0 of a
+    // two-part solve) have converged, their rays start on the context stream,
+    // which that part no longer uses, beside the near-tie events' rounds.
+    auto early_rays = [&]() -> int {
+        auto &er = ctx->early;
+        if (!er.on || !er.events.empty() || others.empty()) return FM3DT_OK;
+        er.events = others;
+        CK(cudaMemcpyAsync(er.d_events, others.data(), others.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        if (er.fdm) CK(cudaMemsetAsync(er.fdm, 0, er.fdm_bytes, s));
+        launch_ray_list(ctx, nev, er, er.d_events, (int)others.size(), s);
+        CKL();
+        return FM3DT_OK;
+    };
     // Rounds of one or two parts until their lists come back empty or the
     // round cap; two parts alternate, each chunk launched as soon as its
     // part's previous one has been read back.
@@ -961,6 +999,10 @@ int solve_common(fm3dt_ctx *ctx, int nev, fm3dt_status *st, int mode = kFrames)
             bool open = false, progressed = false;
             for (int i = 0; i < np; ++i) {
                 Part &p = parts[i];
+                if (p.done && i == 0 && np > 1) {
+                    const int rc = early_rays();
+                    if (rc) return rc;
+                }
                 if (p.done) continue;
                 if (p.pending) {
                     const cudaError_t q = np > 1 ? cudaEventQuery(p.ready) : cudaEventSynchronize(p.ready);
@@ -1305,6 +1347,7 @@ int fm3dt_ctx_create(const fm3dt_grid_desc *desc, fm3dt_ctx **out)
     CKC(cudaMalloc(&ctx->d_list_c, ctx->flag_capacity * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_act_items, 2 * fm3dt_ctx::kMaxTieSweeps * sizeof(unsigned long long)));
     CKC(cudaMalloc(&ctx->d_next, 2 * sizeof(unsigned)));
+    CKC(cudaMalloc(&ctx->d_ray_events, 2 * (size_t)ctx->maxev * sizeof(int)));
     CKC(cudaMalloc(&ctx->d_count_c, sizeof(int)));
     CKC(cudaMalloc(&ctx->d_err, sizeof(int)));
     {
@@ -1594,7 +1637,7 @@ static int rays_trace(fm3dt_ctx *ctx, DeviceScratch &sc, int nrc, const double *
         d_fdm = ctx->d_dense;
         CK(cudaMemsetAsync(d_fdm, 0, need, s));
     }
-    RayArgs ra;
+    RayArgs ra{};
     ra.g = g;
     ra.prec = ctx->prec;
     ra.T = ctx->d_T;
@@ -1765,6 +1808,198 @@ int fm3dt_rays_frechet_device(fm3dt_ctx *ctx, int nrc, const double *d_rcr, cons
     }
     CK(cudaStreamSynchronize(ctx->stream));
     return FM3DT_OK;
+}
+
+// The forward step of a batch whose boundary frames are in ctx->d_frames:
+// the solve, with the rays of the part that converges first traced inside
+// it (ctx->early), then the receiver times (d_times) and the remaining rays;
+// with rows, the row pointers on the device (d_row_ptr) and the entry count
+// in *total, the dense rows in *d_fdm_out for rays_compact.
+static int forward_common(fm3dt_ctx *ctx, DeviceScratch &sc, int nev, int nrc, const double *d_rcr,
+                          const double *d_rcx, const double *d_rcz, float *d_times, bool want_rows, double *d_end,
+                          int64_t *d_row_ptr, int64_t *total, float **d_fdm_out, fm3dt_status *st)
+{
+    const Geom &g = ctx->g;
+    const int nrows = nev * nrc;
+    const size_t nmp = (size_t)(g.nvr + 2) * (g.nvx + 2) * (g.nvz + 2);
+    cudaStream_t s = ctx->stream;
+    int *d_flags = nullptr;   // [0], [1] as RayArgs::flags; [2] the first receiver outside the grid
+    CK(sc.alloc(&d_flags, 3));
+    CK(cudaMemsetAsync(d_flags, 0x7f, 3 * sizeof(int), s));      // 0x7f7f7f7f: none
+    float *d_fdm = nullptr;
+    const size_t need = want_rows ? (size_t)nrows * nmp * sizeof(float) : 0;
+    if (need > ctx->dense_bytes) {
+        CK(cudaStreamSynchronize(s));
+        cudaFree(ctx->d_dense);
+        ctx->d_dense = nullptr;
+        ctx->dense_bytes = 0;
+        CK(cudaMalloc(&ctx->d_dense, need));
+        ctx->dense_bytes = need;
+    }
+    if (want_rows) d_fdm = ctx->d_dense;
+    auto &er = ctx->early;
+    er.nrc = nrc;
+    er.rcr = d_rcr;
+    er.rcx = d_rcx;
+    er.rcz = d_rcz;
+    er.fdm = d_fdm;
+    er.fdm_bytes = need;
+    er.endpoints = d_end;
+    er.flags = d_flags;
+    er.d_events = ctx->d_ray_events;
+    er.events.clear();
+    er.on = nrc > 0;
+    struct Off {
+        fm3dt_ctx::EarlyRays &e;
+        ~Off() { e.on = false; }
+    } off{er};
+    int rc = solve_common(ctx, nev, st);
+    er.on = false;
+    ctx->early_events = (int)er.events.size();
+    if (rc != FM3DT_OK) return rc;
+    *total = 0;
+    if (nrc == 0) return FM3DT_OK;
+    launch_receivers_located(g, ctx->prec, ctx->d_T, ctx->d_base, nev, nrc, d_rcr, d_rcx, d_rcz, d_flags + 2,
+                             d_times, s);
+    ctx->launches += 1;
+    // the rays of the events not traced inside the solve
+    if (er.events.empty()) {
+        if (d_fdm) CK(cudaMemsetAsync(d_fdm, 0, need, s));
+        launch_ray_list(ctx, nev, er, nullptr, 0, s);
+    } else if ((int)er.events.size() < nev) {
+        std::vector<char> early(nev, 0);
+        for (int e : er.events) early[e] = 1;
+        std::vector<int> rest;
+        for (int e = 0; e < nev; ++e)
+            if (!early[e]) rest.push_back(e);
+        int *d_rest = ctx->d_ray_events + ctx->maxev;
+        CK(cudaMemcpyAsync(d_rest, rest.data(), rest.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+        launch_ray_list(ctx, nev, er, d_rest, (int)rest.size(), s);
+    }
+    CKL();
+    if (want_rows) {
+        int64_t *d_counts = nullptr, *d_chunks = nullptr;
+        CK(sc.alloc(&d_counts, (size_t)nrows));
+        CK(sc.alloc(&d_chunks, (size_t)scan_chunks(nrows)));
+        launch_row_counts(d_fdm, nrows, (int)nmp, d_counts, s);
+        launch_row_scan(d_counts, nrows, d_row_ptr, d_chunks, s);
+        ctx->launches += 4;
+        CKL();
+        CK(cudaMemcpyAsync(total, d_row_ptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    }
+    int flags[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(flags, d_flags, sizeof flags, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (flags[2] != 0x7f7f7f7f)
+        return fail(ctx, FM3DT_ERANGE, "receiver " + std::to_string(flags[2] + 1) + " lies outside the grid");
+    if (flags[1] != 0x7f7f7f7f)
+        return fail(ctx, FM3DT_ERANGE, "ray " + std::to_string(flags[1]) + ": receiver " +
+                                           std::to_string(flags[1] % nrc + 1) + " lies outside the grid");
+    if (flags[0] != 0x7f7f7f7f)
+        return fail(ctx, FM3DT_ERANGE, "ray " + std::to_string(flags[0]) +
+                                           ": B-spline support outside the velocity grid");
+    *d_fdm_out = d_fdm;
+    return FM3DT_OK;
+}
+
+int fm3dt_forward_device(fm3dt_ctx *ctx, int nev, const double *d_boundary, int nrc, const double *d_rcr,
+                         const double *d_rcx, const double *d_rcz, float *d_times, int64_t *d_row_ptr,
+                         int32_t *d_cols, float *d_vals, int64_t cap, int64_t *total, double *d_endpoints,
+                         fm3dt_status *st)
+{
+    int rc = check_ready(ctx, nev);
+    if (rc) return rc;
+    if (!d_boundary || nrc < 0 || (nrc > 0 && (!d_rcr || !d_rcx || !d_rcz || !d_times)))
+        return fail(ctx, FM3DT_EINVAL, "null argument");
+    const bool want_rows = d_cols != nullptr && d_vals != nullptr;
+    if (want_rows && (!d_row_ptr || !total)) return fail(ctx, FM3DT_EINVAL, "rows need d_row_ptr and total");
+    if (total) *total = 0;
+    CK(cudaMemcpyAsync(ctx->d_frames, d_boundary, (size_t)nev * ctx->NB * sizeof(double), cudaMemcpyDeviceToDevice,
+                       ctx->stream));
+    DeviceScratch sc(ctx);
+    int64_t n = 0;
+    float *d_fdm = nullptr;
+    rc = forward_common(ctx, sc, nev, nrc, d_rcr, d_rcx, d_rcz, d_times, want_rows, d_endpoints, d_row_ptr, &n,
+                        &d_fdm, st);
+    if (rc != FM3DT_OK || !want_rows || nrc == 0) return rc;
+    *total = n;
+    if (n > cap)
+        return fail(ctx, FM3DT_ERANGE, "Frechet rows need " + std::to_string(n) + " entries, capacity " +
+                                           std::to_string(cap));
+    if (n > 0) {
+        rc = rays_compact(ctx, d_fdm, nev * nrc, d_row_ptr, d_cols, d_vals);
+        if (rc != FM3DT_OK) return rc;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FM3DT_OK;
+}
+
+int fm3dt_forward(fm3dt_ctx *ctx, int nev, const double *boundary, int nrc, const double *rcr, const double *rcx,
+                  const double *rcz, float *times, int64_t *row_ptr, int32_t *cols, float *vals, int64_t cap,
+                  double *endpoints, fm3dt_status *st)
+{
+    int rc = check_ready(ctx, nev);
+    if (rc) return rc;
+    if (!boundary || nrc < 0 || (nrc > 0 && (!rcr || !rcx || !rcz || !times)))
+        return fail(ctx, FM3DT_EINVAL, "null argument");
+    const bool want_rows = cols != nullptr && vals != nullptr;
+    if (want_rows && !row_ptr) return fail(ctx, FM3DT_EINVAL, "rows need row_ptr");
+    cudaStream_t s = ctx->stream;
+    const int nrows = nev * nrc;
+    DeviceScratch sc(ctx);
+    double *d_rec = nullptr, *d_end = nullptr;
+    float *d_times = nullptr;
+    int64_t *d_rowptr = nullptr;
+    if (nrc > 0) {
+        CK(sc.alloc(&d_rec, 3 * (size_t)nrc));
+        CK(sc.alloc(&d_times, (size_t)nrows));
+        if (endpoints) CK(sc.alloc(&d_end, 3 * (size_t)nrows));
+        if (want_rows) CK(sc.alloc(&d_rowptr, (size_t)nrows + 1));
+        CK(cudaMemcpyAsync(d_rec, rcr, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_rec + nrc, rcx, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_rec + 2 * nrc, rcz, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemcpyAsync(ctx->d_frames, boundary, (size_t)nev * ctx->NB * sizeof(double), cudaMemcpyHostToDevice, s));
+    int64_t total = 0;
+    float *d_fdm = nullptr;
+    rc = forward_common(ctx, sc, nev, nrc, d_rec, d_rec + nrc, d_rec + 2 * nrc, d_times, want_rows, d_end, d_rowptr,
+                        &total, &d_fdm, st);
+    if (rc != FM3DT_OK || nrc == 0) return rc;
+    CK(cudaMemcpyAsync(times, d_times, (size_t)nrows * sizeof(float), cudaMemcpyDeviceToHost, s));
+    if (endpoints)
+        CK(cudaMemcpyAsync(endpoints, d_end, 3 * (size_t)nrows * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (want_rows) {
+        CK(cudaMemcpyAsync(row_ptr, d_rowptr, ((size_t)nrows + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        if (total > cap) {
+            CK(cudaStreamSynchronize(s));
+            return fail(ctx, FM3DT_ERANGE, "Frechet rows need " + std::to_string(total) + " entries, capacity " +
+                                               std::to_string(cap));
+        }
+        if (total > 0) {
+            const size_t need = (size_t)total * (sizeof(int32_t) + sizeof(float));
+            if (need > ctx->compact_bytes) {
+                CK(cudaStreamSynchronize(s));
+                cudaFree(ctx->d_compact);
+                ctx->d_compact = nullptr;
+                ctx->compact_bytes = 0;
+                CK(cudaMalloc(&ctx->d_compact, need));
+                ctx->compact_bytes = need;
+            }
+            int32_t *d_cols = (int32_t *)ctx->d_compact;
+            float *d_vals = (float *)((char *)ctx->d_compact + (size_t)total * sizeof(int32_t));
+            rc = rays_compact(ctx, d_fdm, nrows, d_rowptr, d_cols, d_vals);
+            if (rc != FM3DT_OK) return rc;
+            CK(cudaMemcpyAsync(cols, d_cols, (size_t)total * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(vals, d_vals, (size_t)total * sizeof(float), cudaMemcpyDeviceToHost, s));
+        }
+    }
+    CK(cudaStreamSynchronize(s));
+    return FM3DT_OK;
+}
+
+int fm3dt_forward_early_events(const fm3dt_ctx *ctx)
+{
+    return ctx ? ctx->early_events : 0;
 }
 
 int fm3dt_get_times(fm3dt_ctx *ctx, int event, double *ttn)
@@ -1967,6 +2202,7 @@ void fm3dt_ctx_destroy(fm3dt_ctx *ctx)
     cudaFree(ctx->d_list_c);
     cudaFree(ctx->d_act_items);
     cudaFree(ctx->d_next);
+    cudaFree(ctx->d_ray_events);
     for (auto p : ctx->d_done) cudaFree(p);
     cudaFree(ctx->d_dense);
     cudaFree(ctx->d_compact);

@@ -252,6 +252,8 @@ struct RayArgs {
     const void *T;              // [E][N] traveltimes (R)
     const double *veln;         // padded velocity (-1..n+1)
     int nev, nrc;
+    const int *events;          // the events traced (nlist of them), or null for all nev
+    int nlist;
     const double *rcr, *rcx, *rcz;
     float *fdm;                 // [E*nrc][nmp] dense rows, or nullptr
     double *endpoints;          // [E*nrc][3], or nullptr
@@ -332,6 +334,7 @@ struct fm3dt_ctx {
     // events get their extra sweeps; their first round then takes list_b
     cudaStream_t stream2 = nullptr;
     int *d_events_b = nullptr;    // [maxev] the other events
+    int *d_ray_events = nullptr;  // [2 * maxev] a forward call's early ray events, then the rest
     int *d_list_b = nullptr;      // [flag_capacity]
     int *d_count_b = nullptr;
     int *d_list_c = nullptr;      // [flag_capacity] what the near-tie events' first round queues
@@ -353,6 +356,21 @@ struct fm3dt_ctx {
     size_t dense_bytes = 0;
     void *d_compact = nullptr;
     size_t compact_bytes = 0;
+    // A forward call's rays traced inside its solve: when the part of a
+    // two-part solve that converges first is done, its events' rays start on
+    // the context stream while the other part still solves (see
+    // fm3dt_forward_device).  Set for the length of that call only.
+    struct EarlyRays {
+        bool on = false;
+        int nrc = 0;
+        const double *rcr = nullptr, *rcx = nullptr, *rcz = nullptr;
+        float *fdm = nullptr;        // dense rows (zeroed before the first launch), or null
+        size_t fdm_bytes = 0;
+        double *endpoints = nullptr;
+        int *flags = nullptr;        // [2], as RayArgs::flags
+        int *d_events = nullptr;     // [2 * maxev]: the early list, then the rest
+        std::vector<int> events;     // host copy of the early list (empty: none launched)
+    } early;
     unsigned long long h_act_items[2 * kMaxTieSweeps] = {};
     int act_sweeps = 0;
     float tie_sweep_ms[kMaxTieSweeps] = {};      // device time of each (two-part solves)
@@ -381,6 +399,7 @@ struct fm3dt_ctx {
     std::vector<float> round_ms_trace;       // device time of each round of the last solve
     float part_ms[4] = {};                   // the first round's two parts (fm3dt_part_ms)
     float rays_ms[4] = {};                   // the last host-buffer ray call's phases (fm3dt_rays_ms)
+    int early_events = 0;                    // events whose rays the last forward call traced early
     // point sources: fixed node boxes, and the refined source grids' contexts
     int *d_box = nullptr;         // [maxev][6] fixed nodes
     int *d_box_init = nullptr;    // [maxev][6] nodes whose tiles start active

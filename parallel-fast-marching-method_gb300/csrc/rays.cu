@@ -70,7 +70,9 @@ __global__ void __launch_bounds__(kRayBlock) rays_kernel(RayArgs a)
 {
     __shared__ float ray_acc[64 * kRayBlock];
     const Geom g = a.g;
-    const int total = a.nev * a.nrc;
+    // the rays of a.nlist listed events (a.events), or of all a.nev events;
+    // a ray's row, end point and flag index is its event's row e * nrc + i
+    const int total = (a.events ? a.nlist : a.nev) * a.nrc;
     const size_t NB = (size_t)g.nnx * g.nnz;
     const size_t N = NB * g.nnr;
     const size_t nmp = (size_t)(g.nvr + 2) * (g.nvx + 2) * (g.nvz + 2);
@@ -94,8 +96,10 @@ __global__ void __launch_bounds__(kRayBlock) rays_kernel(RayArgs a)
     auto vcellr = [&](double v) { return kFast ? (int)floor((g.gor - v) * ivr_) + 1 : (int)floor((g.gor - v) / g.dvr) + 1; };
     auto vcellx = [&](double v) { return kFast ? (int)floor((v - g.gox) * ivx_) + 1 : (int)floor((v - g.gox) / g.dvx) + 1; };
     auto vcellz = [&](double v) { return kFast ? (int)floor((v - g.goz) * ivz_) + 1 : (int)floor((v - g.goz) / g.dvz) + 1; };
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
-        const int e = q / a.nrc, i = q - e * a.nrc;
+    for (int qq = blockIdx.x * blockDim.x + threadIdx.x; qq < total; qq += gridDim.x * blockDim.x) {
+        const int kk = qq / a.nrc, i = qq - kk * a.nrc;
+        const int e = a.events ? a.events[kk] : kk;
+        const int q = e * a.nrc + i;
         const R *Te = (const R *)a.T + (size_t)e * N;
         float *fdm = a.fdm ? a.fdm + nmp * (size_t)q : nullptr;
         // The row's sums for the velocity cell whose 4 x 4 x 4 B-spline
@@ -479,7 +483,7 @@ void launch_row_scan(const int64_t *counts, int nrows, int64_t *row_ptr, int64_t
 
 void launch_rays(const RayArgs &a, cudaStream_t st)
 {
-    const int total = a.nev * a.nrc;
+    const int total = (a.events ? a.nlist : a.nev) * a.nrc;
     const int block = kRayBlock;
     const int blocks = (total + block - 1) / block;
     if (blocks <= 0) return;

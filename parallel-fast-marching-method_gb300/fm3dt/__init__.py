@@ -56,7 +56,8 @@ class Status(C.Structure):
 EXPORTS = [
     "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_resume",
     "fm3dt_solve_planewave", "fm3dt_solve_point",
-    "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_receiver_times_device", "fm3dt_rays_frechet_device", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
+    "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_receiver_times_device", "fm3dt_rays_frechet_device",
+    "fm3dt_forward", "fm3dt_forward_device", "fm3dt_forward_early_events", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
     "fm3dt_set_tuning", "fm3dt_set_schedule", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_round_trace_ms", "fm3dt_part_ms", "fm3dt_rays_ms", "fm3dt_tie_sweep_items", "fm3dt_tie_sweep_ms", "fm3dt_tile_shapes", "fm3dt_tile_shape",
     "fm3dt_launch_count",
     "fm3dt_last_error", "fm3dt_ctx_destroy",
@@ -89,6 +90,11 @@ def load(path: str | None = None):
     L.fm3dt_receiver_times_device.argtypes = [vp, C.c_int, vp, vp, vp, vp]
     L.fm3dt_rays_frechet_device.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, C.c_int64,
                                             C.POINTER(C.c_int64), vp]
+    L.fm3dt_forward.argtypes = [vp, C.c_int, dp, C.c_int, dp, dp, dp, C.POINTER(C.c_float), C.POINTER(C.c_int64),
+                                C.POINTER(C.c_int32), C.POINTER(C.c_float), C.c_int64, dp, C.POINTER(Status)]
+    L.fm3dt_forward_device.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_int64,
+                                       C.POINTER(C.c_int64), vp, C.POINTER(Status)]
+    L.fm3dt_forward_early_events.argtypes = [vp]
     L.fm3dt_get_times.argtypes = [vp, C.c_int, dp]
     L.fm3dt_set_times.argtypes = [vp, C.c_int, C.c_int, dp]
     L.fm3dt_get_velocity.argtypes = [vp, dp]
@@ -412,6 +418,78 @@ class Solver:
             C.cast(C.c_void_p(cols_ptr), C.POINTER(C.c_int32)), C.cast(C.c_void_p(vals_ptr), C.POINTER(C.c_float)),
             int(cap), C.cast(C.c_void_p(ends_ptr or None), C.POINTER(C.c_double))))
         return int(C.cast(C.c_void_p(row_ptr_ptr + 8 * self.nev * len(rcr)), C.POINTER(C.c_int64))[0])
+
+    def forward(self, frames, rcr, rcx, rcz, rows: bool = True, cap: int | None = None):
+        """One forward step (fm3dt_forward): solve the frames, then receiver
+        times, rays and Frechet rows in one call.  Returns (status, times
+        nev x nrc, (row_ptr, cols, vals) or None, end points nev*nrc x 3)."""
+        frames = np.ascontiguousarray(frames, dtype=np.float64)
+        nnr, nnx, nnz = self.nn
+        nev = frames.size // (nnx * nnz)
+        if frames.size != nev * nnx * nnz:
+            raise ValueError("frames must be nev x nnx x nnz")
+        rcr, rcx, rcz = (np.ascontiguousarray(v, dtype=np.float64) for v in (rcr, rcx, rcz))
+        nrc = len(rcr)
+        times = np.zeros((nev, nrc), dtype=np.float32)
+        ends = np.zeros((nev * nrc, 3), dtype=np.float64)
+        row_ptr = np.zeros(nev * nrc + 1, dtype=np.int64)
+        if cap is None:
+            cap = nev * nrc * 64 + 1024
+        cols = np.zeros(max(cap, 1), dtype=np.int32) if rows else None
+        vals = np.zeros(max(cap, 1), dtype=np.float32) if rows else None
+        st = Status()
+        for _ in range(2):
+            rc = self._L.fm3dt_forward(
+                self._ctx, nev, _d(frames), nrc, _d(rcr), _d(rcx), _d(rcz),
+                times.ctypes.data_as(C.POINTER(C.c_float)), row_ptr.ctypes.data_as(C.POINTER(C.c_int64)),
+                cols.ctypes.data_as(C.POINTER(C.c_int32)) if rows else None,
+                vals.ctypes.data_as(C.POINTER(C.c_float)) if rows else None, int(cap if rows else 0), _d(ends),
+                C.byref(st))
+            if rows and rc == ERANGE and row_ptr[-1] > cap:
+                cap = int(row_ptr[-1])            # sized by the first call: solve once more
+                cols = np.zeros(cap, dtype=np.int32)
+                vals = np.zeros(cap, dtype=np.float32)
+                continue
+            break
+        self._check(rc)
+        self.nev = nev
+        out = (row_ptr, cols[:row_ptr[-1]], vals[:row_ptr[-1]]) if rows else None
+        return st.as_dict(), times, out, ends
+
+    def forward_device(self, nev: int, frames_ptr: int, nrc: int, rcr_ptr: int, rcx_ptr: int, rcz_ptr: int,
+                       times_ptr: int, row_ptr_ptr: int, cols_ptr: int, vals_ptr: int, cap: int,
+                       ends_ptr: int = 0) -> tuple[dict, int]:
+        """One forward step with every array in device memory (raw device
+        addresses; cols/vals 0 to trace rays only).  Returns (status, entry
+        count)."""
+        total = C.c_int64(0)
+        st = Status()
+        self._check(self._L.fm3dt_forward_device(
+            self._ctx, int(nev), C.c_void_p(frames_ptr), int(nrc), C.c_void_p(rcr_ptr), C.c_void_p(rcx_ptr),
+            C.c_void_p(rcz_ptr), C.c_void_p(times_ptr), C.c_void_p(row_ptr_ptr or None),
+            C.c_void_p(cols_ptr or None), C.c_void_p(vals_ptr or None), int(cap), C.byref(total),
+            C.c_void_p(ends_ptr or None), C.byref(st)))
+        self.nev = int(nev)
+        return st.as_dict(), int(total.value)
+
+    def forward_into(self, nev: int, frames_ptr: int, rcr, rcx, rcz, times_ptr: int, row_ptr_ptr: int,
+                     cols_ptr: int, vals_ptr: int, cap: int) -> int:
+        """One forward step with caller-owned host memory (e.g. pinned) at
+        raw addresses: frames in, times, row pointers, cols and vals out.
+        Returns the entry count."""
+        st = Status()
+        self._check(self._L.fm3dt_forward(
+            self._ctx, int(nev), C.cast(C.c_void_p(frames_ptr), C.POINTER(C.c_double)), len(rcr), _d(rcr),
+            _d(rcx), _d(rcz), C.cast(C.c_void_p(times_ptr), C.POINTER(C.c_float)),
+            C.cast(C.c_void_p(row_ptr_ptr), C.POINTER(C.c_int64)), C.cast(C.c_void_p(cols_ptr), C.POINTER(C.c_int32)),
+            C.cast(C.c_void_p(vals_ptr), C.POINTER(C.c_float)), int(cap), None, C.byref(st)))
+        self.nev = int(nev)
+        return int(C.cast(C.c_void_p(row_ptr_ptr + 8 * self.nev * len(rcr)), C.POINTER(C.c_int64))[0])
+
+    @property
+    def forward_early_events(self) -> int:
+        """Events whose rays the last forward call traced inside its solve."""
+        return int(self._L.fm3dt_forward_early_events(self._ctx))
 
     def get_times(self, event: int = 0) -> np.ndarray:
         nnr, nnx, nnz = self.nn

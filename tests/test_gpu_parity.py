@@ -514,3 +514,63 @@ def test_solve_profile_is_reported(gpu_lib):
         assert rows[0][-1] > 0
         rm = s.rays_ms()
         assert rm.shape == (4,) and np.all(rm >= 0.0) and rm[0] > 0.0 and rm[3] > 0.0
+
+
+@pytest.mark.parametrize("nev", [44, 6])
+def test_forward_equals_three_calls(gpu_lib, nev):
+    """fm3dt_forward (solve, receiver times, rays and rows in one call, the
+    rays of the part that converges first traced inside the solve) gives
+    bit for bit what fm3dt_solve, fm3dt_receiver_times and fm3dt_rays_frechet
+    give called in turn: on a batch solved in two parts (44 events, some
+    near ties) and on a small batch solved in one (6 events);
+    the device form matches the host form."""
+    import torch
+    import fm3dt
+    from fm3dt import synth
+    baz = np.concatenate([np.linspace(0.0, 352.5, 40), [0.4, 90.3, 179.6, 270.2]])
+    events = np.stack([np.linspace(32.0, 88.0, len(baz)), baz], axis=1)[:nev]
+    w = _setup(3, 30, events=events)
+    params = _params(w)
+    frames = synth.planewave_frames(w.header, params)
+    rcx, rcz = fm3dt.latlon_to_rad(w.rec_lat, w.rec_lon)
+    rcr = np.asarray(w.rec_elev, dtype=np.float64)
+    nrc = len(rcr)
+    with fm3dt.Solver(w.header, precision=fm3dt.FP32_OFFSET, max_events=nev) as s:
+        s.set_velocity(w.velv)
+        s.set_schedule(4, 0.1, -1, -1.0)
+        assert s.solve(frames)["converged"] == 1
+        t_ref = s.receiver_times(rcr, rcx, rcz)
+        rp_ref, c_ref, v_ref, e_ref = s.rays_frechet(rcr, rcx, rcz)
+        st, times, (rp, c, v), ends = s.forward(frames, rcr, rcx, rcz)
+        assert st["converged"] == 1
+        # (early rays when the other events converge before the near-tie
+        # events' chain ends, which this small grid does not guarantee)
+        print(f"\n{nev} events: rays of {s.forward_early_events} traced inside the solve")
+        assert 0 <= s.forward_early_events < nev
+        if nev < 32:
+            assert s.forward_early_events == 0
+        assert np.array_equal(times, t_ref)
+        assert np.array_equal(rp, rp_ref) and np.array_equal(c, c_ref) and np.array_equal(v, v_ref)
+        assert np.array_equal(ends, e_ref.reshape(-1, 3))
+        # the device form, into device arrays
+        dev = torch.device("cuda")
+        d_frames = torch.from_numpy(frames).to(dev)
+        d_rec = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (rcr, rcx, rcz)]
+        d_times = torch.empty((nev, nrc), dtype=torch.float32, device=dev)
+        d_rp = torch.empty(nev * nrc + 1, dtype=torch.int64, device=dev)
+        cap = int(rp_ref[-1])
+        d_c = torch.empty(cap, dtype=torch.int32, device=dev)
+        d_v = torch.empty(cap, dtype=torch.float32, device=dev)
+        d_e = torch.empty((nev * nrc, 3), dtype=torch.float64, device=dev)
+        st2, total = s.forward_device(nev, d_frames.data_ptr(), nrc, *[x.data_ptr() for x in d_rec],
+                                      d_times.data_ptr(), d_rp.data_ptr(), d_c.data_ptr(), d_v.data_ptr(), cap,
+                                      d_e.data_ptr())
+        assert st2["converged"] == 1 and total == cap
+        assert np.array_equal(d_times.cpu().numpy(), t_ref)
+        assert np.array_equal(d_rp.cpu().numpy(), rp_ref)
+        assert np.array_equal(d_c.cpu().numpy(), c_ref) and np.array_equal(d_v.cpu().numpy(), v_ref)
+        assert np.array_equal(d_e.cpu().numpy(), e_ref.reshape(-1, 3))
+        # too small a capacity: ERANGE with the required count
+        with pytest.raises(fm3dt.Fm3dtError):
+            s.forward_device(nev, d_frames.data_ptr(), nrc, *[x.data_ptr() for x in d_rec], d_times.data_ptr(),
+                             d_rp.data_ptr(), d_c.data_ptr(), d_v.data_ptr(), cap - 1)
