@@ -344,58 +344,106 @@ __global__ void __launch_bounds__(kRayBlock) rays_kernel(RayArgs a)
 }
 
 // Rows: count and compact entries with |f| >= 1e-6 (F:7739-7765).  One block
-// per row; the block scans the row in column order.
+// per row; the block scans the row in column order, V consecutive columns per
+// thread (V = 4: 16-byte loads, when the row length keeps every row 16-byte
+// aligned), so that enough loads are in flight to stream the dense rows at
+// HBM speed.
+template <int V>
+struct RowVec;
+template <>
+struct RowVec<1> {
+    static __device__ __forceinline__ void load(const float *p, float (&v)[1]) { v[0] = __ldcs(p); }
+};
+template <>
+struct RowVec<4> {
+    static __device__ __forceinline__ void load(const float *p, float (&v)[4])
+    {
+        const float4 x = __ldcs(reinterpret_cast<const float4 *>(p));
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    }
+};
+
+template <int V>
 __global__ void row_counts_kernel(const float *__restrict__ fdm, int nrows, int nmp, int64_t *__restrict__ counts)
 {
     const float ftol = 1.0e-6f;
-    for (int row = blockIdx.x; row < nrows; row += gridDim.x) {
+    __shared__ int red[2][32];
+    const int nv = nmp / V;                      // whole vectors (nmp % V == 0)
+    int it = 0;
+    for (int row = blockIdx.x; row < nrows; row += gridDim.x, it ^= 1) {
         const float *f = fdm + (size_t)row * nmp;
         int c = 0;
-        for (int q = threadIdx.x; q < nmp; q += blockDim.x) c += fabsf(f[q]) >= ftol ? 1 : 0;
+#pragma unroll 2
+        for (int q = threadIdx.x; q < nv; q += blockDim.x) {
+            float v[V];
+            RowVec<V>::load(f + (size_t)q * V, v);
+#pragma unroll
+            for (int j = 0; j < V; ++j) c += fabsf(v[j]) >= ftol ? 1 : 0;
+        }
         for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-        __shared__ int red[32];
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+        // (two buffers: a row's sums are not overwritten by the next row's
+        // before thread 0 has read them)
+        if ((threadIdx.x & 31) == 0) red[it][threadIdx.x >> 5] = c;
         __syncthreads();
         if (threadIdx.x == 0) {
-            int s = 0;
-            for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) s += red[w];
-            counts[row] = s;
+            int sum = 0;
+            for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) sum += red[it][w];
+            counts[row] = sum;
         }
-        __syncthreads();
     }
 }
 
-__global__ void row_compact_kernel(const float *__restrict__ fdm, int nrows, int nmp, const int64_t *__restrict__ row_ptr,
-                                   int32_t *__restrict__ cols, float *__restrict__ vals)
+template <int V>
+__global__ void row_compact_kernel(const float *__restrict__ fdm, int nrows, int nmp,
+                                   const int64_t *__restrict__ row_ptr, int32_t *__restrict__ cols,
+                                   float *__restrict__ vals)
 {
     const float ftol = 1.0e-6f;
-    __shared__ int wsum[32];
-    __shared__ int64_t s_base;
+    __shared__ int wsum[2][32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    const int nv = nmp / V;
+    int it = 0;
     for (int row = blockIdx.x; row < nrows; row += gridDim.x) {
         const float *f = fdm + (size_t)row * nmp;
-        if (threadIdx.x == 0) s_base = row_ptr[row];
-        __syncthreads();
-        for (int c0 = 0; c0 < nmp; c0 += blockDim.x) {
+        int64_t base = row_ptr[row];
+        for (int c0 = 0; c0 < nv; c0 += blockDim.x, it ^= 1) {
             const int q = c0 + threadIdx.x;
-            const float v = q < nmp ? f[q] : 0.0f;
-            const bool keep = q < nmp && fabsf(v) >= ftol;
-            const unsigned m = __ballot_sync(0xffffffffu, keep);
-            if (lane == 0) wsum[wid] = __popc(m);
+            float v[V];
+            int k = 0;
+            if (q < nv) {
+                RowVec<V>::load(f + (size_t)q * V, v);
+#pragma unroll
+                for (int j = 0; j < V; ++j) k += fabsf(v[j]) >= ftol ? 1 : 0;
+            }
+            // the thread's first slot: the kept entries of the lower threads
+            // of its warp, then of the lower warps
+            int incl = k;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31) wsum[it][wid] = incl;
             __syncthreads();
             int before = 0, total = 0;
             for (int w = 0; w < nw; ++w) {
-                if (w < wid) before += wsum[w];
-                total += wsum[w];
+                const int x = wsum[it][w];
+                before += w < wid ? x : 0;
+                total += x;
             }
-            if (keep) {
-                const int64_t pos = s_base + before + __popc(m & ((1u << lane) - 1u));
-                cols[pos] = q + 1;
-                vals[pos] = v;
+            if (k > 0) {
+                int64_t pos = base + before + incl - k;
+#pragma unroll
+                for (int j = 0; j < V; ++j)
+                    if (fabsf(v[j]) >= ftol) {
+                        cols[pos] = q * V + j + 1;
+                        vals[pos] = v[j];
+                        ++pos;
+                    }
             }
-            __syncthreads();
-            if (threadIdx.x == 0) s_base += total;
-            __syncthreads();
+            base += total;
+            // (the next chunk writes the other wsum buffer; the one after it
+            // this buffer again, after the next chunk's barrier, which every
+            // thread reaches only after reading this one)
         }
     }
 }
@@ -496,14 +544,22 @@ void launch_rays(const RayArgs &a, cudaStream_t st)
 void launch_row_counts(const float *fdm, int nrows, int nmp, int64_t *counts, cudaStream_t st)
 {
     if (nrows <= 0) return;
-    row_counts_kernel<<<nrows < 152 * 16 ? nrows : 152 * 16, 256, 0, st>>>(fdm, nrows, nmp, counts);
+    const int grid = nrows < 152 * 16 ? nrows : 152 * 16;
+    if (nmp % 4 == 0)
+        row_counts_kernel<4><<<grid, 256, 0, st>>>(fdm, nrows, nmp, counts);
+    else
+        row_counts_kernel<1><<<grid, 256, 0, st>>>(fdm, nrows, nmp, counts);
 }
 
 void launch_row_compact(const float *fdm, int nrows, int nmp, const int64_t *row_ptr, int32_t *cols, float *vals,
                         cudaStream_t st)
 {
     if (nrows <= 0) return;
-    row_compact_kernel<<<nrows < 152 * 16 ? nrows : 152 * 16, 256, 0, st>>>(fdm, nrows, nmp, row_ptr, cols, vals);
+    const int grid = nrows < 152 * 16 ? nrows : 152 * 16;
+    if (nmp % 4 == 0)
+        row_compact_kernel<4><<<grid, 256, 0, st>>>(fdm, nrows, nmp, row_ptr, cols, vals);
+    else
+        row_compact_kernel<1><<<grid, 256, 0, st>>>(fdm, nrows, nmp, row_ptr, cols, vals);
 }
 
 }  // namespace fm3dt
