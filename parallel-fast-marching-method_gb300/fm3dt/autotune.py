@@ -37,7 +37,12 @@ def autotune(solver, frames_ptr: int, nev: int, device: bool = True, repeats: in
     """Returns (round_shape, max_passes, sweep_shape, ms, schedule,
     tie_segments) and applies it; schedule = (tie_sweeps, tie_ratio,
     resweeps, resweep_frac), negative values being the defaults kept;
-    tie_segments None when not tuned (the solver's setting is kept)."""
+    tie_segments None when not tuned (the solver's setting is kept).
+
+    Coordinate descent: the sweep shape, then the round tiles under the
+    default schedule, the schedule under those tiles, the segments; then the
+    round tiles once more under the chosen schedule (the best tile depends
+    on how much work the rounds get), and if they change, the schedule again."""
     nshapes = len(tile_shapes())
     round_shape, cap = 0, PASS_CAPS[0]
     solver.set_tuning(round_shape, cap, 0, 1)
@@ -48,21 +53,30 @@ def autotune(solver, frames_ptr: int, nev: int, device: bool = True, repeats: in
         if best_sweep is None or ms < best_sweep[1]:
             best_sweep = (sshape, ms)
     solver.set_sweep_shape(best_sweep[0])
-    best = None
-    for shape in range(nshapes):
-        for c in PASS_CAPS:
-            solver.set_tuning(shape, c, 0, 1)
+
+    def tune_tiles():
+        best = None
+        for shape in range(nshapes):
+            for c in PASS_CAPS:
+                solver.set_tuning(shape, c, 0, 1)
+                ms = _time(solver, frames_ptr, nev, device, repeats)
+                if best is None or ms < best[2]:
+                    best = (shape, c, ms)
+        solver.set_tuning(best[0], best[1], 0, 1)
+        return best
+
+    def tune_schedule():
+        best_sched = None
+        for ts, tr in SCHEDULES:
+            solver.set_schedule(ts, tr, -1, -1.0)
             ms = _time(solver, frames_ptr, nev, device, repeats)
-            if best is None or ms < best[2]:
-                best = (shape, c, ms)
-    solver.set_tuning(best[0], best[1], 0, 1)
-    best_sched = None
-    for ts, tr in SCHEDULES:
-        solver.set_schedule(ts, tr, -1, -1.0)
-        ms = _time(solver, frames_ptr, nev, device, repeats)
-        if best_sched is None or ms < best_sched[2]:
-            best_sched = (ts, tr, ms)
-    solver.set_schedule(best_sched[0], best_sched[1], -1, -1.0)
+            if best_sched is None or ms < best_sched[2]:
+                best_sched = (ts, tr, ms)
+        solver.set_schedule(best_sched[0], best_sched[1], -1, -1.0)
+        return best_sched
+
+    best = tune_tiles()
+    best_sched = tune_schedule()
     best_seg = (None, best_sched[2])
     if tune_segments:
         for ts in TIE_SEGMENTS:
@@ -71,5 +85,12 @@ def autotune(solver, frames_ptr: int, nev: int, device: bool = True, repeats: in
             if best_seg[0] is None or ms < best_seg[1]:
                 best_seg = (ts, ms)
         solver.set_sweep_segments(0, best_seg[0])
-    return (best[0], best[1], best_sweep[0], min(best[2], best_sched[2], best_seg[1]),
-            (best_sched[0], best_sched[1], -1, -1.0), best_seg[0])
+    again = tune_tiles()
+    ms = again[2]
+    if again[:2] != best[:2]:
+        best = again
+        best_sched = tune_schedule()
+        ms = best_sched[2]
+    else:
+        best = again
+    return (best[0], best[1], best_sweep[0], ms, (best_sched[0], best_sched[1], -1, -1.0), best_seg[0])
