@@ -571,6 +571,17 @@ def test_forward_equals_three_calls(gpu_lib, nev):
         assert np.array_equal(d_c.cpu().numpy(), c_ref) and np.array_equal(d_v.cpu().numpy(), v_ref)
         assert np.array_equal(d_e.cpu().numpy(), e_ref.reshape(-1, 3))
         # too small a capacity: ERANGE with the required count
-        with pytest.raises(fm3dt.Fm3dtError):
+        with pytest.raises(fm3dt.Fm3dtError) as ei:
             s.forward_device(nev, d_frames.data_ptr(), nrc, *[x.data_ptr() for x in d_rec], d_times.data_ptr(),
                              d_rp.data_ptr(), d_c.data_ptr(), d_v.data_ptr(), cap - 1)
+        assert ei.value.code == fm3dt.ERANGE
+        # a receiver outside the grid: ERANGE, as fm3dt_receiver_times gives it
+        bad = rcx.copy()
+        bad[nrc // 2] = 10.0
+        with pytest.raises(fm3dt.Fm3dtError) as ei:
+            s.forward(frames, rcr, bad, rcz)
+        assert ei.value.code == fm3dt.ERANGE
+        with pytest.raises(fm3dt.Fm3dtError) as ej:
+            s.receiver_times(rcr, bad, rcz)
+        assert ej.value.code == fm3dt.ERANGE
+        assert f"receiver {nrc // 2 + 1} " in str(ei.value) and f"receiver {nrc // 2 + 1} " in str(ej.value)
