@@ -204,29 +204,52 @@ int main(int argc, char **argv)
             const int nb = (int)((nsrc - s0) < (size_t)d.max_events ? (nsrc - s0) : (size_t)d.max_events);
             if (!frames.next(nb, fbuf.data())) { status = input_error(in.itimes + ": short read"); break; }
             fm3dt_status st{};
-            rc = fm3dt_solve(ctx, nb, fbuf.data(), &st);
-            if (rc != FM3DT_OK) { status = lib_error(ctx, "fm3dt_solve", rc); break; }
-            for (int e = 0; e < nb; ++e)
-                std::printf("Finish Source: %zu (array %zu) rounds %d\n", s0 + e + 1, ai + 1, st.rounds);
-            if (rt && nrc > 0) {
-                times.resize((size_t)nb * nrc);
-                rc = fm3dt_receiver_times(ctx, nrc, rcr.data(), rcx.data(), rcz.data(), times.data());
-                if (rc != FM3DT_OK) { status = lib_error(ctx, "fm3dt_receiver_times", rc); break; }
-                for (float t : times) std::fprintf(rt, "%s\n", format_real4(t).c_str());
-            }
-            if (fw && nrc > 0) {
-                const size_t rows = (size_t)nb * nrc;
+            const size_t rows = (size_t)nb * nrc;
+            // With both outputs, one forward call (solve, times, rays and rows;
+            // the rays of the batch's faster part start while the rest still
+            // solves); a capacity too small for the rows solves once more.
+            const bool forward = rt && fw && nrc > 0;
+            if (forward) {
+                times.resize(rows);
                 row_ptr.assign(rows + 1, 0);
                 int64_t cap = (int64_t)rows * 512;
                 for (int attempt = 0; attempt < 2; ++attempt) {
                     cols.resize((size_t)cap);
                     vals.resize((size_t)cap);
-                    rc = fm3dt_rays_frechet(ctx, nrc, rcr.data(), rcx.data(), rcz.data(), row_ptr.data(),
-                                            cols.data(), vals.data(), cap, nullptr);
+                    rc = fm3dt_forward(ctx, nb, fbuf.data(), nrc, rcr.data(), rcx.data(), rcz.data(), times.data(),
+                                       row_ptr.data(), cols.data(), vals.data(), cap, nullptr, &st);
                     if (rc == FM3DT_ERANGE && row_ptr[rows] > cap) { cap = row_ptr[rows]; continue; }
                     break;
                 }
-                if (rc != FM3DT_OK) { status = lib_error(ctx, "fm3dt_rays_frechet", rc); break; }
+                if (rc != FM3DT_OK) { status = lib_error(ctx, "fm3dt_forward", rc); break; }
+            } else {
+                rc = fm3dt_solve(ctx, nb, fbuf.data(), &st);
+                if (rc != FM3DT_OK) { status = lib_error(ctx, "fm3dt_solve", rc); break; }
+            }
+            for (int e = 0; e < nb; ++e)
+                std::printf("Finish Source: %zu (array %zu) rounds %d\n", s0 + e + 1, ai + 1, st.rounds);
+            if (rt && nrc > 0) {
+                if (!forward) {
+                    times.resize(rows);
+                    rc = fm3dt_receiver_times(ctx, nrc, rcr.data(), rcx.data(), rcz.data(), times.data());
+                    if (rc != FM3DT_OK) { status = lib_error(ctx, "fm3dt_receiver_times", rc); break; }
+                }
+                for (float t : times) std::fprintf(rt, "%s\n", format_real4(t).c_str());
+            }
+            if (fw && nrc > 0) {
+                if (!forward) {
+                    row_ptr.assign(rows + 1, 0);
+                    int64_t cap = (int64_t)rows * 512;
+                    for (int attempt = 0; attempt < 2; ++attempt) {
+                        cols.resize((size_t)cap);
+                        vals.resize((size_t)cap);
+                        rc = fm3dt_rays_frechet(ctx, nrc, rcr.data(), rcx.data(), rcz.data(), row_ptr.data(),
+                                                cols.data(), vals.data(), cap, nullptr);
+                        if (rc == FM3DT_ERANGE && row_ptr[rows] > cap) { cap = row_ptr[rows]; continue; }
+                        break;
+                    }
+                    if (rc != FM3DT_OK) { status = lib_error(ctx, "fm3dt_rays_frechet", rc); break; }
+                }
                 for (size_t q = 0; q < rows; ++q) {
                     const int k = (int)(q % nrc) + 1;   // receiver index within its array
                     if (!fw->row(k, cols.data() + row_ptr[q], vals.data() + row_ptr[q], row_ptr[q + 1] - row_ptr[q])) {
