@@ -512,7 +512,10 @@ __device__ __forceinline__ void stream_sweep_body(const StreamArgs<R> &a)
 // one-launch form, each with its own register budget: the one-launch form
 // holds its items' queue state, and is bounded to the resident CTAs of the
 // per-hyperplane form's main sweep.
-template <typename R> struct FlowBlocks { static constexpr int value = 20; };
+#ifndef FM_FLOW_BLOCKS_F32
+#define FM_FLOW_BLOCKS_F32 20
+#endif
+template <typename R> struct FlowBlocks { static constexpr int value = FM_FLOW_BLOCKS_F32; };
 template <> struct FlowBlocks<double> { static constexpr int value = 12; };
 
 template <typename R, int SX, int SZ, bool FRESH>
