@@ -434,7 +434,7 @@ class Solver:
         ends = np.zeros((nev * nrc, 3), dtype=np.float64)
         row_ptr = np.zeros(nev * nrc + 1, dtype=np.int64)
         if cap is None:
-            cap = nev * nrc * 64 + 1024
+            cap = nev * nrc * 512 + 1024     # (a smaller capacity costs a second solve when exceeded)
         cols = np.zeros(max(cap, 1), dtype=np.int32) if rows else None
         vals = np.zeros(max(cap, 1), dtype=np.float32) if rows else None
         st = Status()
