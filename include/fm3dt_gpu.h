@@ -213,7 +213,10 @@ int fm3dt_rays_frechet_device(fm3dt_ctx *ctx, int nrc, const double *d_rcr, cons
  * (near-tie events and the others), the rays of the part that converges
  * first are traced while the other part still solves.
  * fm3dt_forward: host buffers (boundary frames, receivers in; times nev x nrc,
- * rows and nullable endpoints out; cols = vals = NULL traces rays only).
+ * rows and nullable endpoints out; cols = vals = NULL traces rays only); when
+ * cols and vals are page-locked memory mapped for the device (cudaHostAlloc,
+ * cudaHostRegister), the compaction kernel writes the rows into them
+ * directly, without a copy through device memory.
  * fm3dt_forward_device: every array a device pointer (d_boundary frames
  * are copied into the context), *total on the host as in
  * fm3dt_rays_frechet_device.  st is nullable.  Both return after the GPU work

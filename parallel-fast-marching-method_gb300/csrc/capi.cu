@@ -386,6 +386,14 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #define FM_SWEEP_GRAPHS 1
 #endif
 
+// Host entry points write the compacted Frechet rows straight into the
+// caller's host arrays from the compaction kernel when those arrays are
+// page-locked memory mapped for the device (one pass over the link instead
+// of a device copy and a copy out); pageable arrays get the copy.
+#ifndef FM_ZERO_COPY_ROWS
+#define FM_ZERO_COPY_ROWS 1
+#endif
+
 // How a solve starts: from boundary frames (initialisation, sweep, rounds),
 // from the current fields (resume: rounds with every tile active), or from
 // point-source boxes the caller already wrote (rounds from the boxes' tiles).
@@ -1678,6 +1686,48 @@ static int rays_trace(fm3dt_ctx *ctx, DeviceScratch &sc, int nrc, const double *
     return FM3DT_OK;
 }
 
+// The address through which this device's kernels reach host memory at p,
+// or null when there is none (pageable memory, or the switch off).
+static void *mapped_host(const void *p)
+{
+    if (!FM_ZERO_COPY_ROWS || !p) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+// Compacted rows of a host entry point into the caller's cols/vals: written
+// there by the compaction kernel when both are mapped page-locked memory,
+// else compacted into the context's buffer and copied out on stream s.
+static int rays_compact(fm3dt_ctx *ctx, const float *d_fdm, int nrows, const int64_t *d_row_ptr, int32_t *d_cols,
+                        float *d_vals);
+static int rays_compact_to_host(fm3dt_ctx *ctx, const float *d_fdm, int nrows, const int64_t *d_rowptr,
+                                int64_t total, int32_t *cols, float *vals, cudaStream_t s)
+{
+    int32_t *m_cols = (int32_t *)mapped_host(cols);
+    float *m_vals = (float *)mapped_host(vals);
+    if (m_cols && m_vals) return rays_compact(ctx, d_fdm, nrows, d_rowptr, m_cols, m_vals);
+    const size_t need = (size_t)total * (sizeof(int32_t) + sizeof(float));
+    if (need > ctx->compact_bytes) {
+        CK(cudaStreamSynchronize(s));
+        cudaFree(ctx->d_compact);
+        ctx->d_compact = nullptr;
+        ctx->compact_bytes = 0;
+        CK(cudaMalloc(&ctx->d_compact, need));
+        ctx->compact_bytes = need;
+    }
+    int32_t *d_cols = (int32_t *)ctx->d_compact;
+    float *d_vals = (float *)((char *)ctx->d_compact + (size_t)total * sizeof(int32_t));
+    const int rc = rays_compact(ctx, d_fdm, nrows, d_rowptr, d_cols, d_vals);
+    if (rc != FM3DT_OK) return rc;
+    CK(cudaMemcpyAsync(cols, d_cols, (size_t)total * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(vals, d_vals, (size_t)total * sizeof(float), cudaMemcpyDeviceToHost, s));
+    return FM3DT_OK;
+}
+
 static int rays_compact(fm3dt_ctx *ctx, const float *d_fdm, int nrows, const int64_t *d_row_ptr, int32_t *d_cols,
                  float *d_vals)
 {
@@ -1976,21 +2026,8 @@ int fm3dt_forward(fm3dt_ctx *ctx, int nev, const double *boundary, int nrc, cons
                                                std::to_string(cap));
         }
         if (total > 0) {
-            const size_t need = (size_t)total * (sizeof(int32_t) + sizeof(float));
-            if (need > ctx->compact_bytes) {
-                CK(cudaStreamSynchronize(s));
-                cudaFree(ctx->d_compact);
-                ctx->d_compact = nullptr;
-                ctx->compact_bytes = 0;
-                CK(cudaMalloc(&ctx->d_compact, need));
-                ctx->compact_bytes = need;
-            }
-            int32_t *d_cols = (int32_t *)ctx->d_compact;
-            float *d_vals = (float *)((char *)ctx->d_compact + (size_t)total * sizeof(int32_t));
-            rc = rays_compact(ctx, d_fdm, nrows, d_rowptr, d_cols, d_vals);
+            rc = rays_compact_to_host(ctx, d_fdm, nrows, d_rowptr, total, cols, vals, s);
             if (rc != FM3DT_OK) return rc;
-            CK(cudaMemcpyAsync(cols, d_cols, (size_t)total * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-            CK(cudaMemcpyAsync(vals, d_vals, (size_t)total * sizeof(float), cudaMemcpyDeviceToHost, s));
         }
     }
     CK(cudaStreamSynchronize(s));

@@ -523,7 +523,7 @@ def test_forward_equals_three_calls(gpu_lib, nev):
     bit for bit what fm3dt_solve, fm3dt_receiver_times and fm3dt_rays_frechet
     give called in turn: on a batch solved in two parts (44 events, some
     near ties) and on a small batch solved in one (6 events);
-    the device form matches the host form."""
+    the device form and the host form into page-locked arrays match."""
     import torch
     import fm3dt
     from fm3dt import synth
@@ -570,6 +570,17 @@ def test_forward_equals_three_calls(gpu_lib, nev):
         assert np.array_equal(d_rp.cpu().numpy(), rp_ref)
         assert np.array_equal(d_c.cpu().numpy(), c_ref) and np.array_equal(d_v.cpu().numpy(), v_ref)
         assert np.array_equal(d_e.cpu().numpy(), e_ref.reshape(-1, 3))
+        # page-locked host arrays: the rows written there by the compaction kernel
+        h_fr = torch.from_numpy(frames).pin_memory()
+        h_t = torch.zeros((nev, nrc), dtype=torch.float32).pin_memory()
+        h_rp = torch.zeros(nev * nrc + 1, dtype=torch.int64).pin_memory()
+        h_c = torch.zeros(cap, dtype=torch.int32).pin_memory()
+        h_v = torch.zeros(cap, dtype=torch.float32).pin_memory()
+        n = s.forward_into(nev, h_fr.data_ptr(), rcr, rcx, rcz, h_t.data_ptr(), h_rp.data_ptr(), h_c.data_ptr(),
+                           h_v.data_ptr(), cap)
+        assert n == cap
+        assert np.array_equal(h_t.numpy(), t_ref) and np.array_equal(h_rp.numpy(), rp_ref)
+        assert np.array_equal(h_c.numpy(), c_ref) and np.array_equal(h_v.numpy(), v_ref)
         # too small a capacity: ERANGE with the required count
         with pytest.raises(fm3dt.Fm3dtError) as ei:
             s.forward_device(nev, d_frames.data_ptr(), nrc, *[x.data_ptr() for x in d_rec], d_times.data_ptr(),
