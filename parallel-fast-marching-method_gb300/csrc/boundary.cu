@@ -195,6 +195,34 @@ void launch_initial_tiles(int nev, const int *events, int tiles_per_event, int f
                                                            count_per_event, list, count, flag);
 }
 
+// Boundary frames copied into device memory by a kernel that reads the
+// caller's page-locked host frames through their device mapping: many loads in
+// flight over the host link, where one copy-engine transfer was slower.
+// 16-byte elements when both ends allow it, else 8-byte ones.
+__global__ void stage_frames_kernel(const double2 *__restrict__ src2, double2 *__restrict__ dst2, size_t n2,
+                                    const double *__restrict__ src, double *__restrict__ dst, size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (src2) {
+        for (size_t i = t; i < n2; i += stride) dst2[i] = __ldcs(src2 + i);
+    } else {
+        for (size_t i = t; i < n; i += stride) dst[i] = __ldcs(src + i);
+    }
+}
+
+void launch_stage_frames(const double *mapped_src, double *dst, size_t n, cudaStream_t st)
+{
+    if (n == 0) return;
+    const bool vec = ((uintptr_t)mapped_src % 16 == 0) && ((uintptr_t)dst % 16 == 0) && (n % 2 == 0);
+    const int grid = 152 * 8;
+    if (vec)
+        stage_frames_kernel<<<grid, 256, 0, st>>>((const double2 *)mapped_src, (double2 *)dst, n / 2, nullptr,
+                                                 nullptr, 0);
+    else
+        stage_frames_kernel<<<grid, 256, 0, st>>>(nullptr, nullptr, 0, mapped_src, dst, n);
+}
+
 void launch_to_absolute(const Geom &g, int prec, const void *T, size_t offset, double base, double *out,
                         cudaStream_t st)
 {

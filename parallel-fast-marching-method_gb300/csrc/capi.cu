@@ -393,6 +393,11 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #ifndef FM_ZERO_COPY_ROWS
 #define FM_ZERO_COPY_ROWS 1
 #endif
+// ... and read page-locked boundary frames through their device mapping with
+// a kernel instead of one copy-engine transfer
+#ifndef FM_STAGE_FRAMES
+#define FM_STAGE_FRAMES 1
+#endif
 
 // How a solve starts: from boundary frames (initialisation, sweep, rounds),
 // from the current fields (resume: rounds with every tile active), or from
@@ -1699,6 +1704,21 @@ static void *mapped_host(const void *p)
     return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
+// A host entry point's boundary frames into ctx->d_frames: read by a kernel
+// through the device mapping when they are page-locked, else copied.
+static int upload_frames(fm3dt_ctx *ctx, const double *boundary, int nev)
+{
+    const size_t n = (size_t)nev * ctx->NB;
+    if (const double *m = FM_STAGE_FRAMES ? (const double *)mapped_host(boundary) : nullptr) {
+        launch_stage_frames(m, ctx->d_frames, n, ctx->stream);
+        ctx->launches += 1;
+        CKL();
+        return FM3DT_OK;
+    }
+    CK(cudaMemcpyAsync(ctx->d_frames, boundary, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    return FM3DT_OK;
+}
+
 // Compacted rows of a host entry point into the caller's cols/vals: written
 // there by the compaction kernel when both are mapped page-locked memory,
 // else compacted into the context's buffer and copied out on stream s.
@@ -2009,7 +2029,8 @@ int fm3dt_forward(fm3dt_ctx *ctx, int nev, const double *boundary, int nrc, cons
         CK(cudaMemcpyAsync(d_rec + nrc, rcx, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(d_rec + 2 * nrc, rcz, nrc * sizeof(double), cudaMemcpyHostToDevice, s));
     }
-    CK(cudaMemcpyAsync(ctx->d_frames, boundary, (size_t)nev * ctx->NB * sizeof(double), cudaMemcpyHostToDevice, s));
+    rc = upload_frames(ctx, boundary, nev);
+    if (rc != FM3DT_OK) return rc;
     int64_t total = 0;
     float *d_fdm = nullptr;
     rc = forward_common(ctx, sc, nev, nrc, d_rec, d_rec + nrc, d_rec + 2 * nrc, d_times, want_rows, d_end, d_rowptr,

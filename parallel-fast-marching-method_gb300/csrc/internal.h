@@ -192,6 +192,8 @@ void launch_planewave_frames(const Geom &g, const PlaneWaveGeom &pg, int nev, co
 void launch_finalize_frames(const Geom &g, int nev, int prec, const double *frames, void *T,
                             uint8_t *frozen, double *base, cudaStream_t st);
 void launch_fill_inf(void *T, size_t n, int prec, cudaStream_t st);
+// n doubles from the device mapping of page-locked host memory into dst
+void launch_stage_frames(const double *mapped_src, double *dst, size_t n, cudaStream_t st);
 void launch_sweep_directions(const Geom &g, int nev, const double *frames, int *dir, double tie_ratio,
                              cudaStream_t st);
 // (events: the event of each of the nev entries; null = 0..nev-1)
