@@ -216,7 +216,8 @@ int fm3dt_rays_frechet_device(fm3dt_ctx *ctx, int nrc, const double *d_rcr, cons
  * rows and nullable endpoints out; cols = vals = NULL traces rays only); when
  * cols and vals are page-locked memory mapped for the device (cudaHostAlloc,
  * cudaHostRegister), the compaction kernel writes the rows into them
- * directly, without a copy through device memory.
+ * directly, without a copy through device memory; page-locked boundary
+ * frames are read through their mapping by a kernel.
  * fm3dt_forward_device: every array a device pointer (d_boundary frames
  * are copied into the context), *total on the host as in
  * fm3dt_rays_frechet_device.  st is nullable.  Both return after the GPU work
