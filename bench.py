@@ -599,6 +599,10 @@ def run_ours(a):
             entries = step_host()
         e2e_s = d.max(time.perf_counter() - t0)
         extras["e2e_ms_per_step"] = {k: statistics.median(v[1:]) for k, v in hphase.items() if len(v) > 1}
+        if fused:
+            # how page-locked frames and rows crossed the host link (measured
+            # on the first call: 0 copy engine, 1 kernels through the mapping)
+            extras["e2e_host_link"] = dict(zip(("frames", "rows"), solver.host_link()))
         if forward and not fused:
             extras["e2e_ms_per_step"]["rays_parts"] = dict(zip(("trace", "compact", "copy_out", "wall"),
                                                                [round(float(x), 3) for x in solver.rays_ms()]))

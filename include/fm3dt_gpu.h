@@ -215,9 +215,9 @@ int fm3dt_rays_frechet_device(fm3dt_ctx *ctx, int nrc, const double *d_rcr, cons
  * fm3dt_forward: host buffers (boundary frames, receivers in; times nev x nrc,
  * rows and nullable endpoints out; cols = vals = NULL traces rays only); when
  * cols and vals are page-locked memory mapped for the device (cudaHostAlloc,
- * cudaHostRegister), the compaction kernel writes the rows into them
- * directly, without a copy through device memory; page-locked boundary
- * frames are read through their mapping by a kernel.
+ * cudaHostRegister), the compaction kernel can write the rows into them
+ * directly, and a kernel can read page-locked boundary frames through their
+ * mapping, where this host's link favours that (fm3dt_set_host_link).
  * fm3dt_forward_device: every array a device pointer (d_boundary frames
  * are copied into the context), *total on the host as in
  * fm3dt_rays_frechet_device.  st is nullable.  Both return after the GPU work
@@ -232,6 +232,16 @@ int fm3dt_forward_device(fm3dt_ctx *ctx, int nev, const double *d_boundary, int 
 /* Events whose rays the last forward call traced inside its solve (0 when
  * the batch was solved in one part). */
 int fm3dt_forward_early_events(const fm3dt_ctx *ctx);
+
+/* How fm3dt_forward moves page-locked host buffers: mode 0 measures it on the
+ * context's next such call (the default: a kernel through the device mapping
+ * against a copy-engine transfer of up to 64 MB of that call's own buffers,
+ * for the frames in and the rows out, the faster kept), 1 always copies, 2
+ * always uses the mapping.  fm3dt_host_link reports the current choice for
+ * the frames and the rows (-1 not yet measured, 0 copies, 1 mapping).
+ * Results do not depend on it. */
+int fm3dt_set_host_link(fm3dt_ctx *ctx, int mode);
+int fm3dt_host_link(const fm3dt_ctx *ctx, int *frames, int *rows);
 
 /* Copies the solved traveltime field of one event to the host: nnr*nnx*nnz
  * doubles, phi fastest (absolute seconds in both precisions; unreached nodes

@@ -195,12 +195,12 @@ void launch_initial_tiles(int nev, const int *events, int tiles_per_event, int f
                                                            count_per_event, list, count, flag);
 }
 
-// Boundary frames copied into device memory by a kernel that reads the
-// caller's page-locked host frames through their device mapping: many loads in
-// flight over the host link, where one copy-engine transfer was slower.
-// 16-byte elements when both ends allow it, else 8-byte ones.
-__global__ void stage_frames_kernel(const double2 *__restrict__ src2, double2 *__restrict__ dst2, size_t n2,
-                                    const double *__restrict__ src, double *__restrict__ dst, size_t n)
+// n doubles copied by a kernel between device memory and the device mapping
+// of page-locked host memory (either side): many loads and stores in flight
+// over the host link, which on some hosts moves data faster than one
+// copy-engine transfer.  16-byte elements when both ends allow it.
+__global__ void link_copy_kernel(const double2 *__restrict__ src2, double2 *__restrict__ dst2, size_t n2,
+                                 const double *__restrict__ src, double *__restrict__ dst, size_t n)
 {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -211,16 +211,36 @@ __global__ void stage_frames_kernel(const double2 *__restrict__ src2, double2 *_
     }
 }
 
-void launch_stage_frames(const double *mapped_src, double *dst, size_t n, cudaStream_t st)
+// `bytes` bytes, both ends 16-byte aligned: 16-byte elements, then the
+// remaining bytes by the first threads of block 0.
+__global__ void link_copy_bytes_kernel(const uint4 *__restrict__ src, uint4 *__restrict__ dst, size_t n16,
+                                       const unsigned char *__restrict__ src_tail,
+                                       unsigned char *__restrict__ dst_tail, int ntail)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) dst[i] = __ldcs(src + i);
+    if (blockIdx.x == 0 && (int)threadIdx.x < ntail) dst_tail[threadIdx.x] = src_tail[threadIdx.x];
+}
+
+void launch_link_copy_bytes(const void *src, void *dst, size_t bytes, cudaStream_t st)
+{
+    if (bytes == 0) return;
+    const size_t n16 = bytes / 16;
+    const int ntail = (int)(bytes % 16);
+    link_copy_bytes_kernel<<<152 * 8, 256, 0, st>>>((const uint4 *)src, (uint4 *)dst, n16,
+                                                    (const unsigned char *)src + 16 * n16,
+                                                    (unsigned char *)dst + 16 * n16, ntail);
+}
+
+void launch_link_copy(const double *src, double *dst, size_t n, cudaStream_t st)
 {
     if (n == 0) return;
-    const bool vec = ((uintptr_t)mapped_src % 16 == 0) && ((uintptr_t)dst % 16 == 0) && (n % 2 == 0);
+    const bool vec = ((uintptr_t)src % 16 == 0) && ((uintptr_t)dst % 16 == 0) && (n % 2 == 0);
     const int grid = 152 * 8;
     if (vec)
-        stage_frames_kernel<<<grid, 256, 0, st>>>((const double2 *)mapped_src, (double2 *)dst, n / 2, nullptr,
-                                                 nullptr, 0);
+        link_copy_kernel<<<grid, 256, 0, st>>>((const double2 *)src, (double2 *)dst, n / 2, nullptr, nullptr, 0);
     else
-        stage_frames_kernel<<<grid, 256, 0, st>>>(nullptr, nullptr, 0, mapped_src, dst, n);
+        link_copy_kernel<<<grid, 256, 0, st>>>(nullptr, nullptr, 0, src, dst, n);
 }
 
 void launch_to_absolute(const Geom &g, int prec, const void *T, size_t offset, double base, double *out,

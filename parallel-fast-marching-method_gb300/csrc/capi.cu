@@ -386,19 +386,6 @@ const CUtensorMap *field_tensor_map(fm3dt_ctx *ctx, int shape)
 #define FM_SWEEP_GRAPHS 1
 #endif
 
-// Host entry points write the compacted Frechet rows straight into the
-// caller's host arrays from the compaction kernel when those arrays are
-// page-locked memory mapped for the device (one pass over the link instead
-// of a device copy and a copy out); pageable arrays get the copy.
-#ifndef FM_ZERO_COPY_ROWS
-#define FM_ZERO_COPY_ROWS 1
-#endif
-// ... and read page-locked boundary frames through their device mapping with
-// a kernel instead of one copy-engine transfer
-#ifndef FM_STAGE_FRAMES
-#define FM_STAGE_FRAMES 1
-#endif
-
 // How a solve starts: from boundary frames (initialisation, sweep, rounds),
 // from the current fields (resume: rounds with every tile active), or from
 // point-source boxes the caller already wrote (rounds from the boxes' tiles).
@@ -1692,10 +1679,10 @@ static int rays_trace(fm3dt_ctx *ctx, DeviceScratch &sc, int nrc, const double *
 }
 
 // The address through which this device's kernels reach host memory at p,
-// or null when there is none (pageable memory, or the switch off).
+// or null when there is none (pageable memory).
 static void *mapped_host(const void *p)
 {
-    if (!FM_ZERO_COPY_ROWS || !p) return nullptr;
+    if (!p) return nullptr;
     cudaPointerAttributes at{};
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         (void)cudaGetLastError();
@@ -1704,13 +1691,62 @@ static void *mapped_host(const void *p)
     return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
-// A host entry point's boundary frames into ctx->d_frames: read by a kernel
-// through the device mapping when they are page-locked, else copied.
+// How a host forward call moves page-locked data over this host's link: a
+// kernel through the device mapping (*kernel = 1) or a copy-engine transfer
+// (0), whichever moved up to 64 MB of the call's own buffers faster (the
+// second of two tries of each; h2d: host -> dev, else dev -> host).  Hosts
+// differ: measured on GB300 machines, 30 GB/s by copy against ~150 GB/s by
+// kernel writes on one, 175 against 55 on another.  Transfers below 1 MB
+// take the copy.
+static int link_choice(fm3dt_ctx *ctx, double *dev, void *host, double *mapped, size_t bytes, bool h2d, int *kernel)
+{
+    *kernel = 0;
+    bytes = std::min(bytes, (size_t)64 << 20) & ~(size_t)15;
+    if (bytes < ((size_t)1 << 20)) return FM3DT_OK;
+    const size_t n = bytes / sizeof(double);
+    cudaStream_t s = ctx->stream;
+    cudaEvent_t ev[3];
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    struct EvGuard {
+        cudaEvent_t *e;
+        ~EvGuard() { for (int i = 0; i < 3; ++i) cudaEventDestroy(e[i]); }
+    } ev_guard{ev};
+    float tk = 0.0f, tc = 0.0f;
+    for (int rep = 0; rep < 2; ++rep) {
+        CK(cudaEventRecord(ev[0], s));
+        if (h2d)
+            launch_link_copy(mapped, dev, n, s);
+        else
+            launch_link_copy(dev, mapped, n, s);
+        ctx->launches += 1;
+        CKL();
+        CK(cudaEventRecord(ev[1], s));
+        CK(cudaMemcpyAsync(h2d ? (void *)dev : host, h2d ? host : (void *)dev, bytes,
+                           h2d ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, s));
+        CK(cudaEventRecord(ev[2], s));
+        CK(cudaStreamSynchronize(s));
+        CK(cudaEventElapsedTime(&tk, ev[0], ev[1]));
+        CK(cudaEventElapsedTime(&tc, ev[1], ev[2]));
+    }
+    *kernel = tk < tc ? 1 : 0;
+    return FM3DT_OK;
+}
+
+// A host forward call's boundary frames into ctx->d_frames: read by a kernel
+// through the device mapping when they are page-locked and the link favours
+// it, else copied.
 static int upload_frames(fm3dt_ctx *ctx, const double *boundary, int nev)
 {
     const size_t n = (size_t)nev * ctx->NB;
-    if (const double *m = FM_STAGE_FRAMES ? (const double *)mapped_host(boundary) : nullptr) {
-        launch_stage_frames(m, ctx->d_frames, n, ctx->stream);
+    const double *m = (const double *)mapped_host(boundary);
+    if (m && ctx->link_frames < 0) {
+        int k = 0;
+        const int rc = link_choice(ctx, ctx->d_frames, (void *)boundary, (double *)m, n * sizeof(double), true, &k);
+        if (rc != FM3DT_OK) return rc;
+        ctx->link_frames = k;
+    }
+    if (m && ctx->link_frames == 1) {
+        launch_link_copy(m, ctx->d_frames, n, ctx->stream);
         ctx->launches += 1;
         CKL();
         return FM3DT_OK;
@@ -1719,18 +1755,39 @@ static int upload_frames(fm3dt_ctx *ctx, const double *boundary, int nev)
     return FM3DT_OK;
 }
 
-// Compacted rows of a host entry point into the caller's cols/vals: written
-// there by the compaction kernel when both are mapped page-locked memory,
-// else compacted into the context's buffer and copied out on stream s.
+// Before a host forward call's rows exist: with page-locked cols and vals and
+// no choice made yet, how its rows will leave (ctx->link_rows), measured on
+// its own cols array (overwritten later) and device scratch.
+static int choose_rows_link(fm3dt_ctx *ctx, DeviceScratch &sc, int32_t *cols, float *vals, int64_t cap)
+{
+    if (ctx->link_rows >= 0 || cap <= 0) return FM3DT_OK;
+    double *m_cols = (double *)mapped_host(cols);
+    if (!m_cols || !mapped_host(vals)) return FM3DT_OK;
+    const size_t bytes = std::min((size_t)cap * sizeof(int32_t), (size_t)64 << 20) & ~(size_t)15;
+    if (bytes < ((size_t)1 << 20)) return FM3DT_OK;
+    if ((uintptr_t)cols % 16 != 0) return FM3DT_OK;
+    double *tmp = nullptr;
+    CK(sc.alloc(&tmp, bytes / sizeof(double)));
+    int k = 0;
+    const int rc = link_choice(ctx, tmp, (void *)cols, m_cols, bytes, false, &k);
+    if (rc != FM3DT_OK) return rc;
+    ctx->link_rows = k;
+    return FM3DT_OK;
+}
+
+// Compacted rows of a host entry point into the caller's cols/vals: compacted
+// into the context's buffer, then moved out by a kernel through the device
+// mapping when both arrays are page-locked (16-byte aligned) and the link
+// favours it, else by copy-engine transfers on stream s.
 static int rays_compact(fm3dt_ctx *ctx, const float *d_fdm, int nrows, const int64_t *d_row_ptr, int32_t *d_cols,
                         float *d_vals);
 static int rays_compact_to_host(fm3dt_ctx *ctx, const float *d_fdm, int nrows, const int64_t *d_rowptr,
                                 int64_t total, int32_t *cols, float *vals, cudaStream_t s)
 {
-    int32_t *m_cols = (int32_t *)mapped_host(cols);
-    float *m_vals = (float *)mapped_host(vals);
-    if (m_cols && m_vals) return rays_compact(ctx, d_fdm, nrows, d_rowptr, m_cols, m_vals);
-    const size_t need = (size_t)total * (sizeof(int32_t) + sizeof(float));
+    // (the values at a 256-byte boundary after the columns)
+    const size_t cbytes = (size_t)total * sizeof(int32_t), vbytes = (size_t)total * sizeof(float);
+    const size_t voff = (cbytes + 255) & ~(size_t)255;
+    const size_t need = voff + vbytes;
     if (need > ctx->compact_bytes) {
         CK(cudaStreamSynchronize(s));
         cudaFree(ctx->d_compact);
@@ -1740,11 +1797,19 @@ static int rays_compact_to_host(fm3dt_ctx *ctx, const float *d_fdm, int nrows, c
         ctx->compact_bytes = need;
     }
     int32_t *d_cols = (int32_t *)ctx->d_compact;
-    float *d_vals = (float *)((char *)ctx->d_compact + (size_t)total * sizeof(int32_t));
+    float *d_vals = (float *)((char *)ctx->d_compact + voff);
     const int rc = rays_compact(ctx, d_fdm, nrows, d_rowptr, d_cols, d_vals);
     if (rc != FM3DT_OK) return rc;
-    CK(cudaMemcpyAsync(cols, d_cols, (size_t)total * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(vals, d_vals, (size_t)total * sizeof(float), cudaMemcpyDeviceToHost, s));
+    void *m_cols = mapped_host(cols), *m_vals = mapped_host(vals);
+    if (m_cols && m_vals && ctx->link_rows == 1 && (uintptr_t)m_cols % 16 == 0 && (uintptr_t)m_vals % 16 == 0) {
+        launch_link_copy_bytes(d_cols, m_cols, cbytes, s);
+        launch_link_copy_bytes(d_vals, m_vals, vbytes, s);
+        ctx->launches += 2;
+        CKL();
+        return FM3DT_OK;
+    }
+    CK(cudaMemcpyAsync(cols, d_cols, cbytes, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(vals, d_vals, vbytes, cudaMemcpyDeviceToHost, s));
     return FM3DT_OK;
 }
 
@@ -2031,6 +2096,10 @@ int fm3dt_forward(fm3dt_ctx *ctx, int nev, const double *boundary, int nrc, cons
     }
     rc = upload_frames(ctx, boundary, nev);
     if (rc != FM3DT_OK) return rc;
+    if (want_rows && nrc > 0) {
+        rc = choose_rows_link(ctx, sc, cols, vals, cap);
+        if (rc != FM3DT_OK) return rc;
+    }
     int64_t total = 0;
     float *d_fdm = nullptr;
     rc = forward_common(ctx, sc, nev, nrc, d_rec, d_rec + nrc, d_rec + 2 * nrc, d_times, want_rows, d_end, d_rowptr,
@@ -2058,6 +2127,22 @@ int fm3dt_forward(fm3dt_ctx *ctx, int nev, const double *boundary, int nrc, cons
 int fm3dt_forward_early_events(const fm3dt_ctx *ctx)
 {
     return ctx ? ctx->early_events : 0;
+}
+
+int fm3dt_set_host_link(fm3dt_ctx *ctx, int mode)
+{
+    if (!ctx || mode < 0 || mode > 2) return FM3DT_EINVAL;
+    const int v = mode == 0 ? -1 : mode - 1;
+    ctx->link_frames = ctx->link_rows = v;
+    return FM3DT_OK;
+}
+
+int fm3dt_host_link(const fm3dt_ctx *ctx, int *frames, int *rows)
+{
+    if (!ctx || !frames || !rows) return FM3DT_EINVAL;
+    *frames = ctx->link_frames;
+    *rows = ctx->link_rows;
+    return FM3DT_OK;
 }
 
 int fm3dt_get_times(fm3dt_ctx *ctx, int event, double *ttn)

@@ -192,8 +192,11 @@ void launch_planewave_frames(const Geom &g, const PlaneWaveGeom &pg, int nev, co
 void launch_finalize_frames(const Geom &g, int nev, int prec, const double *frames, void *T,
                             uint8_t *frozen, double *base, cudaStream_t st);
 void launch_fill_inf(void *T, size_t n, int prec, cudaStream_t st);
-// n doubles from the device mapping of page-locked host memory into dst
-void launch_stage_frames(const double *mapped_src, double *dst, size_t n, cudaStream_t st);
+// n doubles between device memory and the device mapping of page-locked host
+// memory (either way round), by a kernel
+void launch_link_copy(const double *src, double *dst, size_t n, cudaStream_t st);
+// the same for `bytes` bytes between 16-byte aligned addresses
+void launch_link_copy_bytes(const void *src, void *dst, size_t bytes, cudaStream_t st);
 void launch_sweep_directions(const Geom &g, int nev, const double *frames, int *dir, double tie_ratio,
                              cudaStream_t st);
 // (events: the event of each of the nev entries; null = 0..nev-1)
@@ -402,6 +405,10 @@ struct fm3dt_ctx {
     float part_ms[4] = {};                   // the first round's two parts (fm3dt_part_ms)
     float rays_ms[4] = {};                   // the last host-buffer ray call's phases (fm3dt_rays_ms)
     int early_events = 0;                    // events whose rays the last forward call traced early
+    // how a host forward call moves page-locked frames in and rows out: through
+    // the device mapping by kernels (1) or by copy-engine transfers (0);
+    // -1 until measured on the context's first such call (fm3dt_set_host_link)
+    int link_frames = -1, link_rows = -1;
     // point sources: fixed node boxes, and the refined source grids' contexts
     int *d_box = nullptr;         // [maxev][6] fixed nodes
     int *d_box_init = nullptr;    // [maxev][6] nodes whose tiles start active

@@ -57,7 +57,8 @@ EXPORTS = [
     "fm3dt_ctx_create", "fm3dt_set_velocity", "fm3dt_solve", "fm3dt_solve_device", "fm3dt_solve_resume",
     "fm3dt_solve_planewave", "fm3dt_solve_point",
     "fm3dt_receiver_times", "fm3dt_rays_frechet", "fm3dt_receiver_times_device", "fm3dt_rays_frechet_device",
-    "fm3dt_forward", "fm3dt_forward_device", "fm3dt_forward_early_events", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
+    "fm3dt_forward", "fm3dt_forward_device", "fm3dt_forward_early_events", "fm3dt_set_host_link",
+    "fm3dt_host_link", "fm3dt_get_times", "fm3dt_get_velocity", "fm3dt_set_times",
     "fm3dt_set_tuning", "fm3dt_set_schedule", "fm3dt_set_sweep_shape", "fm3dt_set_sweep_segments", "fm3dt_round_trace", "fm3dt_round_trace_ms", "fm3dt_part_ms", "fm3dt_rays_ms", "fm3dt_tie_sweep_items", "fm3dt_tie_sweep_ms", "fm3dt_tile_shapes", "fm3dt_tile_shape",
     "fm3dt_launch_count",
     "fm3dt_last_error", "fm3dt_ctx_destroy",
@@ -95,6 +96,8 @@ def load(path: str | None = None):
     L.fm3dt_forward_device.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_int64,
                                        C.POINTER(C.c_int64), vp, C.POINTER(Status)]
     L.fm3dt_forward_early_events.argtypes = [vp]
+    L.fm3dt_set_host_link.argtypes = [vp, C.c_int]
+    L.fm3dt_host_link.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.fm3dt_get_times.argtypes = [vp, C.c_int, dp]
     L.fm3dt_set_times.argtypes = [vp, C.c_int, C.c_int, dp]
     L.fm3dt_get_velocity.argtypes = [vp, dp]
@@ -485,6 +488,18 @@ class Solver:
             C.cast(C.c_void_p(vals_ptr), C.POINTER(C.c_float)), int(cap), None, C.byref(st)))
         self.nev = int(nev)
         return int(C.cast(C.c_void_p(row_ptr_ptr + 8 * self.nev * len(rcr)), C.POINTER(C.c_int64))[0])
+
+    def set_host_link(self, mode: int):
+        """How forward calls move page-locked host buffers: 0 measure on the
+        next call, 1 copies, 2 kernels through the device mapping."""
+        self._check(self._L.fm3dt_set_host_link(self._ctx, int(mode)))
+
+    def host_link(self) -> tuple[int, int]:
+        """The current choice for (frames, rows): -1 not measured, 0
+        copies, 1 device mapping."""
+        f, r = C.c_int(), C.c_int()
+        self._check(self._L.fm3dt_host_link(self._ctx, C.byref(f), C.byref(r)))
+        return f.value, r.value
 
     @property
     def forward_early_events(self) -> int:

@@ -576,11 +576,23 @@ def test_forward_equals_three_calls(gpu_lib, nev):
         h_rp = torch.zeros(nev * nrc + 1, dtype=torch.int64).pin_memory()
         h_c = torch.zeros(cap, dtype=torch.int32).pin_memory()
         h_v = torch.zeros(cap, dtype=torch.float32).pin_memory()
-        n = s.forward_into(nev, h_fr.data_ptr(), rcr, rcx, rcz, h_t.data_ptr(), h_rp.data_ptr(), h_c.data_ptr(),
-                           h_v.data_ptr(), cap)
-        assert n == cap
-        assert np.array_equal(h_t.numpy(), t_ref) and np.array_equal(h_rp.numpy(), rp_ref)
-        assert np.array_equal(h_c.numpy(), c_ref) and np.array_equal(h_v.numpy(), v_ref)
+        # (measured choice, then each way forced)
+        assert s.host_link() == (-1, -1)
+        for mode in (0, 2, 1):
+            s.set_host_link(mode) if mode else None
+            for h in (h_t, h_rp, h_c, h_v):
+                h.zero_()
+            n = s.forward_into(nev, h_fr.data_ptr(), rcr, rcx, rcz, h_t.data_ptr(), h_rp.data_ptr(),
+                               h_c.data_ptr(), h_v.data_ptr(), cap)
+            assert n == cap
+            assert np.array_equal(h_t.numpy(), t_ref) and np.array_equal(h_rp.numpy(), rp_ref)
+            assert np.array_equal(h_c.numpy(), c_ref) and np.array_equal(h_v.numpy(), v_ref)
+            frames_link, rows_link = s.host_link()
+            if mode == 0:
+                assert frames_link in (0, 1) and rows_link in (-1, 0, 1)
+                print(f"\nhost link measured: frames {frames_link}, rows {rows_link}")
+            else:
+                assert (frames_link, rows_link) == ((1, 1) if mode == 2 else (0, 0))
         # too small a capacity: ERANGE with the required count
         with pytest.raises(fm3dt.Fm3dtError) as ei:
             s.forward_device(nev, d_frames.data_ptr(), nrc, *[x.data_ptr() for x in d_rec], d_times.data_ptr(),
