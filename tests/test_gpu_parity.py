@@ -579,7 +579,8 @@ def test_forward_equals_three_calls(gpu_lib, nev):
         # (measured choice, then each way forced)
         assert s.host_link() == (-1, -1)
         for mode in (0, 2, 1):
-            s.set_host_link(mode) if mode else None
+            if mode:
+                s.set_host_link(mode)
             for h in (h_t, h_rp, h_c, h_v):
                 h.zero_()
             n = s.forward_into(nev, h_fr.data_ptr(), rcr, rcx, rcz, h_t.data_ptr(), h_rp.data_ptr(),
