@@ -101,3 +101,19 @@ def test_latlon_conversion_matches_oracle(orc):
     a = fm3dt.latlon_to_rad(lat, lon)
     b = orc.latlon_to_rad(lat, lon)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_forward_entry_points_reject_a_null_context(gpu_lib):
+    """The one-call forward step and its host-link switch check their
+    arguments before any device work (callable without a GPU)."""
+    import ctypes as C
+    import fm3dt
+    L = gpu_lib
+    st = fm3dt.Status()
+    assert L.fm3dt_forward(None, 1, None, 0, None, None, None, None, None, None, None, 0, None, C.byref(st)) == fm3dt.EINVAL
+    assert L.fm3dt_forward_device(None, 1, None, 0, None, None, None, None, None, None, None, 0, None, None,
+                                  C.byref(st)) == fm3dt.EINVAL
+    assert L.fm3dt_set_host_link(None, 0) == fm3dt.EINVAL
+    f, r = C.c_int(), C.c_int()
+    assert L.fm3dt_host_link(None, C.byref(f), C.byref(r)) == fm3dt.EINVAL
+    assert L.fm3dt_forward_early_events(None) == 0
